@@ -1,0 +1,357 @@
+#!/usr/bin/env python3
+"""Benchmark of the local RBF-FD hot path on one GB300 (or N independent replicas).
+
+Workload (default): 3D Laplacian, N = 4,000,000 points i.i.d. uniform in [0,1]^3 (seeded),
+PHS(3) with degree-2 polynomials (10 monomials), k = 30 (40x40 saddle-point systems).
+A step is one pass of the hot path over the cloud: k-NN stencils, the weight build
+(assembly + solve + scatter into CSR) and one apply of the operator to a field.
+
+  value  : stencils built per second over the whole job (all ranks), device-resident inputs
+  e2e    : the same metric through the public API with host inputs and a host result
+           (points and field copied in, Laplacian of the field copied out, every step)
+
+The headline build is the FP32-factorised, FP64-refined solve; the plain FP64 build is
+timed beside it and the max row-relative weight difference between them is reported
+(equal-error requirement: <= 1e-8).  `--impl reference` times the CPU oracle (a C
+restatement of the reference algorithm: grid kNN + raw-coordinate assembly + rook
+Bunch-Kaufman, OpenMP on all host cores) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "stencils/s built (learned+FP32-refined vs plain FP64, equal err); apply GB/s"
+
+CONFIGS = {
+    # name: (dim, N, phs, poly_deg, k, ops, field description)
+    "lap3d_4M": dict(dim=3, n=4_000_000, phs=3, deg=2, k=30, ops=[(3, 0)], dist="uniform",
+                     desc="3D Laplacian, N=4,000,000 uniform in [0,1]^3, PHS3 deg 2, k=30 (40x40 systems)"),
+    "lap2d_10k": dict(dim=2, n=10_000, phs=3, deg=2, k=20, ops=[(3, 0)], dist="uniform",
+                      desc="2D Laplacian, N=10,000 uniform in [0,1]^2, PHS3 deg 2, k=20 (26x26 systems)"),
+    "gradlap3d_1M": dict(dim=3, n=1_000_000, phs=5, deg=2, k=40, ops=[(1, 0), (1, 1), (1, 2), (3, 0)],
+                         dist="lattice", desc="3D gradient+Laplacian, 100^3 jittered lattice, PHS5 deg 2, k=40"),
+}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--config", default="lap3d_4M", choices=sorted(CONFIGS))
+    p.add_argument("--n", type=int, default=0, help="override the point count (development runs)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample", type=int, default=0, help="stencils in the CPU baseline sample")
+    return p.parse_args()
+
+
+def make_points(cfg, n, seed, torch=None, device=None):
+    rng = np.random.default_rng(seed)
+    if cfg["dist"] == "uniform":
+        X = rng.uniform(0.0, 1.0, (n, cfg["dim"]))
+    else:
+        m = round(n ** (1.0 / cfg["dim"]))
+        g = np.stack(np.meshgrid(*[np.arange(m)] * cfg["dim"], indexing="ij"), -1).reshape(-1, cfg["dim"])
+        X = (g + 0.5 + rng.uniform(-0.3, 0.3, g.shape)) / m
+    return X
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def row_rel_err_torch(torch, row_ptr, k, v, vref):
+    ne = row_ptr.numel() - 1
+    d = (v - vref).abs().reshape(ne, k).amax(1)
+    s = vref.abs().reshape(ne, k).amax(1).clamp_min(1e-300)
+    return float((d / s).max())
+
+
+def cpu_baseline(cfg, n, sample, steps=1):
+    """The oracle (C restatement of the reference algorithm) on host cores, bounded sample."""
+    from oracle import oracle as O
+    X = make_points(cfg, n, 12345)
+    q = X[:sample]
+    t0 = time.perf_counter()
+    adjl = O.knn(X, q, cfg["k"])
+    t1 = time.perf_counter()
+    O.build(X, q, adjl, cfg["dim"], cfg["phs"], cfg["deg"], cfg["ops"])
+    t2 = time.perf_counter()
+    return {"stencils_per_s": sample / (t2 - t0), "knn_s": t1 - t0, "build_s": t2 - t1,
+            "cores": O.num_threads(), "sample": sample}
+
+
+def run_reference(args, cfg, n):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sample = args.cpu_sample or (200_000 if cfg["n"] >= 1_000_000 else n)
+    times = []
+    res = None
+    for s in range(args.warmup + args.steps):
+        res = cpu_baseline(cfg, n, sample)
+        if s >= args.warmup:
+            times.append(sample / res["stencils_per_s"])
+    v = sample * len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "stencils/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": cfg["desc"], "sample_stencils": sample},
+        "cpu_baseline": {"value": v, "unit": "stencils/s", "cores": res["cores"], "kind": "port",
+                         "sample": f"{sample} stencils (kNN over all {n} points + build) per step"},
+        "e2e": {"value": v, "unit": "stencils/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference Julia path: unavailable on this box (no Julia); CPU oracle timed instead",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    cfg = CONFIGS[args.config]
+    n = args.n or cfg["n"]
+    if args.impl == "reference":
+        run_reference(args, cfg, n)
+        return
+
+    import torch
+    import torch.distributed as dist
+    import __graft_entry__ as g
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    g.build()
+    pkg = g.load_package()
+    ctx = pkg.Context.default(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    dev = torch.device("cuda", local)
+
+    # independent seeded cloud per rank (weak scaling: per-GPU work fixed)
+    X_h = make_points(cfg, n, 1000 + rank)
+    Xd = torch.from_numpy(X_h).to(dev)
+    f_h = np.sin(4 * X_h[:, 0]) * np.cos(3 * X_h[:, 1]) * (np.exp(X_h[:, 2]) if cfg["dim"] == 3 else 1.0)
+    fd = torch.from_numpy(f_h).to(dev)
+    basis = pkg.PHS(cfg["phs"], poly_deg=cfg["deg"])
+    k = cfg["k"]
+
+    def step(precision, X=Xd, f=fd):
+        adjl = pkg.find_neighbors(X, k=k, ctx=ctx)
+        Ws = pkg.build_weights(cfg["ops"], X, None, adjl, basis, precision=precision, ctx=ctx)
+        y = Ws[-1].apply(f)
+        return adjl, Ws, y
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+            torch.cuda.synchronize()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    headline = "fp32_refined"
+    launches0 = ctx.lib.rbf_ctx_kernel_launches(ctx.handle)
+    clocks = ClockSampler(local)
+    # ---- headline timed region
+    for _ in range(args.warmup):
+        step(headline)
+    barrier()
+    launches0 = ctx.lib.rbf_ctx_kernel_launches(ctx.handle)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step(headline)
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = (ctx.lib.rbf_ctx_kernel_launches(ctx.handle) - launches0) // args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * world / (ms * 1e-3)
+
+    # ---- plain FP64 beside it, same workload
+    ms_fp64 = timed(lambda: step("fp64"), max(1, args.steps // 2), 1)
+    # ---- equal-error check: refined vs plain GPU weights, max row-relative difference
+    adjl = pkg.find_neighbors(Xd, k=k, ctx=ctx)
+    W64 = pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision="fp64", ctx=ctx)
+    st = pkg._native.BuildStats()
+    W32 = pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision=headline, ctx=ctx, stats=st)
+    err = max(row_rel_err_torch(torch, a.row_ptr, k, a.val, b.val) for a, b in zip(W32, W64))
+    n_fallback = int(st.n_fallback)
+    # ---- per-kernel timings (device-resident, events on the launching stream)
+    st64 = pkg._native.BuildStats()
+    pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision="fp64", ctx=ctx, stats=st64)
+    ms_build32 = float(st.ms_build)
+    ms_build64 = float(st64.ms_build)
+    ms_knn = timed(lambda: pkg.find_neighbors(Xd, k=k, ctx=ctx), 3, 1)
+    W = W32[-1]
+    y = torch.empty(n, dtype=torch.float64, device=dev)
+    ms_spmv = timed(lambda: W.apply(fd), 10, 3)
+    nnz = W.nnz
+    apply_bytes = nnz * 12 + (n + 1) * 8 + 2 * n * 8
+    apply_gbs = apply_bytes / (ms_spmv * 1e-3) / 1e9
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm_src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in peaks else "fallback"
+    fp64_peak = pkg.ctypes.c_double(0.0)
+    ctx.check(ctx.lib.rbf_diag_fma_peak(ctx.handle, 1, pkg.ctypes.byref(fp64_peak)))
+    fp32_peak = pkg.ctypes.c_double(0.0)
+    ctx.check(ctx.lib.rbf_diag_fma_peak(ctx.handle, 0, pkg.ctypes.byref(fp32_peak)))
+    nsys = k + math.comb(cfg["deg"] + cfg["dim"], cfg["dim"])
+    R = len(cfg["ops"])
+    # algorithmic FLOPs of the reference algorithm per stencil: symmetric factor n^3/3,
+    # solve 2 n^2 R, assembly ~10 flops per phi / L(phi) evaluation
+    flops_stencil = nsys ** 3 / 3 + 2 * nsys ** 2 * R + 10 * (k * (k + 1) / 2 + R * k)
+    kernels = {"knn_query": ms_knn, "build_fp32r": ms_build32, "spmv": ms_spmv}
+    dom = max(kernels, key=kernels.get)
+    if dom == "spmv":
+        roof = {"kernel": "spmv_kernel", "bound": "hbm", "achieved": apply_gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": apply_gbs / hbm_peak, "traffic": None, "peak_source": hbm_src}
+    elif dom == "build_fp32r":
+        ach = flops_stencil * n / (ms_build32 * 1e-3) / 1e12
+        roof = {"kernel": "build_fp32r_kernel", "bound": "fp32 pipe", "achieved": ach, "peak": fp32_peak.value,
+                "unit": "TFLOP/s", "frac": ach / fp32_peak.value, "traffic": None,
+                "peak_source": "FFMA loop measured in this run (rbf_diag_fma_peak)",
+                "flops_per_stencil": flops_stencil}
+    else:
+        kb = (2 * n * cfg["dim"] * 8 + n * k * 4)
+        ach = kb / (ms_knn * 1e-3) / 1e9
+        roof = {"kernel": "knn (grid build + knn_query_kernel)", "bound": "hbm", "achieved": ach, "peak": hbm_peak,
+                "unit": "GB/s", "frac": ach / hbm_peak, "traffic": None, "peak_source": hbm_src}
+
+    # ---- e2e through the public API: host points in, host Laplacian of a host field out
+    X_pin = torch.from_numpy(X_h).pin_memory()
+    f_pin = torch.from_numpy(f_h).pin_memory()
+    y_pin = torch.empty(n, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        Xg = X_pin.to(dev, non_blocking=True)
+        adj = pkg.find_neighbors(Xg, k=k, ctx=ctx)
+        Ws = pkg.build_weights(cfg["ops"], Xg, None, adj, basis, precision=headline, ctx=ctx)
+        yy = Ws[-1].apply(f_pin.to(dev, non_blocking=True))
+        y_pin.copy_(yy, non_blocking=True)
+
+    ms_e2e = timed(e2e_step, max(1, args.steps // 2), 1)
+    e2e = {"value": n * world / (ms_e2e * 1e-3), "unit": "stencils/s", "h2d_bytes_per_step": n * cfg["dim"] * 8 + n * 8,
+           "d2h_bytes_per_step": n * 8}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sample = args.cpu_sample or (200_000 if n >= 1_000_000 else n)
+        cb = cpu_baseline(cfg, n, sample)
+        cpu = {"value": cb["stencils_per_s"], "unit": "stencils/s", "cores": cb["cores"], "kind": "port",
+               "sample": f"{sample} stencils: grid kNN over all {n} points + raw-coordinate rook-BK build"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "stencils/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 factor + f64 refinement", "data": "synthetic (seeded)",
+            "config": {"workload": cfg["desc"], "n": n, "k": k, "step": "kNN + build (CSR) + one apply",
+                       "l2": "inputs larger than L2 (CSR 12 B/nnz x nnz, adjacency 4 B x N x k)",
+                       "parallelism": f"replicas x{world}"},
+            "plain_fp64": {"value": n * world / (ms_fp64 * 1e-3), "unit": "stencils/s", "ms_per_step": ms_fp64},
+            "speedup_vs_plain_fp64": ms_fp64 / ms,
+            "equal_error": {"max_row_rel_weight_diff_vs_fp64": err, "bar": 1e-8, "fallback_stencils": n_fallback},
+            "apply": {"value": apply_gbs, "unit": "GB/s", "ms": ms_spmv, "nnz": nnz,
+                      "frac_of_hbm": apply_gbs / hbm_peak},
+            "kernels_ms": {"knn": ms_knn, "build_fp32r": ms_build32, "build_fp64": ms_build64, "spmv": ms_spmv},
+            "peaks": {"fp64_tflops_measured": fp64_peak.value, "fp32_tflops_measured": fp32_peak.value,
+                      "hbm_gbs": hbm_peak},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

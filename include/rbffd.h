@@ -1,0 +1,165 @@
+/*
+ * rbffd.h -- C ABI of the GB300 (sm_103a) local RBF-FD library.
+ *
+ * One shared library (librbffd_gb300.so) exposes the hot path of
+ * RadialBasisFunctions.jl's local RBF-FD operators as plain C entry points:
+ * k-nearest-neighbour stencils, per-stencil assembly + dense solve, scatter into
+ * sparse rows (CSR), and the sparse apply.  Every entry point returns an int status
+ * (RBF_OK = 0, negative = error; the message is in rbf_last_error()).
+ *
+ * Pointers: every array argument may be a host pointer (pageable or pinned) or a
+ * device pointer of the context's GPU; the library detects which and copies host
+ * data through the context's stream.  Calls are stream-ordered on the context's
+ * stream and return after the result is complete (host outputs are written, device
+ * outputs are ready to use on that stream).
+ *
+ * Indices are 0-based int32 (point counts < 2^31).  Points are AoS doubles
+ * (dim values per point, the memory layout of Vector{SVector{dim,Float64}}).
+ */
+#ifndef RBFFD_H
+#define RBFFD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define RBF_OK 0
+#define RBF_ERR_ARGUMENT -1        /* ArgumentError in the reference              */
+#define RBF_ERR_DIMENSION -2       /* DimensionMismatch in the reference          */
+#define RBF_ERR_CUDA -3            /* CUDA runtime error                          */
+#define RBF_ERR_SINGULAR -4        /* a stencil system is exactly singular        */
+#define RBF_ERR_UNSUPPORTED -5     /* combination not supported (e.g. no normal form) */
+#define RBF_ERR_NOT_FOUND -6       /* Hermite eval point absent from its stencil  */
+#define RBF_ERR_INTERNAL -7
+
+/* ---- operator and precision vocabulary ----------------------------------- */
+enum rbf_op_code {
+    RBF_OP_IDENTITY = 0,  /* Regrid()(basis) = basis           (operators/regridding.jl:7)  */
+    RBF_OP_PARTIAL1 = 1,  /* Partial(1, dim) / one entry of Jacobian (operators/partial.jl) */
+    RBF_OP_PARTIAL2 = 2,  /* Partial(2, dim)                                                */
+    RBF_OP_LAPLACIAN = 3  /* Laplacian()                       (operators/laplacian.jl:7)   */
+};
+
+enum rbf_precision {
+    RBF_PREC_FP64 = 0,          /* plain FP64 solve (the oracle-matched drop-in)            */
+    RBF_PREC_FP32_REFINED = 1,  /* FP32 factor + FP64-residual iterative refinement         */
+    RBF_PREC_LEARNED = 2        /* learned seed + FP32 refinement, FP64 fallback            */
+};
+
+#define RBF_MAX_OPS 8
+#define RBF_MAX_STENCIL 64   /* k <= 64 */
+#define RBF_MAX_SYSTEM 80    /* k + nmon <= 80 */
+
+/* Build configuration: basis, augmentation, the operators that share one
+ * factorisation (one right-hand side each), and the solve precision. */
+typedef struct rbf_build_cfg {
+    int32_t dim;                  /* 1, 2 or 3                                      */
+    int32_t phs;                  /* PHS order: 1, 3, 5 or 7                        */
+    int32_t poly_deg;             /* -1 (none) .. 4                                 */
+    int32_t nops;                 /* 1 .. RBF_MAX_OPS                               */
+    int32_t op_code[RBF_MAX_OPS]; /* enum rbf_op_code                               */
+    int32_t op_dim[RBF_MAX_OPS];  /* 0-based dimension of partial derivatives       */
+    int32_t precision;            /* enum rbf_precision                             */
+    int32_t refine_steps;         /* max refinement steps for FP32 paths (0: default 3) */
+    double tol;                   /* FP32 paths: accept when the FP64 residual, relative
+                                     to the right-hand side, is below tol (0: default 1e-12) */
+} rbf_build_cfg;
+
+/* Hermite boundary description (src/solve/types.jl:18-42,178-182).  Boundary
+ * conditions are B u = alpha*u + beta*du/dn; Dirichlet is (1,0), Neumann (0,1).
+ * alpha/beta/normals are indexed by boundary ordinal (the i-th point with
+ * is_boundary set), as the reference's global_to_boundary map does. */
+typedef struct rbf_hermite {
+    const uint8_t *is_boundary; /* one flag per data point                          */
+    const double *alpha;        /* n_boundary                                       */
+    const double *beta;         /* n_boundary                                       */
+    const double *normals;      /* n_boundary x dim (AoS)                           */
+    int64_t n_boundary;
+} rbf_hermite;
+
+/* Per-build statistics (optional output). */
+typedef struct rbf_build_stats {
+    int64_t n_stencils;      /* eval rows solved (Dirichlet identity rows excluded) */
+    int64_t n_identity_rows; /* Dirichlet eval rows                                 */
+    int64_t n_fallback;      /* FP32 paths: stencils that fell back to the FP64 solve */
+    int64_t n_singular;      /* stencils with an exactly singular system            */
+    double max_residual;     /* FP32 paths: largest accepted relative FP64 residual   */
+    float ms_knn, ms_build, ms_total;
+} rbf_build_stats;
+
+typedef struct rbf_ctx rbf_ctx;
+
+/* ---- context -------------------------------------------------------------- */
+/* Create a context on CUDA device `device` with its own non-blocking stream.
+ * Replaces the reference's device keyword / KernelAbstractions backend
+ * (src/operators/operators.jl:117-126, src/solve/execution.jl:140-148). */
+int rbf_ctx_create(int device, rbf_ctx **out);
+int rbf_ctx_destroy(rbf_ctx *ctx);
+/* Run on a caller-owned cudaStream_t (e.g. the stream of a Julia task or a torch
+ * stream); NULL restores the context's own stream. */
+int rbf_ctx_set_stream(rbf_ctx *ctx, void *cuda_stream);
+const char *rbf_last_error(const rbf_ctx *ctx);
+const char *rbf_version(void);
+
+/* ---- k nearest neighbours ------------------------------------------------- */
+/* Replaces find_neighbors(data, eval_points, k), src/utils.jl:12-18
+ * (NearestNeighbors.KDTree + knn(tree, eval, k, true)).  idx_out is ne x k
+ * (row-major), each row sorted by ascending distance, exact ties broken by the
+ * smaller point index (self first when eval == data). */
+int rbf_knn(rbf_ctx *ctx, const double *data, int64_t ns, const double *eval, int64_t ne,
+            int32_t dim, int32_t k, int32_t *idx_out);
+
+/* ---- weight build ---------------------------------------------------------- */
+/* Exact row layout of the sparse weights: row_ptr_out[ne+1] (int64, 0-based) and
+ * the total number of stored entries.  Interior and Neumann/Robin eval rows hold
+ * k entries, Dirichlet eval rows hold 1 (src/solve/execution.jl:16-69).
+ * herm may be NULL (no boundary). */
+int rbf_build_count(rbf_ctx *ctx, int64_t ns, int64_t ne, int32_t k, const rbf_hermite *herm,
+                    int64_t *row_ptr_out, int64_t *nnz_out);
+
+/* Build the weights of cfg->nops operators on the stencils adjl (ne x k, 0-based).
+ * Replaces _build_weights(ℒ, data, eval_points, adjl, basis; device)
+ * (src/solve/api.jl:26-35, and its Hermite twin api.jl:167-196) down to
+ * build_weights_kernel (src/solve/execution.jl:128-174).  The result is
+ * cfg->nops CSR matrices (ne x ns) sharing one structure: row_ptr (from
+ * rbf_build_count), col[nnz] with columns ascending within each row, and
+ * val[op * nnz + p].  status_out (optional, ne int8): 0 solved, 1 singular,
+ * 2 Dirichlet identity row, 3 solved by the FP64 fallback of an FP32 path.
+ * Returns RBF_ERR_SINGULAR if any stencil is singular (the reference raises
+ * from bunchkaufman!, src/solve/assembly.jl:220-222). */
+int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns,
+              const double *eval, int64_t ne, const int32_t *adjl, int32_t k,
+              const rbf_hermite *herm, const int64_t *row_ptr, int32_t *col, double *val,
+              int8_t *status_out, rbf_build_stats *stats);
+
+/* ---- apply ------------------------------------------------------------------ */
+/* Y = alpha * W X + beta * Y for nf fields, W the op_index-th operator of a built
+ * CSR (ne x ns).  Replaces _eval_op / mul! (src/operators/operators.jl:217-218,
+ * 529-542).  layout 0: column-major (field f of X at X[f*ldx + i], the layout of a
+ * Julia Matrix); layout 1: interleaved (X[i*ldx + f]).  beta == 0 ignores Y. */
+int rbf_spmm(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const int32_t *col,
+             const double *val, int32_t nf, int32_t layout, const double *X, int64_t ldx,
+             double alpha, double beta, double *Y, int64_t ldy);
+
+/* Transpose a built CSR (ne x ns) into CSC form: col_ptr_out[ns+1], row_out[nnz],
+ * val_out[nnz] -- the SparseMatrixCSC layout the reference returns
+ * (src/solve/execution.jl:105-115).  Rows within a column are ascending. */
+int rbf_csr_to_csc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr,
+                   const int32_t *col, const double *val, int64_t *col_ptr_out,
+                   int32_t *row_out, double *val_out);
+
+/* ---- diagnostics (no counterpart in the reference) ------------------------ */
+/* Measured FMA throughput of the context's GPU in TFLOP/s (fp64 != 0: FP64,
+ * else FP32), used as the roofline denominator of the build kernels. */
+int rbf_diag_fma_peak(rbf_ctx *ctx, int32_t fp64, double *tflops);
+/* Number of kernels this context has launched so far. */
+int64_t rbf_ctx_kernel_launches(const rbf_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RBFFD_H */

@@ -1,0 +1,622 @@
+"""GB300-native local RBF-FD operators with the interface of RadialBasisFunctions.jl.
+
+Host-side mirror of the reference's operator API for the local RBF-FD hot path
+(RadialBasisFunctions.jl v0.7.0).  Every compute step runs in librbffd_gb300.so
+(hand-written sm_103a CUDA behind the C ABI of include/rbffd.h); this module only
+validates arguments, owns device buffers (through torch) and maps errors to the
+reference's exception classes.  There is no CPU fallback.
+
+Reference surface mirrored here (file:line in the reference):
+  PHS / PHS1 / PHS3 / PHS5 / PHS7         src/basis/polyharmonic_spline.jl:21-34,43-305
+  BoundaryCondition, Dirichlet, Neumann,
+  Robin, Internal                         src/solve/types.jl:18-42
+  find_neighbors, autoselect_k            src/utils.jl:5-18,39-43
+  Laplacian, Partial, Jacobian, Regrid    src/operators/{laplacian,partial,jacobian,regridding}.jl
+  laplacian, partial, gradient, jacobian,
+  regrid                                  same files
+  RadialBasisOperator (+ call, weights,
+  update_weights, mul)                    src/operators/operators.jl:50-186,529-602
+
+Indices (neighbour lists, sparse rows) are 0-based.  The `dim` argument of `partial`
+keeps the reference's meaning and numbering (1-based dimension index).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+from typing import Sequence
+
+import numpy as np
+
+from . import _native
+
+__all__ = [
+    "PHS", "PHS1", "PHS3", "PHS5", "PHS7", "BoundaryCondition", "Dirichlet", "Neumann", "Robin", "Internal",
+    "find_neighbors", "autoselect_k", "Laplacian", "Partial", "Jacobian", "Regrid", "Operators",
+    "laplacian", "partial", "gradient", "jacobian", "regrid", "RadialBasisOperator", "WeightsCSR",
+    "weights", "update_weights", "mul", "DimensionMismatch", "SingularException", "Context", "build_library",
+]
+
+build_library = _native.build_library
+
+OP_IDENTITY, OP_PARTIAL1, OP_PARTIAL2, OP_LAPLACIAN = 0, 1, 2, 3
+PRECISIONS = {"fp64": 0, "fp32_refined": 1, "learned": 2}
+
+
+class DimensionMismatch(ValueError):
+    """The reference's DimensionMismatch."""
+
+
+class SingularException(np.linalg.LinAlgError):
+    """A stencil's saddle-point system is exactly singular (LAPACK info > 0 in the reference)."""
+
+
+def _raise(code: int, msg: str):
+    if code == -1:
+        raise ValueError(msg)
+    if code == -2:
+        raise DimensionMismatch(msg)
+    if code == -4:
+        raise SingularException(msg)
+    if code == -5:
+        raise ValueError(msg)
+    if code == -6:
+        raise ValueError(msg)
+    raise RuntimeError(f"librbffd_gb300 error {code}: {msg}")
+
+
+# ------------------------------------------------------------------------------ context
+class Context:
+    """One CUDA context handle of the library (a device + a stream)."""
+
+    _default: dict = {}
+
+    def __init__(self, device: int = 0):
+        self.lib = _native.load()
+        h = ctypes.c_void_p()
+        st = self.lib.rbf_ctx_create(device, ctypes.byref(h))
+        if st != 0:
+            raise RuntimeError(f"rbf_ctx_create({device}) failed with {st}: no usable CUDA device")
+        self.handle = h
+        self.device = device
+
+    @classmethod
+    def default(cls, device: int = 0) -> "Context":
+        ctx = cls._default.get(device)
+        if ctx is None:
+            ctx = cls._default[device] = Context(device)
+        return ctx
+
+    def check(self, st: int):
+        if st != 0:
+            _raise(st, self.lib.rbf_last_error(self.handle).decode())
+
+    def set_stream(self, stream_handle: int | None):
+        self.check(self.lib.rbf_ctx_set_stream(self.handle, ctypes.c_void_p(stream_handle or 0)))
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self.lib.rbf_ctx_destroy(self.handle)
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------------------ arrays
+def _torch():
+    import torch
+    return torch
+
+
+def _is_torch(x):
+    try:
+        import torch
+        return isinstance(x, torch.Tensor)
+    except ImportError:
+        return False
+
+
+def _points(x, name="data"):
+    """(N, dim) float64 array: numpy (host) or torch (host or cuda), C-contiguous."""
+    if _is_torch(x):
+        t = x.detach()
+        if t.dtype != _torch().float64:
+            t = t.to(_torch().float64)
+        t = t.contiguous()
+        if t.ndim == 1:
+            t = t.reshape(-1, 1)
+        return t
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    if a.ndim == 1:
+        a = a.reshape(-1, 1)
+    if a.ndim != 2:
+        raise ValueError(f"{name} must be an (N, dim) array of points")
+    return a
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_torch(a):
+        return ctypes.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _to_device(a, ctx):
+    torch = _torch()
+    if _is_torch(a):
+        return a.to(torch.device("cuda", ctx.device), torch.float64).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(torch.device("cuda", ctx.device))
+
+
+def _device_of(*arrays):
+    for a in arrays:
+        if _is_torch(a) and a.is_cuda:
+            return a.device.index or 0
+    return 0
+
+
+# ------------------------------------------------------------------------------ bases
+@dataclass(frozen=True)
+class _PHSBase:
+    poly_deg: int = 2
+    order: int = 3
+
+    def __post_init__(self):
+        check_poly_deg(self.poly_deg)
+
+    def __repr__(self):
+        sup = {1: "¹", 3: "³", 5: "⁵", 7: "⁷"}[self.order]
+        return f"Polyharmonic spline (r{sup})\n└─Polynomial augmentation: degree {self.poly_deg}"
+
+
+class PHS1(_PHSBase):
+    def __init__(self, poly_deg: int = 2):
+        super().__init__(poly_deg, 1)
+
+
+class PHS3(_PHSBase):
+    def __init__(self, poly_deg: int = 2):
+        super().__init__(poly_deg, 3)
+
+
+class PHS5(_PHSBase):
+    def __init__(self, poly_deg: int = 2):
+        super().__init__(poly_deg, 5)
+
+
+class PHS7(_PHSBase):
+    def __init__(self, poly_deg: int = 2):
+        super().__init__(poly_deg, 7)
+
+
+def check_poly_deg(poly_deg: int):
+    """src/utils.jl:57-66"""
+    if poly_deg < -1:
+        raise ValueError(f"poly_deg must be >= -1 (got {poly_deg}). Use poly_deg=2 (default) for quadratic, "
+                         "poly_deg=0 for constant, or poly_deg=-1 to disable polynomial augmentation.")
+
+
+def PHS(n: int = 3, poly_deg: int = 2):
+    """Polyharmonic spline r^n with degree-poly_deg augmentation (polyharmonic_spline.jl:21-34)."""
+    check_poly_deg(poly_deg)
+    if n % 2 == 0 or n > 7 or n < 1:
+        raise ValueError(f"n must be 1, 3, 5, or 7 (got n={n}). Use PHS(3) for cubic or PHS(5) for quintic.")
+    return {1: PHS1, 3: PHS3, 5: PHS5, 7: PHS7}[n](poly_deg)
+
+
+# ------------------------------------------------------------------------------ boundary conditions
+@dataclass(frozen=True)
+class BoundaryCondition:
+    """B u = alpha*u + beta*du/dn (src/solve/types.jl:18-42)."""
+    alpha: float
+    beta: float
+
+    def is_dirichlet(self):
+        return self.alpha == 1 and self.beta == 0
+
+    def is_neumann(self):
+        return self.alpha == 0 and self.beta == 1
+
+    def is_robin(self):
+        return self.alpha != 0 and self.beta != 0
+
+    def is_internal(self):
+        return self.alpha == 0 and self.beta == 0
+
+
+def Dirichlet():
+    return BoundaryCondition(1.0, 0.0)
+
+
+def Neumann():
+    return BoundaryCondition(0.0, 1.0)
+
+
+def Robin(alpha: float, beta: float):
+    return BoundaryCondition(float(alpha), float(beta))
+
+
+def Internal():
+    return BoundaryCondition(0.0, 0.0)
+
+
+# ------------------------------------------------------------------------------ operators
+class _Op:
+    rank = 0
+
+    def ops(self, dim: int):
+        raise NotImplementedError
+
+
+class Laplacian(_Op):
+    """∇² (src/operators/laplacian.jl:6-7)."""
+
+    def ops(self, dim):
+        return [(OP_LAPLACIAN, 0)]
+
+    def __repr__(self):
+        return "Laplacian (∇²f)"
+
+
+class Partial(_Op):
+    """∂ⁿ/∂x_dim (src/operators/partial.jl:6-10,49-61); dim is 1-based as in the reference."""
+
+    def __init__(self, order: int, dim: int):
+        if order not in (1, 2):
+            raise ValueError("Only first and second order derivatives are supported. "
+                             "Use the custom operator for higher orders.")
+        self.order, self.dim = order, dim
+
+    def ops(self, dim):
+        if not 1 <= self.dim <= dim:
+            raise ValueError(f"dimension {self.dim} out of range 1..{dim}")
+        return [(OP_PARTIAL1 if self.order == 1 else OP_PARTIAL2, self.dim - 1)]
+
+    def __repr__(self):
+        return f"∂ⁿf/∂xᵢ (n = {self.order}, i = {self.dim})"
+
+
+class Jacobian(_Op):
+    """Tuple of first partials, one factorisation with D right-hand sides (jacobian.jl:19,53-62)."""
+    rank = 1
+
+    def __init__(self, dim: int | None = None):
+        self.dim = dim
+
+    def ops(self, dim):
+        return [(OP_PARTIAL1, d) for d in range(dim)]
+
+    def __repr__(self):
+        return "Jacobian (J)"
+
+
+class Regrid(_Op):
+    """Interpolation to other points: the operator is the identity (regridding.jl:6-7)."""
+
+    def ops(self, dim):
+        return [(OP_IDENTITY, 0)]
+
+    def __repr__(self):
+        return "regrid"
+
+
+class Operators(_Op):
+    """Several operators built from one factorisation per stencil (e.g. gradient + Laplacian).
+
+    Not in the reference, which factorises once per operator; the weights are identical."""
+    rank = 1
+
+    def __init__(self, *ops: _Op):
+        self.parts = ops
+
+    def ops(self, dim):
+        out = []
+        for p in self.parts:
+            out.extend(p.ops(dim))
+        return out
+
+    def __repr__(self):
+        return " + ".join(map(repr, self.parts))
+
+
+# ------------------------------------------------------------------------------ neighbours
+def autoselect_k(data, basis) -> int:
+    """min(N, max(2*binomial(m+d, d), 2d+1)) (src/utils.jl:39-43)."""
+    pts = _points(data)
+    n, d = pts.shape
+    m = basis.poly_deg
+    return min(n, max(2 * math.comb(m + d, d) if m >= 0 else 0, 2 * d + 1))
+
+
+def find_neighbors(data, eval_points=None, k: int | None = None, *, ctx: Context | None = None, out=None):
+    """k nearest data points of every eval point, sorted by distance, ties by index (0-based).
+
+    Mirrors find_neighbors(data, [eval_points,] k) (src/utils.jl:5-18).  Returns an
+    (N_eval, k) int32 array (numpy for host inputs, torch on the GPU for cuda inputs)."""
+    if k is None:
+        if isinstance(eval_points, (int, np.integer)):
+            k, eval_points = int(eval_points), None
+        else:
+            raise TypeError("find_neighbors needs k")
+    d = _points(data)
+    q = d if eval_points is None else _points(eval_points, "eval_points")
+    if d.shape[1] != q.shape[1]:
+        raise DimensionMismatch("data and eval_points must have the same dimension")
+    ctx = ctx or Context.default(_device_of(d, q))
+    ne = q.shape[0]
+    if out is None:
+        if _is_torch(q) and q.is_cuda:
+            out = _torch().empty((ne, k), dtype=_torch().int32, device=q.device)
+        else:
+            out = np.empty((ne, k), dtype=np.int32)
+    ctx.check(ctx.lib.rbf_knn(ctx.handle, _ptr(d), d.shape[0], _ptr(q), ne, d.shape[1], k, _ptr(out)))
+    return out
+
+
+# ------------------------------------------------------------------------------ weights
+class WeightsCSR:
+    """Sparse weights on the GPU (CSR, columns ascending within rows).
+
+    The reference returns SparseMatrixCSC (src/solve/execution.jl:105-115); the same
+    matrix in CSR is the CSC of its transpose, and to_csc() produces the CSC arrays."""
+
+    def __init__(self, row_ptr, col, val, shape, ctx: Context):
+        self.row_ptr, self.col, self.val, self.shape, self.ctx = row_ptr, col, val, shape, ctx
+
+    @property
+    def nnz(self):
+        return int(self.col.shape[0])
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.val.cpu().numpy(), self.col.cpu().numpy(), self.row_ptr.cpu().numpy()),
+                             shape=self.shape)
+
+    def to_csc(self):
+        torch = _torch()
+        ne, ns = self.shape
+        dev = self.col.device
+        cp = torch.empty(ns + 1, dtype=torch.int64, device=dev)
+        rw = torch.empty(self.nnz, dtype=torch.int32, device=dev)
+        vv = torch.empty(self.nnz, dtype=torch.float64, device=dev)
+        self.ctx.check(self.ctx.lib.rbf_csr_to_csc(self.ctx.handle, ne, ns, _ptr(self.row_ptr), _ptr(self.col),
+                                                   _ptr(self.val), _ptr(cp), _ptr(rw), _ptr(vv)))
+        return cp, rw, vv
+
+    def apply(self, x, y=None, alpha=1.0, beta=0.0, layout="colmajor"):
+        return _spmm(self, x, y, alpha, beta, layout)
+
+    def __matmul__(self, x):
+        return self.apply(x)
+
+
+def _spmm(W: WeightsCSR, x, y=None, alpha=1.0, beta=0.0, layout="colmajor"):
+    torch = _torch()
+    ne, ns = W.shape
+    ctx = W.ctx
+    host = not (_is_torch(x) and x.is_cuda)
+    if _is_torch(x):
+        xt = x.detach().to(torch.float64).contiguous()
+    else:
+        xt = np.asarray(x, dtype=np.float64)
+    if xt.shape[0] != ns:
+        raise DimensionMismatch(f"operand has {xt.shape[0]} rows, operator has {ns} columns")
+    nf = 1 if xt.ndim == 1 else int(np.prod(xt.shape[1:]))
+    if layout == "colmajor" and nf > 1:
+        # (ns, nf) with fields in columns -> column-major buffer (field f contiguous)
+        xb = xt.reshape(ns, nf).T.contiguous() if _is_torch(xt) else np.ascontiguousarray(xt.reshape(ns, nf).T)
+        lay, ldx, ldy = 0, ns, ne
+    else:
+        xb = xt.reshape(ns, nf).contiguous() if _is_torch(xt) else np.ascontiguousarray(xt.reshape(ns, nf))
+        lay, ldx, ldy = 1, nf, nf
+    out_shape = (ne,) if xt.ndim == 1 else (ne,) + tuple(xt.shape[1:])
+    if host:
+        yb = np.zeros((nf, ne) if lay == 0 else (ne, nf), dtype=np.float64)
+        if y is not None and beta != 0.0:
+            yy = np.asarray(y, dtype=np.float64).reshape(ne, nf)
+            yb[:] = yy.T if lay == 0 else yy
+    else:
+        yb = torch.zeros((nf, ne) if lay == 0 else (ne, nf), dtype=torch.float64, device=xt.device)
+        if y is not None and beta != 0.0:
+            yy = y.reshape(ne, nf).to(torch.float64)
+            yb.copy_(yy.T if lay == 0 else yy)
+    if nf == 1:
+        ldx = ldy = 1
+    ctx.check(ctx.lib.rbf_spmm(ctx.handle, ne, ns, _ptr(W.row_ptr), _ptr(W.col), _ptr(W.val), nf, lay, _ptr(xb),
+                               ldx, float(alpha), float(beta), _ptr(yb), ldy))
+    res = yb.T if lay == 0 else yb
+    res = res.reshape(out_shape)
+    if y is not None:
+        if _is_torch(y):
+            y.copy_(res if _is_torch(res) else torch.from_numpy(np.ascontiguousarray(res)))
+        else:
+            y[...] = res.cpu().numpy() if _is_torch(res) else res
+        return y
+    return res
+
+
+def _hermite_arrays(hermite, ns, dim):
+    if hermite is None:
+        return None
+    if isinstance(hermite, dict):
+        isb, bcs, normals = hermite["is_boundary"], hermite["bc"], hermite["normals"]
+    else:
+        isb, bcs, normals = hermite.is_boundary, hermite.bc, hermite.normals
+    isb = np.ascontiguousarray(np.asarray(isb, dtype=np.uint8))
+    if isb.shape[0] != ns:
+        raise DimensionMismatch(f"length(is_boundary) = {isb.shape[0]} must equal the number of data points ({ns})")
+    alpha = np.ascontiguousarray([float(b.alpha) for b in bcs], dtype=np.float64)
+    beta = np.ascontiguousarray([float(b.beta) for b in bcs], dtype=np.float64)
+    nrm = np.ascontiguousarray(np.asarray(normals, dtype=np.float64).reshape(-1, dim) if len(bcs) else
+                               np.zeros((0, dim)))
+    nb = int(isb.sum())
+    if len(bcs) != nb or nrm.shape[0] != nb:
+        raise DimensionMismatch(f"boundary_conditions ({len(bcs)}) and normals ({nrm.shape[0]}) must each have "
+                                f"one entry per boundary point (count(is_boundary) = {nb})")
+    return isb, alpha, beta, nrm
+
+
+def build_weights(ops, data, eval_points, adjl, basis, hermite=None, precision="fp64", *, ctx=None,
+                  refine_steps=0, tol=0.0, return_status=False, stats=None):
+    """Weights of `ops` (list of (op_code, op_dim)) on stencils adjl; returns a list of WeightsCSR.
+
+    The drop-in for _build_weights (src/solve/api.jl:26-35, 167-196)."""
+    torch = _torch()
+    d = _points(data)
+    q = d if eval_points is None else _points(eval_points, "eval_points")
+    ns, dim = d.shape
+    ne = q.shape[0]
+    ctx = ctx or Context.default(_device_of(d, q, adjl))
+    dev = torch.device("cuda", ctx.device)
+    if _is_torch(adjl):
+        a = adjl.to(torch.int32).contiguous()
+    else:
+        a = np.ascontiguousarray(np.asarray(adjl, dtype=np.int32))
+    if a.ndim != 2 or a.shape[0] != ne:
+        raise DimensionMismatch("adjl must be an (N_eval, k) array of 0-based data indices")
+    k = int(a.shape[1])
+    cfg = _native.BuildCfg()
+    cfg.dim, cfg.phs, cfg.poly_deg, cfg.nops = dim, basis.order, basis.poly_deg, len(ops)
+    for i, (c, od) in enumerate(ops):
+        cfg.op_code[i] = c
+        cfg.op_dim[i] = od
+    cfg.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    cfg.refine_steps = refine_steps
+    cfg.tol = tol
+    herm = _hermite_arrays(hermite, ns, dim)
+    hs = None
+    keep = []
+    if herm is not None:
+        isb, al, be, nr = herm
+        hs = _native.Hermite(isb.ctypes.data, al.ctypes.data, be.ctypes.data, nr.ctypes.data, len(al))
+        keep.append(herm)
+    row_ptr = torch.empty(ne + 1, dtype=torch.int64, device=dev)
+    nnz = ctypes.c_int64(0)
+    ctx.check(ctx.lib.rbf_build_count(ctx.handle, ns, ne, k, ctypes.byref(hs) if hs else None, _ptr(row_ptr),
+                                      ctypes.byref(nnz)))
+    col = torch.empty(nnz.value, dtype=torch.int32, device=dev)
+    val = torch.empty((len(ops), nnz.value), dtype=torch.float64, device=dev)
+    status = torch.empty(ne, dtype=torch.int8, device=dev) if return_status else None
+    st = _native.BuildStats() if stats is None else stats
+    ctx.check(ctx.lib.rbf_build(ctx.handle, ctypes.byref(cfg), _ptr(d), ns, _ptr(q), ne, _ptr(a), k,
+                                ctypes.byref(hs) if hs else None, _ptr(row_ptr), _ptr(col), _ptr(val),
+                                _ptr(status), ctypes.byref(st)))
+    Ws = [WeightsCSR(row_ptr, col, val[i], (ne, ns), ctx) for i in range(len(ops))]
+    if return_status:
+        return Ws, status
+    return Ws
+
+
+# ------------------------------------------------------------------------------ operator object
+class RadialBasisOperator:
+    """Operator of data with a radial basis and monomial augmentation (operators.jl:50-143).
+
+    weights are device CSR matrices (a tuple for Jacobian / Operators)."""
+
+    def __init__(self, L: _Op, data, eval_points=None, basis=None, k: int | None = None, adjl=None,
+                 hermite=None, precision: str = "fp64", ctx: Context | None = None):
+        self.L = L
+        data = _points(data)
+        ev = None if eval_points is None else _points(eval_points, "eval_points")
+        self.ctx = ctx or Context.default(_device_of(data, ev))
+        # points live on the GPU for the operator's lifetime (one host->device copy)
+        self.data = _to_device(data, self.ctx)
+        self.eval_points = self.data if ev is None else _to_device(ev, self.ctx)
+        self.basis = basis if basis is not None else PHS(3, poly_deg=2)
+        self.k = k if k is not None else autoselect_k(self.data, self.basis)
+        self.adjl = adjl if adjl is not None else find_neighbors(self.data, self.eval_points, self.k, ctx=self.ctx)
+        self.hermite = hermite
+        self.precision = precision
+        self.weights = None
+        self.valid_cache = False
+        self.update_weights()
+
+    @property
+    def dim(self):
+        return self.data.shape[1]
+
+    def _build(self):
+        ops = self.L.ops(self.dim)
+        Ws = build_weights(ops, self.data, self.eval_points, self.adjl, self.basis, self.hermite, self.precision,
+                           ctx=self.ctx)
+        return Ws[0] if (len(Ws) == 1 and self.L.rank == 0) else tuple(Ws)
+
+    def update_weights(self):
+        """Rebuild the weights from data / eval_points (operators.jl:589-602)."""
+        self.weights = self._build()
+        self.valid_cache = True
+
+    def invalidate_cache(self):
+        self.valid_cache = False
+
+    def __call__(self, x, y=None):
+        if not self.valid_cache:
+            self.update_weights()
+        if isinstance(self.weights, tuple):
+            outs = [W.apply(x) for W in self.weights]
+            if _is_torch(outs[0]):
+                res = _torch().stack(outs, dim=-1)
+            else:
+                res = np.stack(outs, axis=-1)
+            if y is not None:
+                y[...] = res
+                return y
+            return res
+        return self.weights.apply(x, y)
+
+    @property
+    def shape(self):
+        return (self.eval_points.shape[0], self.data.shape[0])
+
+    def __repr__(self):
+        return f"RadialBasisOperator\n├─Operator: {self.L!r}\n├─Data type: float64\n├─Number of weights: " \
+               f"{self.weights.nnz if isinstance(self.weights, WeightsCSR) else self.weights[0].nnz}\n" \
+               f"└─Basis: {self.basis!r}"
+
+
+def weights(op: RadialBasisOperator):
+    """operators.jl:569-572"""
+    if not op.valid_cache:
+        op.update_weights()
+    return op.weights
+
+
+def update_weights(op: RadialBasisOperator):
+    op.update_weights()
+
+
+def mul(y, op: RadialBasisOperator, x, alpha: float = 1.0, beta: float = 0.0):
+    """y = alpha * op * x + beta * y (mul!, operators.jl:529-542; rank-0 operators only)."""
+    if not op.valid_cache:
+        op.update_weights()
+    if isinstance(op.weights, tuple):
+        raise ValueError("mul is only defined for rank-0 operators with scalar weights")
+    return op.weights.apply(x, y, alpha, beta)
+
+
+# ------------------------------------------------------------------------------ front ends
+def laplacian(data, basis=None, **kw):
+    """laplacian(data; basis=PHS(3; poly_deg=2), eval_points, k, adjl, hermite)"""
+    return RadialBasisOperator(Laplacian(), data, basis=basis, **kw)
+
+
+def partial(data, order: int, dim: int, basis=None, **kw):
+    """partial(data, order, dim; ...) with dim 1-based as in the reference."""
+    return RadialBasisOperator(Partial(order, dim), data, basis=basis, **kw)
+
+
+def jacobian(data, basis=None, **kw):
+    d = _points(data)
+    return RadialBasisOperator(Jacobian(d.shape[1]), d, basis=basis, **kw)
+
+
+def gradient(data, basis=None, **kw):
+    """gradient(data; ...) = jacobian(data; ...) (gradient.jl:32)."""
+    return jacobian(data, basis=basis, **kw)
+
+
+def regrid(data, eval_points, basis=None, **kw):
+    """regrid(data, eval_points; basis, k, adjl) (regridding.jl:38-47)."""
+    return RadialBasisOperator(Regrid(), data, eval_points=eval_points, basis=basis, **kw)

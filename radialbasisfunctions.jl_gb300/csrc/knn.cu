@@ -1,0 +1,450 @@
+// Grid-bucketed exact k-nearest-neighbour search (replaces find_neighbors,
+// src/utils.jl:12-18, which builds a KDTree and calls knn(tree, eval, k, true)).
+//
+// Layout in HBM
+//   source points are counting-sorted into a uniform grid: sp[] (AoS doubles, cell order),
+//   sidx[] (original index per sorted slot), cstart[ncells+1] (first slot of each cell).
+//   Queries are visited in cell order (qorder[]) so that neighbouring warps touch the same
+//   cells and the candidate reads hit L1/L2.
+// Search (one warp per query)
+//   The warp scans the block of cells within Chebyshev radius R0 of the query's cell, then
+//   shells R0+1, R0+2, ... until the k-th best squared distance is below the squared
+//   distance from the query to the outside of the scanned block.  Candidates are read as
+//   one flattened list of contiguous cell runs (each x-row of cells is contiguous in the
+//   sorted order), 32 per step, so all lanes stay busy.
+// Ordering
+//   Keys are (squared distance, point index): the squared distance is accumulated in
+//   dimension order without FMA contraction, exactly as the reference's Euclidean
+//   reduction does, and exact ties go to the smaller index.  The running top-k list is a
+//   sorted array spread over the warp (slot j at lane j%32, register j/32) and candidates
+//   that beat the current k-th key are inserted with warp shuffles.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "rbf_internal.cuh"
+
+namespace {
+
+constexpr int KNN_WARPS = 8;     // warps per block
+constexpr int KNN_RANGES = 64;   // cell runs buffered per warp step
+
+struct GridDesc {
+    double lo[3];
+    double h[3];
+    double inv_h[3];
+    int nc[3];
+    int64_t ncells;
+};
+
+__device__ __forceinline__ double sqdist(const double *a, const double *b, int dim) {
+    double t = __dsub_rn(a[0], b[0]);
+    double s = __dmul_rn(t, t);
+    for (int d = 1; d < dim; d++) {
+        t = __dsub_rn(a[d], b[d]);
+        s = __dadd_rn(s, __dmul_rn(t, t));
+    }
+    return s;
+}
+
+template <int DIM>
+__device__ __forceinline__ int64_t cell_of(const GridDesc &g, const double *x, int *c) {
+    int64_t id = 0;
+#pragma unroll
+    for (int d = DIM - 1; d >= 0; d--) {
+        double f = floor((x[d] - g.lo[d]) * g.inv_h[d]);
+        int cd;
+        if (!(f >= 0.0)) cd = 0;  // also catches NaN
+        else if (f >= (double)(g.nc[d] - 1)) cd = g.nc[d] - 1;
+        else cd = (int)f;
+        c[d] = cd;
+        id = id * g.nc[d] + cd;
+    }
+    return id;
+}
+
+__global__ void bbox_partial_kernel(const double *__restrict__ x, int64_t n, int dim, double *__restrict__ part) {
+    __shared__ double smin[3][256], smax[3][256];
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        for (int d = 0; d < dim; d++) {
+            double v = x[i * dim + d];
+            mn[d] = fmin(mn[d], v);
+            mx[d] = fmax(mx[d], v);
+        }
+    for (int d = 0; d < 3; d++) {
+        smin[d][threadIdx.x] = mn[d];
+        smax[d][threadIdx.x] = mx[d];
+    }
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s)
+            for (int d = 0; d < 3; d++) {
+                smin[d][threadIdx.x] = fmin(smin[d][threadIdx.x], smin[d][threadIdx.x + s]);
+                smax[d][threadIdx.x] = fmax(smax[d][threadIdx.x], smax[d][threadIdx.x + s]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int d = 0; d < 3; d++) {
+            part[blockIdx.x * 6 + d] = smin[d][0];
+            part[blockIdx.x * 6 + 3 + d] = smax[d][0];
+        }
+}
+
+template <int DIM>
+__global__ void cell_count_kernel(GridDesc g, const double *__restrict__ x, int64_t n,
+                                  int32_t *__restrict__ cell, int32_t *__restrict__ count) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double p[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; d++) p[d] = x[i * DIM + d];
+        int c[DIM];
+        int64_t id = cell_of<DIM>(g, p, c);
+        cell[i] = (int32_t)id;
+        atomicAdd(&count[id], 1);
+    }
+}
+
+template <int DIM>
+__global__ void cell_scatter_kernel(const double *__restrict__ x, int64_t n, const int32_t *__restrict__ cell,
+                                    const int32_t *__restrict__ start, int32_t *__restrict__ fill,
+                                    double *__restrict__ sp, int32_t *__restrict__ sidx) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t c = cell[i];
+        int32_t pos = start[c] + atomicAdd(&fill[c], 1);
+        if (sp)
+#pragma unroll
+            for (int d = 0; d < DIM; d++) sp[(int64_t)pos * DIM + d] = x[i * DIM + d];
+        sidx[pos] = (int32_t)i;
+    }
+}
+
+__device__ __forceinline__ bool key_less(double d1, int32_t i1, double d2, int32_t i2) {
+    return d1 < d2 || (d1 == d2 && i1 < i2);
+}
+
+template <int DIM, int SLOTS>
+__global__ void __launch_bounds__(KNN_WARPS * 32)
+knn_query_kernel(GridDesc g, const double *__restrict__ sp, const int32_t *__restrict__ sidx,
+                 const int32_t *__restrict__ cstart, const double *__restrict__ q,
+                 const int32_t *__restrict__ qorder, int64_t nq, int k, int R0,
+                 int32_t *__restrict__ out) {
+    __shared__ int32_t s_start[KNN_WARPS][KNN_RANGES];
+    __shared__ int32_t s_off[KNN_WARPS][KNN_RANGES + 1];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t warp0 = (int64_t)blockIdx.x * KNN_WARPS + wib;
+    const int64_t nwarps = (int64_t)gridDim.x * KNN_WARPS;
+    int32_t *my_start = s_start[wib];
+    int32_t *my_off = s_off[wib];
+
+    for (int64_t t = warp0; t < nq; t += nwarps) {
+        const int32_t qi = qorder[t];
+        double qp[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; d++) qp[d] = q[(int64_t)qi * DIM + d];
+        int qc[3] = {0, 0, 0};
+        cell_of<DIM>(g, qp, qc);
+
+        double key[SLOTS];
+        int32_t kid[SLOTS];
+#pragma unroll
+        for (int s = 0; s < SLOTS; s++) {
+            key[s] = INFINITY;
+            kid[s] = 0x7fffffff;
+        }
+        double kth = INFINITY;
+        int32_t kth_id = 0x7fffffff;
+        const int kl = (k - 1) & 31, ks = (k - 1) >> 5;
+
+        int r_in = -1;
+        for (int R = R0;; R++) {
+            // rows of cells: (dy, dz) in [-R, R]^(DIM-1)
+            const int side = 2 * R + 1;
+            const int nrows = DIM == 1 ? 1 : (DIM == 2 ? side : side * side);
+            for (int row0 = 0; row0 < nrows; row0 += 32) {
+                // each lane describes up to two runs of cells of one row
+                int row = row0 + lane;
+                int32_t a0 = 0, l0 = 0, a1 = 0, l1 = 0;
+                if (row < nrows) {
+                    int dy = 0, dz = 0;
+                    if (DIM >= 2) dy = (row % side) - R;
+                    if (DIM == 3) dz = (row / side) - R;
+                    int cy = qc[1] + dy, cz = qc[2] + dz;
+                    bool inside = (DIM < 2 || (cy >= 0 && cy < g.nc[1])) && (DIM < 3 || (cz >= 0 && cz < g.nc[2]));
+                    if (inside) {
+                        int m = max(abs(dy), abs(dz));
+                        int64_t rowbase = ((int64_t)cz * g.nc[1] + cy) * g.nc[0];
+                        if (m > r_in) {
+                            int x0 = max(qc[0] - R, 0), x1 = min(qc[0] + R, g.nc[0] - 1);
+                            if (x0 <= x1) {
+                                a0 = cstart[rowbase + x0];
+                                l0 = cstart[rowbase + x1 + 1] - a0;
+                            }
+                        } else {
+                            int x0 = max(qc[0] - R, 0), x1 = min(qc[0] - r_in - 1, g.nc[0] - 1);
+                            if (x0 <= x1) {
+                                a0 = cstart[rowbase + x0];
+                                l0 = cstart[rowbase + x1 + 1] - a0;
+                            }
+                            x0 = max(qc[0] + r_in + 1, 0);
+                            x1 = min(qc[0] + R, g.nc[0] - 1);
+                            if (x0 <= x1) {
+                                a1 = cstart[rowbase + x0];
+                                l1 = cstart[rowbase + x1 + 1] - a1;
+                            }
+                        }
+                    }
+                }
+                // exclusive offsets of the 64 runs (run 2*lane and 2*lane+1)
+                int32_t pair = l0 + l1, incl = pair;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                int32_t excl = incl - pair;
+                my_start[2 * lane] = a0;
+                my_start[2 * lane + 1] = a1;
+                my_off[2 * lane] = excl;
+                my_off[2 * lane + 1] = excl + l0;
+                const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                if (lane == 31) my_off[KNN_RANGES] = total;
+                __syncwarp();
+                for (int32_t f0 = 0; f0 < total; f0 += 32) {
+                    int32_t f = f0 + lane;
+                    double dd = INFINITY;
+                    int32_t id = 0x7fffffff;
+                    if (f < total) {
+                        // last run whose offset <= f (runs of length 0 are skipped by <=)
+                        int lo = 0, hi = KNN_RANGES - 1;
+                        while (lo < hi) {
+                            int mid = (lo + hi + 1) >> 1;
+                            if (my_off[mid] <= f) lo = mid;
+                            else hi = mid - 1;
+                        }
+                        int32_t p = my_start[lo] + (f - my_off[lo]);
+                        double xp[DIM];
+#pragma unroll
+                        for (int d = 0; d < DIM; d++) xp[d] = sp[(int64_t)p * DIM + d];
+                        dd = sqdist(qp, xp, DIM);
+                        id = sidx[p];
+                    }
+                    bool pass = (f < total) && key_less(dd, id, kth, kth_id);
+                    unsigned m = __ballot_sync(0xffffffffu, pass);
+                    while (m) {
+                        const int src = __ffs(m) - 1;
+                        m &= m - 1;
+                        const double cd = __shfl_sync(0xffffffffu, dd, src);
+                        const int32_t ci = __shfl_sync(0xffffffffu, id, src);
+                        if (!key_less(cd, ci, kth, kth_id)) continue;  // uniform across the warp
+                        int pos = 0;
+#pragma unroll
+                        for (int s = 0; s < SLOTS; s++)
+                            pos += __popc(__ballot_sync(0xffffffffu, key_less(key[s], kid[s], cd, ci)));
+                        // shift right by one from pos, insert at pos
+                        double pk[SLOTS];
+                        int32_t pi[SLOTS];
+#pragma unroll
+                        for (int s = 0; s < SLOTS; s++) {
+                            pk[s] = __shfl_up_sync(0xffffffffu, key[s], 1);
+                            pi[s] = __shfl_up_sync(0xffffffffu, kid[s], 1);
+                            const int sp = s > 0 ? s - 1 : 0;
+                            double wk = __shfl_sync(0xffffffffu, key[sp], 31);
+                            int32_t wi = __shfl_sync(0xffffffffu, kid[sp], 31);
+                            if (lane == 0) {
+                                pk[s] = wk;
+                                pi[s] = wi;
+                            }
+                        }
+#pragma unroll
+                        for (int s = 0; s < SLOTS; s++) {
+                            int j = lane + 32 * s;
+                            if (j == pos) {
+                                key[s] = cd;
+                                kid[s] = ci;
+                            } else if (j > pos) {
+                                key[s] = pk[s];
+                                kid[s] = pi[s];
+                            }
+                        }
+                        double kv = key[0];
+                        int32_t ki = kid[0];
+#pragma unroll
+                        for (int s = 1; s < SLOTS; s++)
+                            if (s == ks) {
+                                kv = key[s];
+                                ki = kid[s];
+                            }
+                        kth = __shfl_sync(0xffffffffu, kv, kl);
+                        kth_id = __shfl_sync(0xffffffffu, ki, kl);
+                    }
+                }
+                __syncwarp();
+            }
+            // distance from the query to the outside of the scanned block
+            double cover = INFINITY;
+            bool all_covered = true;
+#pragma unroll
+            for (int d = 0; d < DIM; d++) {
+                if (qc[d] - R > 0) {
+                    all_covered = false;
+                    cover = fmin(cover, qp[d] - (g.lo[d] + (double)(qc[d] - R) * g.h[d]));
+                }
+                if (qc[d] + R < g.nc[d] - 1) {
+                    all_covered = false;
+                    cover = fmin(cover, (g.lo[d] + (double)(qc[d] + R + 1) * g.h[d]) - qp[d]);
+                }
+            }
+            if (all_covered) break;
+            if (kth < INFINITY) {
+                // slack for the rounding of cell assignment vs. face positions
+                double mag = 0.0;
+#pragma unroll
+                for (int d = 0; d < DIM; d++) mag = fmax(mag, fabs(qp[d]) + fabs(g.lo[d]) + g.h[d] * g.nc[d]);
+                double c = cover * (1.0 - 1e-9) - 4e-15 * mag;
+                if (c > 0.0 && kth < c * c) break;
+            }
+            r_in = R;
+        }
+        // write the sorted row
+#pragma unroll
+        for (int s = 0; s < SLOTS; s++) {
+            int j = lane + 32 * s;
+            if (j < k) out[(int64_t)qi * k + j] = kid[s];
+        }
+    }
+}
+
+int grid_blocks(rbf_ctx *ctx, int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    int64_t cap = (int64_t)ctx->num_sms * 16;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+template <int DIM>
+int knn_dim(rbf_ctx *ctx, const double *d_data, int64_t ns, const double *d_eval, int64_t ne, int k,
+            int32_t *d_idx) {
+    // bounding box of the sources
+    const int pb = std::min<int64_t>((ns + 255) / 256, 1024);
+    DevBuf part;
+    RBF_TRY(part.alloc(ctx, sizeof(double) * 6 * pb));
+    bbox_partial_kernel<<<pb, 256, 0, ctx->stream>>>(d_data, ns, DIM, part.as<double>());
+    RBF_CHECK_LAUNCH(ctx);
+    std::vector<double> hp(6 * (size_t)pb);
+    RBF_CUDA(ctx, cudaMemcpyAsync(hp.data(), part.ptr, sizeof(double) * 6 * pb, cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int b = 0; b < pb; b++)
+        for (int d = 0; d < DIM; d++) {
+            lo[d] = std::min(lo[d], hp[b * 6 + d]);
+            hi[d] = std::max(hi[d], hp[b * 6 + 3 + d]);
+        }
+    for (int d = 0; d < DIM; d++)
+        if (!std::isfinite(lo[d]) || !std::isfinite(hi[d]))
+            return rbf_fail(ctx, RBF_ERR_ARGUMENT, "data points contain non-finite coordinates");
+
+    // cell size: about 1.5 k points expected inside the ball of radius R0 cells
+    const int R0 = 2;
+    const double unit_ball = DIM == 1 ? 2.0 : (DIM == 2 ? M_PI : 4.0 * M_PI / 3.0);
+    double ppc = 1.5 * k / (unit_ball * std::pow((double)R0, DIM));
+    if (ppc < 0.5) ppc = 0.5;
+    double vol = 1.0;
+    int eff = 0;
+    for (int d = 0; d < DIM; d++)
+        if (hi[d] > lo[d]) {
+            vol *= hi[d] - lo[d];
+            eff++;
+        }
+    double target_cells = std::max(1.0, (double)ns / ppc);
+    double h = eff > 0 ? std::pow(vol / target_cells, 1.0 / eff) : 1.0;
+    GridDesc g{};
+    int64_t ncells = 1;
+    for (int d = 0; d < 3; d++) {
+        if (d >= DIM) {
+            g.nc[d] = 1;
+            g.lo[d] = 0;
+            g.h[d] = 1;
+            g.inv_h[d] = 1;
+            continue;
+        }
+        double ext = hi[d] - lo[d];
+        int64_t m = ext > 0 ? (int64_t)std::floor(ext / h) : 1;
+        m = std::max<int64_t>(1, std::min<int64_t>(m, 1 << 20));
+        g.nc[d] = (int)m;
+        g.lo[d] = lo[d];
+        g.h[d] = ext > 0 ? ext / (double)m : 1.0;
+        g.inv_h[d] = 1.0 / g.h[d];
+        ncells *= m;
+    }
+    while (ncells > (int64_t)1 << 27) {  // keep cell starts in int32 and memory modest
+        ncells = 1;
+        for (int d = 0; d < DIM; d++) {
+            g.nc[d] = std::max(1, g.nc[d] / 2);
+            g.h[d] = (hi[d] > lo[d]) ? (hi[d] - lo[d]) / g.nc[d] : 1.0;
+            g.inv_h[d] = 1.0 / g.h[d];
+            ncells *= g.nc[d];
+        }
+    }
+    g.ncells = ncells;
+
+    DevBuf cell, count, start, fill, sp, sidx, qcell, qcount, qstart, qfill, qorder;
+    RBF_TRY(cell.alloc(ctx, sizeof(int32_t) * ns));
+    RBF_TRY(count.alloc(ctx, sizeof(int32_t) * (ncells + 1)));
+    RBF_TRY(start.alloc(ctx, sizeof(int32_t) * (ncells + 1)));
+    RBF_TRY(fill.alloc(ctx, sizeof(int32_t) * (ncells + 1)));
+    RBF_TRY(sp.alloc(ctx, sizeof(double) * DIM * ns));
+    RBF_TRY(sidx.alloc(ctx, sizeof(int32_t) * ns));
+    RBF_CUDA(ctx, cudaMemsetAsync(count.ptr, 0, sizeof(int32_t) * (ncells + 1), ctx->stream));
+    RBF_CUDA(ctx, cudaMemsetAsync(fill.ptr, 0, sizeof(int32_t) * (ncells + 1), ctx->stream));
+    cell_count_kernel<DIM><<<grid_blocks(ctx, ns, 256), 256, 0, ctx->stream>>>(g, d_data, ns, cell.as<int32_t>(), count.as<int32_t>());
+    RBF_CHECK_LAUNCH(ctx);
+    RBF_TRY(rbf_exclusive_scan_i32(ctx, count.as<int32_t>(), start.as<int32_t>(), ncells + 1, nullptr));
+    cell_scatter_kernel<DIM><<<grid_blocks(ctx, ns, 256), 256, 0, ctx->stream>>>(
+        d_data, ns, cell.as<int32_t>(), start.as<int32_t>(), fill.as<int32_t>(), sp.as<double>(), sidx.as<int32_t>());
+    RBF_CHECK_LAUNCH(ctx);
+
+    // visit queries in cell order
+    RBF_TRY(qcell.alloc(ctx, sizeof(int32_t) * ne));
+    RBF_TRY(qcount.alloc(ctx, sizeof(int32_t) * (ncells + 1)));
+    RBF_TRY(qstart.alloc(ctx, sizeof(int32_t) * (ncells + 1)));
+    RBF_TRY(qfill.alloc(ctx, sizeof(int32_t) * (ncells + 1)));
+    RBF_TRY(qorder.alloc(ctx, sizeof(int32_t) * ne));
+    RBF_CUDA(ctx, cudaMemsetAsync(qcount.ptr, 0, sizeof(int32_t) * (ncells + 1), ctx->stream));
+    RBF_CUDA(ctx, cudaMemsetAsync(qfill.ptr, 0, sizeof(int32_t) * (ncells + 1), ctx->stream));
+    cell_count_kernel<DIM><<<grid_blocks(ctx, ne, 256), 256, 0, ctx->stream>>>(g, d_eval, ne, qcell.as<int32_t>(), qcount.as<int32_t>());
+    RBF_CHECK_LAUNCH(ctx);
+    RBF_TRY(rbf_exclusive_scan_i32(ctx, qcount.as<int32_t>(), qstart.as<int32_t>(), ncells + 1, nullptr));
+    cell_scatter_kernel<DIM><<<grid_blocks(ctx, ne, 256), 256, 0, ctx->stream>>>(
+        d_eval, ne, qcell.as<int32_t>(), qstart.as<int32_t>(), qfill.as<int32_t>(), nullptr, qorder.as<int32_t>());
+    RBF_CHECK_LAUNCH(ctx);
+
+    int64_t warps_needed = ne;
+    int64_t blocks = (warps_needed + KNN_WARPS - 1) / KNN_WARPS;
+    int64_t cap = (int64_t)ctx->num_sms * 32;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    if (k <= 32)
+        knn_query_kernel<DIM, 1><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
+            g, sp.as<double>(), sidx.as<int32_t>(), start.as<int32_t>(), d_eval, qorder.as<int32_t>(), ne, k, R0, d_idx);
+    else
+        knn_query_kernel<DIM, 2><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
+            g, sp.as<double>(), sidx.as<int32_t>(), start.as<int32_t>(), d_eval, qorder.as<int32_t>(), ne, k, R0, d_idx);
+    RBF_CHECK_LAUNCH(ctx);
+    return RBF_OK;
+}
+
+}  // namespace
+
+int rbf_knn_device(rbf_ctx *ctx, const double *d_data, int64_t ns, const double *d_eval, int64_t ne, int dim,
+                   int k, int32_t *d_idx) {
+    if (ne == 0) return RBF_OK;
+    switch (dim) {
+    case 1: return knn_dim<1>(ctx, d_data, ns, d_eval, ne, k, d_idx);
+    case 2: return knn_dim<2>(ctx, d_data, ns, d_eval, ne, k, d_idx);
+    case 3: return knn_dim<3>(ctx, d_data, ns, d_eval, ne, k, d_idx);
+    default: return rbf_fail(ctx, RBF_ERR_ARGUMENT, "dim must be 1, 2 or 3 (got %d)", dim);
+    }
+}

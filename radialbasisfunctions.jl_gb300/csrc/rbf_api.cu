@@ -1,0 +1,447 @@
+// C ABI of librbffd_gb300.so: contexts, argument checks (with the reference's error
+// classes), host/device pointer staging and the orchestration of the kernels.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "rbf_internal.cuh"
+#include "stencil_common.cuh"
+
+int rbf_build_fp64_launch(rbf_ctx *ctx, const StencilParams &P);
+int rbf_build_fp32_launch(rbf_ctx *ctx, const StencilParams &P);
+
+int rbf_fail(rbf_ctx *ctx, int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->last_error = buf;
+    return code;
+}
+
+bool rbf_is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int InArray::bind(rbf_ctx *ctx, const void *p, size_t bytes) {
+    if (!p || bytes == 0 || rbf_is_device_ptr(p)) {
+        dptr = p;
+        return RBF_OK;
+    }
+    RBF_TRY(staged.alloc(ctx, bytes));
+    RBF_CUDA(ctx, cudaMemcpyAsync(staged.ptr, p, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    dptr = staged.ptr;
+    return RBF_OK;
+}
+
+int OutArray::bind(rbf_ctx *ctx, void *p, size_t bytes_) {
+    user = p;
+    bytes = bytes_;
+    if (!p || bytes == 0 || rbf_is_device_ptr(p)) {
+        dptr = p;
+        host = false;
+        return RBF_OK;
+    }
+    host = true;
+    RBF_TRY(staged.alloc(ctx, bytes));
+    dptr = staged.ptr;
+    return RBF_OK;
+}
+
+int OutArray::finish(rbf_ctx *ctx) {
+    if (host && bytes) RBF_CUDA(ctx, cudaMemcpyAsync(user, dptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return RBF_OK;
+}
+
+namespace {
+
+int binom(int n, int k) {
+    if (k < 0 || k > n) return 0;
+    long r = 1;
+    for (int i = 1; i <= k; i++) r = r * (n - k + i) / i;
+    return (int)r;
+}
+
+void multiexp(int slots, int remaining, int pos, int *cur, std::vector<std::vector<int>> &out) {
+    if (pos == slots) {
+        out.emplace_back(cur, cur + slots);
+        return;
+    }
+    for (int e = remaining; e >= 0; e--) {
+        if (pos == slots - 1 && e != remaining) break;
+        cur[pos] = e;
+        multiexp(slots, remaining - e, pos + 1, cur, out);
+    }
+}
+
+// Monomial exponents in the reference's order (src/basis/monomial.jl:27-123): hand-coded
+// evaluators for 1D and for 2D/3D up to degree 2, Combinatorics.multiexponents(dim+1, deg)
+// (reverse lexicographic, last entry the slack) otherwise.
+int monomial_exponents(int dim, int deg, int8_t (*ex)[3]) {
+    if (deg < 0) return 0;
+    int nmon = binom(dim + deg, dim);
+    for (int m = 0; m < nmon; m++) ex[m][0] = ex[m][1] = ex[m][2] = 0;
+    if (deg == 0) return 1;
+    if (dim == 1) {
+        for (int j = 0; j <= deg; j++) ex[j][0] = (int8_t)j;
+        return nmon;
+    }
+    static const int t21[3][2] = {{0, 0}, {1, 0}, {0, 1}};
+    static const int t22[6][2] = {{0, 0}, {1, 0}, {0, 1}, {1, 1}, {2, 0}, {0, 2}};
+    static const int t31[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    static const int t32[10][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0},
+                                   {1, 0, 1}, {0, 1, 1}, {2, 0, 0}, {0, 2, 0}, {0, 0, 2}};
+    if (dim == 2 && deg == 1) {
+        for (int m = 0; m < 3; m++) ex[m][0] = t21[m][0], ex[m][1] = t21[m][1];
+        return nmon;
+    }
+    if (dim == 2 && deg == 2) {
+        for (int m = 0; m < 6; m++) ex[m][0] = t22[m][0], ex[m][1] = t22[m][1];
+        return nmon;
+    }
+    if (dim == 3 && deg == 1) {
+        for (int m = 0; m < 4; m++) ex[m][0] = t31[m][0], ex[m][1] = t31[m][1], ex[m][2] = t31[m][2];
+        return nmon;
+    }
+    if (dim == 3 && deg == 2) {
+        for (int m = 0; m < 10; m++) ex[m][0] = t32[m][0], ex[m][1] = t32[m][1], ex[m][2] = t32[m][2];
+        return nmon;
+    }
+    std::vector<std::vector<int>> all;
+    int cur[8];
+    multiexp(dim + 1, deg, 0, cur, all);
+    for (int m = 0; m < nmon; m++)
+        for (int d = 0; d < dim; d++) ex[m][d] = (int8_t)all[m][d];
+    return nmon;
+}
+
+int op_order(int code) {
+    switch (code) {
+    case RBF_OP_IDENTITY: return 0;
+    case RBF_OP_PARTIAL1: return 1;
+    default: return 2;
+    }
+}
+
+int check_ctx(rbf_ctx *ctx) {
+    if (!ctx) return RBF_ERR_ARGUMENT;
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (cur != ctx->device) RBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    return RBF_OK;
+}
+
+// Boundary bookkeeping shared by rbf_build_count and rbf_build.
+struct BoundaryDev {
+    InArray isb, alpha, beta, normals;
+    DevBuf g2b;
+    int64_t nb = 0;
+    bool any = false;
+    bool any_nr = false;
+};
+
+int bind_boundary(rbf_ctx *ctx, const rbf_hermite *h, int64_t ns, int dim, BoundaryDev &b) {
+    if (!h || !h->is_boundary) return RBF_OK;
+    b.any = true;
+    if (h->n_boundary < 0) return rbf_fail(ctx, RBF_ERR_DIMENSION, "n_boundary must be >= 0");
+    RBF_TRY(b.isb.bind(ctx, h->is_boundary, (size_t)ns));
+    RBF_TRY(b.alpha.bind(ctx, h->alpha, sizeof(double) * h->n_boundary));
+    RBF_TRY(b.beta.bind(ctx, h->beta, sizeof(double) * h->n_boundary));
+    RBF_TRY(b.normals.bind(ctx, h->normals, sizeof(double) * h->n_boundary * dim));
+    RBF_TRY(b.g2b.alloc(ctx, sizeof(int32_t) * (ns + 1)));
+    RBF_TRY(rbf_boundary_map_device(ctx, ns, b.isb.as<uint8_t>(), b.g2b.as<int32_t>(), &b.nb));
+    // _validate_boundary_inputs (src/solve/api.jl:96-116)
+    if (b.nb != h->n_boundary)
+        return rbf_fail(ctx, RBF_ERR_DIMENSION,
+                        "boundary_conditions (%lld) and normals (%lld) must each have one entry per boundary "
+                        "point (count(is_boundary) = %lld)",
+                        (long long)h->n_boundary, (long long)h->n_boundary, (long long)b.nb);
+    if (b.nb > 0) {
+        std::vector<double> a(b.nb), be(b.nb);
+        RBF_CUDA(ctx, cudaMemcpyAsync(a.data(), b.alpha.dptr, sizeof(double) * b.nb, cudaMemcpyDeviceToHost, ctx->stream));
+        RBF_CUDA(ctx, cudaMemcpyAsync(be.data(), b.beta.dptr, sizeof(double) * b.nb, cudaMemcpyDeviceToHost, ctx->stream));
+        RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int64_t i = 0; i < b.nb; i++)
+            if (!(a[i] == 1.0 && be[i] == 0.0)) b.any_nr = true;
+    }
+    return RBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *rbf_version(void) { return "rbffd-gb300 0.1.0 (sm_103a)"; }
+
+int rbf_ctx_create(int device, rbf_ctx **out) {
+    if (!out) return RBF_ERR_ARGUMENT;
+    *out = nullptr;
+    rbf_ctx *ctx = new rbf_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        delete ctx;
+        cudaGetLastError();
+        return RBF_ERR_CUDA;
+    }
+    ctx->stream = ctx->own_stream;
+    *out = ctx;
+    return RBF_OK;
+}
+
+int rbf_ctx_destroy(rbf_ctx *ctx) {
+    if (!ctx) return RBF_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->own_stream) {
+        cudaStreamSynchronize(ctx->own_stream);
+        cudaStreamDestroy(ctx->own_stream);
+    }
+    delete ctx;
+    return RBF_OK;
+}
+
+int rbf_ctx_set_stream(rbf_ctx *ctx, void *s) {
+    if (!ctx) return RBF_ERR_ARGUMENT;
+    ctx->stream = s ? static_cast<cudaStream_t>(s) : ctx->own_stream;
+    return RBF_OK;
+}
+
+const char *rbf_last_error(const rbf_ctx *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int rbf_knn(rbf_ctx *ctx, const double *data, int64_t ns, const double *eval, int64_t ne, int32_t dim, int32_t k,
+            int32_t *idx_out) {
+    RBF_TRY(check_ctx(ctx));
+    if (dim < 1 || dim > 3) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "dim must be 1, 2 or 3 (got %d)", dim);
+    if (k < 1 || k > 64) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "k must be in 1..64 (got %d)", k);
+    if (ns < 1 || ns >= INT32_MAX || ne < 0 || ne >= INT32_MAX)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "point counts must be in [1, 2^31)");
+    if (k > ns) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "k = %d exceeds the number of data points (%lld)", k, (long long)ns);
+    if (!data || (!eval && ne > 0) || (!idx_out && ne > 0)) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null array");
+    InArray d, q;
+    OutArray o;
+    RBF_TRY(d.bind(ctx, data, sizeof(double) * ns * dim));
+    RBF_TRY(q.bind(ctx, eval, sizeof(double) * ne * dim));
+    RBF_TRY(o.bind(ctx, idx_out, sizeof(int32_t) * ne * k));
+    RBF_TRY(rbf_knn_device(ctx, d.as<double>(), ns, q.as<double>(), ne, dim, k, o.as<int32_t>()));
+    RBF_TRY(o.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
+int rbf_build_count(rbf_ctx *ctx, int64_t ns, int64_t ne, int32_t k, const rbf_hermite *herm,
+                    int64_t *row_ptr_out, int64_t *nnz_out) {
+    RBF_TRY(check_ctx(ctx));
+    if (k < 1 || ne < 0 || ns < 1) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid sizes");
+    if (herm && herm->is_boundary && ne > ns)
+        return rbf_fail(ctx, RBF_ERR_DIMENSION, "Hermite builds evaluate at the data points (ne <= ns)");
+    BoundaryDev b;
+    RBF_TRY(bind_boundary(ctx, herm, ns, 1, b));
+    OutArray rp;
+    RBF_TRY(rp.bind(ctx, row_ptr_out, sizeof(int64_t) * (ne + 1)));
+    int64_t nnz = 0;
+    RBF_TRY(rbf_count_rows_device(ctx, ne, k, b.any ? b.isb.as<uint8_t>() : nullptr, b.any ? b.g2b.as<int32_t>() : nullptr,
+                                  b.any ? b.alpha.as<double>() : nullptr, b.any ? b.beta.as<double>() : nullptr,
+                                  rp.as<int64_t>(), &nnz));
+    RBF_TRY(rp.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (nnz_out) *nnz_out = nnz;
+    return RBF_OK;
+}
+
+int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns, const double *eval,
+              int64_t ne, const int32_t *adjl, int32_t k, const rbf_hermite *herm, const int64_t *row_ptr,
+              int32_t *col, double *val, int8_t *status_out, rbf_build_stats *stats) {
+    RBF_TRY(check_ctx(ctx));
+    if (!cfg) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null configuration");
+    const int dim = cfg->dim;
+    if (dim < 1 || dim > 3) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "dim must be 1, 2 or 3 (got %d)", dim);
+    if (!(cfg->phs == 1 || cfg->phs == 3 || cfg->phs == 5 || cfg->phs == 7))
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "n must be 1, 3, 5, or 7 (got n=%d)", cfg->phs);
+    if (cfg->poly_deg < -1)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "poly_deg must be >= -1 (got %d)", cfg->poly_deg);
+    if (cfg->nops < 1 || cfg->nops > RBF_MAX_OPS)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "nops must be in 1..%d", RBF_MAX_OPS);
+    if (k < 1 || k > RBF_MAX_STENCIL) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "k must be in 1..%d", RBF_MAX_STENCIL);
+    if (k > ns) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "k exceeds the number of data points");
+    if (ns >= INT32_MAX || ne >= INT32_MAX || ne < 0) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "point counts must be < 2^31");
+    StencilParams P;
+    memset(&P, 0, sizeof P);
+    P.nmon = monomial_exponents(dim, cfg->poly_deg, P.exps);
+    if (k + P.nmon > RBF_MAX_SYSTEM)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "k + number of monomials (%d) exceeds %d", k + P.nmon, RBF_MAX_SYSTEM);
+    for (int r = 0; r < cfg->nops; r++) {
+        int c = cfg->op_code[r];
+        if (c < RBF_OP_IDENTITY || c > RBF_OP_LAPLACIAN) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "unknown operator code %d", c);
+        if ((c == RBF_OP_PARTIAL1 || c == RBF_OP_PARTIAL2) && (cfg->op_dim[r] < 0 || cfg->op_dim[r] >= dim))
+            return rbf_fail(ctx, RBF_ERR_ARGUMENT, "partial derivative dimension %d out of range", cfg->op_dim[r]);
+        P.op_code[r] = c;
+        P.op_dim[r] = (c == RBF_OP_PARTIAL1 || c == RBF_OP_PARTIAL2) ? cfg->op_dim[r] : 0;
+        P.op_order[r] = op_order(c);
+    }
+    if (herm && herm->is_boundary && ne > ns)
+        return rbf_fail(ctx, RBF_ERR_DIMENSION, "Hermite builds evaluate at the data points (ne <= ns)");
+    BoundaryDev b;
+    RBF_TRY(bind_boundary(ctx, herm, ns, dim, b));
+    if (b.any_nr)
+        for (int r = 0; r < cfg->nops; r++)
+            if (P.op_code[r] == RBF_OP_IDENTITY)  // _check_normal_form_support, src/solve/api.jl:79-94
+                return rbf_fail(ctx, RBF_ERR_UNSUPPORTED,
+                                "Neumann/Robin boundary conditions require the operator's basis action to support "
+                                "the normal-derivative form; the identity (regrid) has none");
+    InArray d, q, a, rp;
+    RBF_TRY(d.bind(ctx, data, sizeof(double) * ns * dim));
+    RBF_TRY(q.bind(ctx, eval, sizeof(double) * ne * dim));
+    RBF_TRY(a.bind(ctx, adjl, sizeof(int32_t) * ne * k));
+    RBF_TRY(rp.bind(ctx, row_ptr, sizeof(int64_t) * (ne + 1)));
+    bool idx_ok = true;
+    RBF_TRY(rbf_check_indices(ctx, a.as<int32_t>(), ne * (int64_t)k, (int32_t)ns, &idx_ok));
+    if (!idx_ok) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "adjl holds indices outside [0, %lld)", (long long)ns);
+    int64_t nnz = 0;
+    RBF_CUDA(ctx, cudaMemcpyAsync(&nnz, rp.as<int64_t>() + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (nnz < 0 || nnz > ne * (int64_t)k) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "row_ptr is not the layout of this build");
+    OutArray oc, ov, os;
+    RBF_TRY(oc.bind(ctx, col, sizeof(int32_t) * nnz));
+    RBF_TRY(ov.bind(ctx, val, sizeof(double) * nnz * cfg->nops));
+    RBF_TRY(os.bind(ctx, status_out, (size_t)ne));
+    DevBuf counters;
+    RBF_TRY(counters.alloc(ctx, sizeof(unsigned long long) * 8 + sizeof(double)));
+    RBF_CUDA(ctx, cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long) * 8 + sizeof(double), ctx->stream));
+
+    P.dim = dim;
+    P.phs = cfg->phs;
+    P.poly_deg = cfg->poly_deg;
+    P.k = k;
+    P.n = k + P.nmon;
+    P.nops = cfg->nops;
+    P.ne = ne;
+    P.ns = ns;
+    P.nnz = nnz;
+    P.data = d.as<double>();
+    P.eval = q.as<double>();
+    P.adjl = a.as<int32_t>();
+    P.isb = b.any ? b.isb.as<uint8_t>() : nullptr;
+    P.g2b = b.any ? b.g2b.as<int32_t>() : nullptr;
+    P.alpha = b.any ? b.alpha.as<double>() : nullptr;
+    P.beta = b.any ? b.beta.as<double>() : nullptr;
+    P.normals = b.any ? b.normals.as<double>() : nullptr;
+    P.row_ptr = rp.as<int64_t>();
+    P.col = oc.as<int32_t>();
+    P.val = ov.as<double>();
+    P.status = os.as<int8_t>();
+    P.counters = counters.as<unsigned long long>();
+    P.max_resid = reinterpret_cast<double *>(counters.as<unsigned long long>() + 8);
+    P.refine_steps = cfg->refine_steps > 0 ? cfg->refine_steps : 3;
+    P.tol = cfg->tol > 0 ? cfg->tol : 1e-12;
+
+    cudaEvent_t ev0, ev1;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    cudaEventRecord(ev0, ctx->stream);
+    int st;
+    if (cfg->precision == RBF_PREC_FP64)
+        st = rbf_build_fp64_launch(ctx, P);
+    else if (cfg->precision == RBF_PREC_FP32_REFINED)
+        st = rbf_build_fp32_launch(ctx, P);
+    else
+        st = rbf_fail(ctx, RBF_ERR_UNSUPPORTED, "precision mode %d is driven from the host (learned seed)", cfg->precision);
+    cudaEventRecord(ev1, ctx->stream);
+    if (st != RBF_OK) {
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+        return st;
+    }
+    unsigned long long hc[8];
+    double hres = 0.0;
+    RBF_CUDA(ctx, cudaMemcpyAsync(hc, counters.ptr, sizeof hc, cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaMemcpyAsync(&hres, P.max_resid, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_TRY(oc.finish(ctx));
+    RBF_TRY(ov.finish(ctx));
+    RBF_TRY(os.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    if (stats) {
+        stats->n_identity_rows = (int64_t)hc[3];
+        stats->n_stencils = ne - (int64_t)hc[3];
+        stats->n_singular = (int64_t)hc[0];
+        stats->n_fallback = (int64_t)hc[2];
+        stats->max_residual = hres;
+        stats->ms_build = ms;
+        stats->ms_knn = 0.f;
+        stats->ms_total = ms;
+    }
+    if (hc[1]) return rbf_fail(ctx, RBF_ERR_NOT_FOUND, "evaluation point not found in stencil data (%llu stencils)", hc[1]);
+    if (hc[0]) return rbf_fail(ctx, RBF_ERR_SINGULAR, "%llu stencil system(s) are singular", hc[0]);
+    return RBF_OK;
+}
+
+int rbf_spmm(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const int32_t *col, const double *val,
+             int32_t nf, int32_t layout, const double *X, int64_t ldx, double alpha, double beta, double *Y,
+             int64_t ldy) {
+    RBF_TRY(check_ctx(ctx));
+    if (nf < 1 || ne < 0 || ns < 0) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid sizes");
+    if (layout != 0 && layout != 1) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "layout must be 0 or 1");
+    if (layout == 0 && nf > 1 && (ldx < ns || ldy < ne)) return rbf_fail(ctx, RBF_ERR_DIMENSION, "leading dimension too small");
+    if (layout == 1 && (ldx < nf || ldy < nf)) return rbf_fail(ctx, RBF_ERR_DIMENSION, "leading dimension too small");
+    InArray rp, c, v, x;
+    RBF_TRY(rp.bind(ctx, row_ptr, sizeof(int64_t) * (ne + 1)));
+    if (rbf_is_device_ptr(col) && rbf_is_device_ptr(val)) {  // no staging: nnz not needed
+        c.dptr = col;
+        v.dptr = val;
+    } else {
+        int64_t nnz = 0;
+        RBF_CUDA(ctx, cudaMemcpyAsync(&nnz, rp.as<int64_t>() + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+        RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        RBF_TRY(c.bind(ctx, col, sizeof(int32_t) * nnz));
+        RBF_TRY(v.bind(ctx, val, sizeof(double) * nnz));
+    }
+    size_t xbytes = sizeof(double) * (size_t)(layout == 0 ? (nf > 1 ? ldx * (nf - 1) + ns : ns) : ns * ldx);
+    size_t ybytes = sizeof(double) * (size_t)(layout == 0 ? (nf > 1 ? ldy * (nf - 1) + ne : ne) : ne * ldy);
+    RBF_TRY(x.bind(ctx, X, xbytes));
+    OutArray y;
+    RBF_TRY(y.bind(ctx, Y, ybytes));
+    if (y.host && beta != 0.0) RBF_CUDA(ctx, cudaMemcpyAsync(y.dptr, Y, ybytes, cudaMemcpyHostToDevice, ctx->stream));
+    RBF_TRY(rbf_spmm_device(ctx, ne, ns, rp.as<int64_t>(), c.as<int32_t>(), v.as<double>(), nf, layout, x.as<double>(),
+                            nf == 1 ? 1 : ldx, alpha, beta, y.as<double>(), nf == 1 ? 1 : ldy));
+    RBF_TRY(y.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
+int rbf_csr_to_csc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const int32_t *col,
+                   const double *val, int64_t *col_ptr_out, int32_t *row_out, double *val_out) {
+    RBF_TRY(check_ctx(ctx));
+    InArray rp, c, v;
+    RBF_TRY(rp.bind(ctx, row_ptr, sizeof(int64_t) * (ne + 1)));
+    int64_t nnz = 0;
+    RBF_CUDA(ctx, cudaMemcpyAsync(&nnz, rp.as<int64_t>() + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    RBF_TRY(c.bind(ctx, col, sizeof(int32_t) * nnz));
+    RBF_TRY(v.bind(ctx, val, sizeof(double) * nnz));
+    OutArray cp, ro, vo;
+    RBF_TRY(cp.bind(ctx, col_ptr_out, sizeof(int64_t) * (ns + 1)));
+    RBF_TRY(ro.bind(ctx, row_out, sizeof(int32_t) * nnz));
+    RBF_TRY(vo.bind(ctx, val_out, sizeof(double) * nnz));
+    RBF_TRY(rbf_csr_to_csc_device(ctx, ne, ns, rp.as<int64_t>(), c.as<int32_t>(), v.as<double>(), cp.as<int64_t>(),
+                                  ro.as<int32_t>(), vo.as<double>()));
+    RBF_TRY(cp.finish(ctx));
+    RBF_TRY(ro.finish(ctx));
+    RBF_TRY(vo.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
+}  // extern "C"

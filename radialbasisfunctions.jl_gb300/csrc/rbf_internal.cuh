@@ -1,0 +1,118 @@
+// Internal declarations shared by the translation units of librbffd_gb300.so.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "rbffd.h"
+
+struct rbf_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    long long launches = 0;  // kernels launched through this context
+};
+
+int rbf_fail(rbf_ctx *ctx, int code, const char *fmt, ...);
+
+#define RBF_CUDA(ctx, expr)                                                                  \
+    do {                                                                                     \
+        cudaError_t e_ = (expr);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return rbf_fail((ctx), RBF_ERR_CUDA, "%s failed: %s", #expr, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define RBF_CHECK_LAUNCH(ctx)                                                                \
+    do {                                                                                     \
+        (ctx)->launches++;                                                                   \
+        RBF_CUDA(ctx, cudaGetLastError());                                                   \
+    } while (0)
+
+#define RBF_TRY(expr)             \
+    do {                          \
+        int s_ = (expr);          \
+        if (s_ != RBF_OK) return s_; \
+    } while (0)
+
+// Stream-ordered device buffer owned by a host scope.
+struct DevBuf {
+    void *ptr = nullptr;
+    cudaStream_t stream = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() {
+        if (ptr) cudaFreeAsync(ptr, stream);
+    }
+    int alloc(rbf_ctx *ctx, size_t bytes) {
+        stream = ctx->stream;
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMallocAsync(&ptr, bytes, stream);
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            return rbf_fail(ctx, RBF_ERR_CUDA, "device allocation of %zu bytes failed: %s", bytes,
+                            cudaGetErrorString(e));
+        }
+        return RBF_OK;
+    }
+    template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// An input array that may live on the host or the device; host data is staged to the
+// device on the context stream.
+struct InArray {
+    const void *dptr = nullptr;
+    DevBuf staged;
+    int bind(rbf_ctx *ctx, const void *p, size_t bytes);
+    template <class T> const T *as() const { return static_cast<const T *>(dptr); }
+};
+
+// An output array that may live on the host or the device; host outputs are written
+// through a device staging buffer and copied back by finish().
+struct OutArray {
+    void *user = nullptr;
+    void *dptr = nullptr;
+    size_t bytes = 0;
+    bool host = false;
+    DevBuf staged;
+    int bind(rbf_ctx *ctx, void *p, size_t bytes_);
+    int finish(rbf_ctx *ctx);
+    template <class T> T *as() const { return static_cast<T *>(dptr); }
+};
+
+bool rbf_is_device_ptr(const void *p);
+
+// ---- kernels (launch wrappers), one per translation unit --------------------------
+struct KnnGrid;  // opaque grid description (knn.cu)
+
+int rbf_knn_device(rbf_ctx *ctx, const double *d_data, int64_t ns, const double *d_eval, int64_t ne,
+                   int dim, int k, int32_t *d_idx);
+
+struct StencilParams;  // stencil.cuh
+
+int rbf_count_rows_device(rbf_ctx *ctx, int64_t ne, int k, const uint8_t *d_isb,
+                          const int32_t *d_g2b, const double *d_alpha, const double *d_beta,
+                          int64_t *d_row_ptr, int64_t *nnz);
+
+int rbf_boundary_map_device(rbf_ctx *ctx, int64_t n, const uint8_t *d_isb, int32_t *d_g2b,
+                            int64_t *n_boundary);
+
+int rbf_check_indices(rbf_ctx *ctx, const int32_t *d_idx, int64_t n, int32_t hi, bool *ok);
+int rbf_exclusive_scan_i64(rbf_ctx *ctx, const int64_t *d_in, int64_t *d_out, int64_t n,
+                           int64_t *total);
+int rbf_exclusive_scan_i32(rbf_ctx *ctx, const int32_t *d_in, int32_t *d_out, int64_t n,
+                           int64_t *total);
+
+int rbf_spmm_device(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *d_row_ptr,
+                    const int32_t *d_col, const double *d_val, int nf, int layout,
+                    const double *d_X, int64_t ldx, double alpha, double beta, double *d_Y,
+                    int64_t ldy);
+
+int rbf_csr_to_csc_device(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *d_row_ptr,
+                          const int32_t *d_col, const double *d_val, int64_t *d_col_ptr,
+                          int32_t *d_row, double *d_valc);

@@ -1,0 +1,228 @@
+// Sparse apply Y = alpha * W X + beta * Y (replaces _eval_op / mul!,
+// src/operators/operators.jl:217-218 and 529-542, a SparseMatrixCSC product) and the
+// CSR -> CSC transpose (the layout _construct_sparse returns, src/solve/execution.jl:105-115).
+//
+// Single field: a group of TPR lanes per row; the groups of a warp cover consecutive rows,
+// so val/col are streamed contiguously and each lane keeps several loads in flight.
+// Several interleaved fields (X[i*ldx + f]): lanes are fields, a row's (val, col) pair is
+// a broadcast load and each gather of x is one contiguous run of nf doubles.
+// Column-major fields (a Julia Matrix) are transposed to interleaved scratch first.
+// Roofline: HBM bandwidth; algorithmic bytes nnz*(8+4) + (ne+1)*8 + nf*(ns+ne)*8.
+#include <algorithm>
+
+#include "rbf_internal.cuh"
+
+namespace {
+
+template <int TPR>
+__global__ void __launch_bounds__(256) spmv_kernel(int64_t ne, const int64_t *__restrict__ rp,
+                                                   const int32_t *__restrict__ col,
+                                                   const double *__restrict__ val,
+                                                   const double *__restrict__ x, double alpha, double beta,
+                                                   double *__restrict__ y) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int sub = threadIdx.x % TPR;
+    const int64_t groups = (int64_t)gridDim.x * blockDim.x / TPR;
+    // warp-uniform trip count: every lane of a warp runs the same iterations
+    const int64_t first = (tid / 32) * (32 / TPR);
+    for (int64_t r0 = first; r0 < ne; r0 += groups) {
+        const int64_t r = r0 + (threadIdx.x & 31) / TPR;
+        const bool live = r < ne;
+        const int64_t a = live ? rp[r] : 0, b = live ? rp[r + 1] : 0;
+        double s0 = 0.0, s1 = 0.0;
+        int64_t p = a + sub;
+        for (; p + TPR < b; p += 2 * TPR) {
+            s0 = fma(__ldg(&val[p]), __ldg(&x[__ldg(&col[p])]), s0);
+            s1 = fma(__ldg(&val[p + TPR]), __ldg(&x[__ldg(&col[p + TPR])]), s1);
+        }
+        if (p < b) s0 = fma(__ldg(&val[p]), __ldg(&x[__ldg(&col[p])]), s0);
+        double s = s0 + s1;
+#pragma unroll
+        for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
+        if (sub == 0 && live) y[r] = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * y[r]);
+    }
+}
+
+// lanes = fields (nf <= 32), 32/nfp rows per warp, nfp = nf rounded up to a power of two
+__global__ void __launch_bounds__(256) spmm_interleaved_kernel(int64_t ne, const int64_t *__restrict__ rp,
+                                                               const int32_t *__restrict__ col,
+                                                               const double *__restrict__ val, int nf, int nfp,
+                                                               const double *__restrict__ X, int64_t ldx,
+                                                               double alpha, double beta, double *__restrict__ Y,
+                                                               int64_t ldy) {
+    const int lane = threadIdx.x & 31;
+    const int f = lane % nfp;
+    const int rows_per_warp = 32 / nfp;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r0 = warp * rows_per_warp; r0 < ne; r0 += nwarps * rows_per_warp) {
+        const int64_t r = r0 + lane / nfp;
+        if (r >= ne || f >= nf) continue;
+        const int64_t a = rp[r], b = rp[r + 1];
+        double s0 = 0.0, s1 = 0.0;
+        int64_t p = a;
+        for (; p + 1 < b; p += 2) {
+            s0 = fma(__ldg(&val[p]), __ldg(&X[(int64_t)__ldg(&col[p]) * ldx + f]), s0);
+            s1 = fma(__ldg(&val[p + 1]), __ldg(&X[(int64_t)__ldg(&col[p + 1]) * ldx + f]), s1);
+        }
+        if (p < b) s0 = fma(__ldg(&val[p]), __ldg(&X[(int64_t)__ldg(&col[p]) * ldx + f]), s0);
+        const double s = s0 + s1;
+        double *yp = &Y[r * ldy + f];
+        *yp = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * *yp);
+    }
+}
+
+// out[i*nf + f] = in[f*ld + i] (tiled through shared memory)
+__global__ void to_interleaved_kernel(int64_t n, int nf, const double *__restrict__ in, int64_t ld,
+                                      double *__restrict__ out) {
+    __shared__ double tile[32][33];
+    const int64_t i0 = (int64_t)blockIdx.x * 32;
+    const int f0 = blockIdx.y * 32;
+    for (int fy = threadIdx.y; fy < 32; fy += blockDim.y) {
+        int f = f0 + fy;
+        int64_t i = i0 + threadIdx.x;
+        tile[fy][threadIdx.x] = (f < nf && i < n) ? in[(int64_t)f * ld + i] : 0.0;
+    }
+    __syncthreads();
+    for (int iy = threadIdx.y; iy < 32; iy += blockDim.y) {
+        int64_t i = i0 + iy;
+        int f = f0 + threadIdx.x;
+        if (i < n && f < nf) out[i * nf + f] = tile[threadIdx.x][iy];
+    }
+}
+
+// out[f*ld + i] = in[i*nf + f]
+__global__ void from_interleaved_kernel(int64_t n, int nf, const double *__restrict__ in,
+                                        double *__restrict__ out, int64_t ld) {
+    __shared__ double tile[32][33];
+    const int64_t i0 = (int64_t)blockIdx.x * 32;
+    const int f0 = blockIdx.y * 32;
+    for (int iy = threadIdx.y; iy < 32; iy += blockDim.y) {
+        int64_t i = i0 + iy;
+        int f = f0 + threadIdx.x;
+        tile[iy][threadIdx.x] = (i < n && f < nf) ? in[i * nf + f] : 0.0;
+    }
+    __syncthreads();
+    for (int fy = threadIdx.y; fy < 32; fy += blockDim.y) {
+        int f = f0 + fy;
+        int64_t i = i0 + threadIdx.x;
+        if (f < nf && i < n) out[(int64_t)f * ld + i] = tile[threadIdx.x][fy];
+    }
+}
+
+__global__ void csc_count_kernel(int64_t nnz, const int32_t *__restrict__ col, int64_t *__restrict__ cnt) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnz; p += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd((unsigned long long *)&cnt[col[p]], 1ull);
+}
+
+__global__ void csc_scatter_kernel(int64_t ne, const int64_t *__restrict__ rp, const int32_t *__restrict__ col,
+                                   const double *__restrict__ val, const int64_t *__restrict__ cp,
+                                   unsigned long long *__restrict__ fill, int32_t *__restrict__ row_out,
+                                   double *__restrict__ val_out) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < ne; r += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t p = rp[r]; p < rp[r + 1]; p++) {
+            int32_t c = col[p];
+            int64_t q = cp[c] + (int64_t)atomicAdd(&fill[c], 1ull);
+            row_out[q] = (int32_t)r;
+            val_out[q] = val[p];
+        }
+}
+
+// rows within each column ascending (insertion sort; columns hold about k entries)
+__global__ void csc_sort_kernel(int64_t ns, const int64_t *__restrict__ cp, int32_t *__restrict__ row,
+                                double *__restrict__ v) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ns; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t a = cp[c], b = cp[c + 1];
+        for (int64_t i = a + 1; i < b; i++) {
+            int32_t rr = row[i];
+            double vv = v[i];
+            int64_t j = i - 1;
+            while (j >= a && row[j] > rr) {
+                row[j + 1] = row[j];
+                v[j + 1] = v[j];
+                j--;
+            }
+            row[j + 1] = rr;
+            v[j + 1] = vv;
+        }
+    }
+}
+
+int blocks_for(rbf_ctx *ctx, int64_t work, int threads, int per_sm) {
+    int64_t b = (work + threads - 1) / threads;
+    b = std::min<int64_t>(b, (int64_t)ctx->num_sms * per_sm);
+    return (int)std::max<int64_t>(b, 1);
+}
+
+}  // namespace
+
+int rbf_spmm_device(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *d_rp, const int32_t *d_col,
+                    const double *d_val, int nf, int layout, const double *d_X, int64_t ldx, double alpha,
+                    double beta, double *d_Y, int64_t ldy) {
+    if (ne == 0 || nf == 0) return RBF_OK;
+    if (nf == 1) {
+        const int TPR = 8;
+        spmv_kernel<TPR><<<blocks_for(ctx, ne * TPR, 256, 16), 256, 0, ctx->stream>>>(ne, d_rp, d_col, d_val, d_X,
+                                                                                      alpha, beta, d_Y);
+        RBF_CHECK_LAUNCH(ctx);
+        return RBF_OK;
+    }
+    const double *Xi = d_X;
+    double *Yi = d_Y;
+    int64_t lx = ldx, ly = ldy;
+    DevBuf xs, ys;
+    if (layout == 0) {  // column-major: stage through interleaved scratch
+        RBF_TRY(xs.alloc(ctx, sizeof(double) * ns * nf));
+        RBF_TRY(ys.alloc(ctx, sizeof(double) * ne * nf));
+        dim3 tb(32, 8);
+        to_interleaved_kernel<<<dim3((unsigned)((ns + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
+            ns, nf, d_X, ldx, xs.as<double>());
+        RBF_CHECK_LAUNCH(ctx);
+        if (beta != 0.0) {
+            to_interleaved_kernel<<<dim3((unsigned)((ne + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
+                ne, nf, d_Y, ldy, ys.as<double>());
+            RBF_CHECK_LAUNCH(ctx);
+        }
+        Xi = xs.as<double>();
+        Yi = ys.as<double>();
+        lx = nf;
+        ly = nf;
+    }
+    for (int f0 = 0; f0 < nf; f0 += 32) {
+        int nfc = std::min(32, nf - f0);
+        int nfp = 1;
+        while (nfp < nfc) nfp <<= 1;
+        int64_t warps = (ne + (32 / nfp) - 1) / (32 / nfp);
+        spmm_interleaved_kernel<<<blocks_for(ctx, warps * 32, 256, 16), 256, 0, ctx->stream>>>(
+            ne, d_rp, d_col, d_val, nfc, nfp, Xi + f0, lx, alpha, beta, Yi + f0, ly);
+        RBF_CHECK_LAUNCH(ctx);
+    }
+    if (layout == 0) {
+        dim3 tb(32, 8);
+        from_interleaved_kernel<<<dim3((unsigned)((ne + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
+            ne, nf, Yi, d_Y, ldy);
+        RBF_CHECK_LAUNCH(ctx);
+    }
+    return RBF_OK;
+}
+
+int rbf_csr_to_csc_device(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *d_rp, const int32_t *d_col,
+                          const double *d_val, int64_t *d_cp, int32_t *d_row, double *d_valc) {
+    int64_t nnz = 0;
+    RBF_CUDA(ctx, cudaMemcpyAsync(&nnz, d_rp + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    DevBuf cnt, fill;
+    RBF_TRY(cnt.alloc(ctx, sizeof(int64_t) * (ns + 1)));
+    RBF_TRY(fill.alloc(ctx, sizeof(int64_t) * (ns + 1)));
+    RBF_CUDA(ctx, cudaMemsetAsync(cnt.ptr, 0, sizeof(int64_t) * (ns + 1), ctx->stream));
+    RBF_CUDA(ctx, cudaMemsetAsync(fill.ptr, 0, sizeof(int64_t) * (ns + 1), ctx->stream));
+    csc_count_kernel<<<blocks_for(ctx, nnz, 256, 8), 256, 0, ctx->stream>>>(nnz, d_col, cnt.as<int64_t>());
+    RBF_CHECK_LAUNCH(ctx);
+    RBF_TRY(rbf_exclusive_scan_i64(ctx, cnt.as<int64_t>(), d_cp, ns + 1, nullptr));
+    csc_scatter_kernel<<<blocks_for(ctx, ne, 256, 8), 256, 0, ctx->stream>>>(
+        ne, d_rp, d_col, d_val, d_cp, fill.as<unsigned long long>(), d_row, d_valc);
+    RBF_CHECK_LAUNCH(ctx);
+    csc_sort_kernel<<<blocks_for(ctx, ns, 256, 8), 256, 0, ctx->stream>>>(ns, d_cp, d_row, d_valc);
+    RBF_CHECK_LAUNCH(ctx);
+    return RBF_OK;
+}

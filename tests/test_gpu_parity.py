@@ -1,0 +1,297 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Bars (from the target specification of the drop-in path):
+  neighbour indices and CSR structure bit-exact; FP64 weights within 1e-8 relative per
+  stencil (row max-norm); applied results within 1e-10 relative.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+W_TOL = 1e-8      # per-stencil relative weight error
+APPLY_TOL = 1e-10  # relative error of W @ x
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import __graft_entry__ as g
+    g.build()
+    return g.load_package()
+
+
+def row_rel_err(row_ptr, v, vref):
+    """max over rows of max|v - vref| / max|vref| (row-norm relative error)."""
+    ne = len(row_ptr) - 1
+    rows = np.repeat(np.arange(ne), np.diff(row_ptr))
+    num = np.zeros(ne)
+    den = np.zeros(ne)
+    np.maximum.at(num, rows, np.abs(v - vref))
+    np.maximum.at(den, rows, np.abs(vref))
+    den[den == 0] = 1.0
+    return float((num / den).max())
+
+
+def check_against(W, row_ptr, col, val, tol=W_TOL):
+    assert np.array_equal(W.row_ptr.cpu().numpy(), row_ptr)
+    assert np.array_equal(W.col.cpu().numpy(), col)
+    err = row_rel_err(row_ptr, W.val.cpu().numpy(), val)
+    assert err <= tol, f"row-relative weight error {err:.3e} > {tol}"
+    return err
+
+
+# ---------------------------------------------------------------------------- kNN
+@pytest.mark.parametrize("dim,k,n", [(1, 7, 500), (2, 20, 5000), (2, 30, 3000), (3, 30, 8000), (3, 40, 6000)])
+def test_knn_matches_oracle(pkg, orc, dim, k, n):
+    rng = np.random.default_rng(100 + dim * k)
+    X = rng.uniform(0, 1, (n, dim))
+    Q = np.concatenate([X[: n // 2], rng.uniform(-0.3, 1.3, (n // 4, dim))])
+    got = pkg.find_neighbors(torch.from_numpy(X).cuda(), torch.from_numpy(Q).cuda(), k).cpu().numpy()
+    assert np.array_equal(got, orc.knn(X, Q, k))
+    # host inputs take the same path (staged through the context stream)
+    got_h = pkg.find_neighbors(X, Q, k)
+    assert np.array_equal(got_h, got)
+
+
+def test_knn_ties_by_index(pkg, orc):
+    """Exact distance ties (lattice) are broken by point index; self first (test/utils.jl:28-43)."""
+    g = np.stack(np.meshgrid(np.arange(20.0), np.arange(20.0), indexing="ij"), -1).reshape(-1, 2) * 0.05
+    got = pkg.find_neighbors(g, k=15)
+    assert np.array_equal(got, orc.knn(g, g, 15, brute=True))
+    assert (got[:, 0] == np.arange(len(g))).all()
+    pts = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [2.0, 2.0]])
+    adj = pkg.find_neighbors(pts, k=2)
+    assert adj[0, 1] == 1 and adj[3, 1] != 0
+
+
+def test_knn_clustered_queries(pkg, orc):
+    """Regrid-like queries: half uniform, half from narrow Gaussian clusters."""
+    rng = np.random.default_rng(5)
+    S = rng.uniform(0, 1, (20000, 3))
+    c = rng.uniform(0.2, 0.8, (8, 3))
+    T = np.clip(np.concatenate([rng.uniform(0, 1, (3000, 3)),
+                                c[rng.integers(0, 8, 3000)] + 0.05 * rng.standard_normal((3000, 3))]), 0, 1)
+    got = pkg.find_neighbors(S, T, 20)
+    assert np.array_equal(got, orc.knn(S, T, 20))
+
+
+# ---------------------------------------------------------------------------- builds vs golden fixtures
+def test_lap2d_golden(pkg):
+    z = np.load(os.path.join(GOLD, "oracle_small_lap2d.npz"))
+    X = torch.from_numpy(z["points"]).cuda()
+    adjl = pkg.find_neighbors(X, k=20)
+    assert np.array_equal(adjl.cpu().numpy(), z["adjl"])
+    op = pkg.laplacian(X, basis=pkg.PHS(3, poly_deg=2), k=20, adjl=adjl)
+    check_against(op.weights, z["row_ptr"], z["col"], z["val"][0])
+
+
+def test_grad_lap3d_golden(pkg):
+    z = np.load(os.path.join(GOLD, "oracle_small_grad_lap3d.npz"))
+    X = torch.from_numpy(z["points"]).cuda()
+    adjl = pkg.find_neighbors(X, k=40)
+    assert np.array_equal(adjl.cpu().numpy(), z["adjl"])
+    op = pkg.RadialBasisOperator(pkg.Operators(pkg.Jacobian(3), pkg.Laplacian()), X, basis=pkg.PHS(5, poly_deg=2),
+                                 k=40, adjl=adjl)
+    for i in range(4):
+        check_against(op.weights[i], z["row_ptr"], z["col"], z["val"][i])
+    # the reference builds gradient and Laplacian separately: same weights
+    g = pkg.gradient(X, basis=pkg.PHS(5, poly_deg=2), k=40, adjl=adjl)
+    for i in range(3):
+        check_against(g.weights[i], z["row_ptr"], z["col"], z["val"][i])
+
+
+def test_regrid3d_golden(pkg):
+    z = np.load(os.path.join(GOLD, "oracle_small_regrid3d.npz"))
+    S, T = torch.from_numpy(z["src"]).cuda(), torch.from_numpy(z["tgt"]).cuda()
+    adjl = pkg.find_neighbors(S, T, 20)
+    assert np.array_equal(adjl.cpu().numpy(), z["adjl"])
+    op = pkg.regrid(S, T, basis=pkg.PHS(3, poly_deg=1), k=20, adjl=adjl)
+    check_against(op.weights, z["row_ptr"], z["col"], z["val"][0])
+
+
+# ---------------------------------------------------------------------------- builds vs oracle, more shapes
+@pytest.mark.parametrize("phs,deg,dim,k,op", [
+    (1, 1, 2, 12, ("lap",)), (3, 3, 2, 30, ("lap",)), (7, 2, 2, 20, ("d2", 1)), (5, 1, 3, 20, ("d1", 2)),
+    (3, 0, 3, 10, ("lap",)), (3, -1, 2, 8, ("d1", 1)), (5, 3, 3, 40, ("lap",)), (3, 2, 1, 7, ("d2", 1)),
+])
+def test_build_matches_oracle(pkg, orc, phs, deg, dim, k, op):
+    rng = np.random.default_rng(phs * 100 + deg * 10 + dim)
+    X = rng.uniform(0, 1, (1500, dim))
+    adjl = orc.knn(X, X, k)
+    if op[0] == "lap":
+        L, ops = pkg.Laplacian(), [(orc.OP_LAP, 0)]
+    elif op[0] == "d1":
+        L, ops = pkg.Partial(1, op[1]), [(orc.OP_D1, op[1] - 1)]
+    else:
+        L, ops = pkg.Partial(2, op[1]), [(orc.OP_D2, op[1] - 1)]
+    ref = orc.build(X, X, adjl, dim, phs, deg, ops)
+    o = pkg.RadialBasisOperator(L, torch.from_numpy(X).cuda(), basis=pkg.PHS(phs, poly_deg=deg), k=k,
+                                adjl=torch.from_numpy(adjl).cuda())
+    check_against(o.weights, ref.row_ptr, ref.col, ref.val[0])
+
+
+def test_apply_matches_oracle(pkg, orc):
+    z = np.load(os.path.join(GOLD, "oracle_small_lap2d.npz"))
+    X = z["points"]
+    op = pkg.laplacian(torch.from_numpy(X).cuda(), k=20, adjl=torch.from_numpy(z["adjl"]).cuda())
+    ref = orc.CSR(z["row_ptr"], z["col"], z["val"], None, (len(X), len(X)))
+    f = np.sin(4 * X[:, 0]) * np.cos(3 * X[:, 1])
+    y = op(torch.from_numpy(f).cuda()).cpu().numpy()
+    yr = orc.spmm(ref, f)
+    assert np.abs(y - yr).max() <= APPLY_TOL * np.abs(yr).max()
+    # host operand, host result
+    yh = op(f)
+    assert isinstance(yh, np.ndarray) and np.abs(yh - yr).max() <= APPLY_TOL * np.abs(yr).max()
+    # several fields, both layouts; mul! 5-argument form (operators.jl:536-542)
+    rng = np.random.default_rng(0)
+    F = rng.standard_normal((len(X), 5))
+    YR = orc.spmm(ref, F)
+    Y = op(torch.from_numpy(F).cuda()).cpu().numpy()
+    assert np.abs(Y - YR).max() <= APPLY_TOL * np.abs(YR).max()
+    Yi = op.weights.apply(torch.from_numpy(F).cuda(), layout="interleaved").cpu().numpy()
+    assert np.abs(Yi - YR).max() <= APPLY_TOL * np.abs(YR).max()
+    y0 = rng.standard_normal(len(X))
+    out = pkg.mul(y0.copy(), op, f, 2.0, -0.5)
+    assert np.abs(out - (2.0 * yr - 0.5 * y0)).max() <= APPLY_TOL * np.abs(yr).max() * 3
+
+
+def test_csc_matches_scipy(pkg):
+    z = np.load(os.path.join(GOLD, "oracle_small_regrid3d.npz"))
+    op = pkg.regrid(z["src"], z["tgt"], basis=pkg.PHS(3, poly_deg=1), k=20)
+    cp, rw, vv = op.weights.to_csc()
+    M = op.weights.to_scipy().tocsc()
+    M.sort_indices()
+    assert np.array_equal(cp.cpu().numpy(), M.indptr)
+    assert np.array_equal(rw.cpu().numpy(), M.indices)
+    assert np.array_equal(vv.cpu().numpy(), M.data)
+
+
+# ---------------------------------------------------------------------------- Hermite
+def _twelve(orc_unused=None):
+    import json
+    g = json.load(open(os.path.join(GOLD, "reference_known_answers.json")))["hermite_12pt"]
+    return g
+
+
+@pytest.mark.parametrize("case", ["dirichlet", "neumann", "mixed", "robin"])
+def test_hermite_12pt(pkg, orc, case):
+    g = _twelve()
+    X = np.array(g["points"])
+    isb = np.array(g["is_boundary"], dtype=np.uint8)
+    normals = np.array(g["normals"])
+    spec = g["cases"][case]
+    bcs = [pkg.BoundaryCondition(a, b) for a, b in zip(spec["alpha"], spec["beta"])]
+    op = pkg.laplacian(X, basis=pkg.PHS(3, poly_deg=2), k=12,
+                       hermite=dict(is_boundary=isb.astype(bool), bc=bcs, normals=normals))
+    adjl = orc.knn(X, X, 12)
+    ref = orc.build(X, X, adjl, 2, 3, 2, [(orc.OP_LAP, 0)],
+                    hermite=(isb, np.array(spec["alpha"]), np.array(spec["beta"]), normals))
+    check_against(op.weights, ref.row_ptr, ref.col, ref.val[0])
+    u = np.array([eval(spec["u"], {"x": p[0], "y": p[1]}) for p in X])
+    r = op(u)
+    assert np.abs(r[isb == 0] - spec["lap"]).max() < 1e-10
+
+
+def _square_441():
+    xs = np.round(np.arange(0.0, 1.0 + 1e-12, 0.05), 12)
+    X = np.array([(x, y) for x in xs for y in xs])
+    isb = ((X[:, 0] == 0) | (X[:, 0] == 1) | (X[:, 1] == 0) | (X[:, 1] == 1))
+    normals, alpha, beta = [], [], []
+    for x, y in X[isb]:
+        n = np.zeros(2)
+        n += [-1, 0] if x == 0 else ([1, 0] if x == 1 else [0, 0])
+        n += [0, -1] if y == 0 else ([0, 1] if y == 1 else [0, 0])
+        normals.append(n / np.linalg.norm(n))
+        if y == 0 or y == 1:
+            alpha.append(1.0), beta.append(0.0)
+        elif x == 0:
+            alpha.append(0.5), beta.append(0.5)
+        else:
+            alpha.append(0.0), beta.append(1.0)
+    return X, isb, np.array(normals), np.array(alpha), np.array(beta)
+
+
+def test_hermite_441_end_to_end(pkg, orc):
+    """Mixed Dirichlet / Robin / Neumann square (laplacian_end_to_end.jl): forward exactness and
+    parity with the oracle, including the Neumann/Robin eval-node polynomial right-hand side."""
+    X, isb, normals, alpha, beta = _square_441()
+    bcs = [pkg.BoundaryCondition(a, b) for a, b in zip(alpha, beta)]
+    adjl = pkg.find_neighbors(X, k=15)
+    op = pkg.laplacian(X, basis=pkg.PHS(3, poly_deg=2), k=15, adjl=adjl,
+                       hermite=dict(is_boundary=isb, bc=bcs, normals=normals))
+    ref = orc.build(X, X, adjl, 2, 3, 2, [(orc.OP_LAP, 0)], hermite=(isb.astype(np.uint8), alpha, beta, normals))
+    check_against(op.weights, ref.row_ptr, ref.col, ref.val[0])
+    f = X[:, 0] ** 2 + X[:, 1] ** 2 + 1.0
+    u = f.copy()
+    bi = np.nonzero(isb)[0]
+    for b, i in enumerate(bi):
+        gval = 2 * X[i] @ normals[b]
+        if alpha[b] == 0:
+            u[i] = gval
+        elif beta[b] != 0:
+            u[i] = 0.5 * f[i] + 0.5 * gval
+    r = op(u)
+    err = r[~isb] - 4.0
+    assert np.abs(err).max() < 1e-10 and math.sqrt((err ** 2).mean()) < 1e-11
+
+
+def test_hermite_gradient_robin(pkg, orc):
+    """Jacobian with Neumann/Robin neighbours: one factorisation, D normal-form right-hand sides."""
+    X, isb, normals, alpha, beta = _square_441()
+    bcs = [pkg.BoundaryCondition(a, b) for a, b in zip(alpha, beta)]
+    adjl = orc.knn(X, X, 15)
+    op = pkg.gradient(X, basis=pkg.PHS(3, poly_deg=2), k=15, adjl=adjl,
+                      hermite=dict(is_boundary=isb, bc=bcs, normals=normals))
+    ref = orc.build(X, X, adjl, 2, 3, 2, [(orc.OP_D1, 0), (orc.OP_D1, 1)],
+                    hermite=(isb.astype(np.uint8), alpha, beta, normals))
+    for i in range(2):
+        check_against(op.weights[i], ref.row_ptr, ref.col, ref.val[i])
+
+
+# ---------------------------------------------------------------------------- FP32 + refinement
+@pytest.mark.parametrize("which", ["lap2d", "grad_lap3d", "regrid3d"])
+def test_fp32_refined_equal_error(pkg, which):
+    z = np.load(os.path.join(GOLD, f"oracle_small_{which}.npz"))
+    if which == "lap2d":
+        X = torch.from_numpy(z["points"]).cuda()
+        ops, basis, data, ev = [(3, 0)], pkg.PHS(3, poly_deg=2), X, None
+    elif which == "grad_lap3d":
+        X = torch.from_numpy(z["points"]).cuda()
+        ops, basis, data, ev = [(1, 0), (1, 1), (1, 2), (3, 0)], pkg.PHS(5, poly_deg=2), X, None
+    else:
+        data, ev = torch.from_numpy(z["src"]).cuda(), torch.from_numpy(z["tgt"]).cuda()
+        ops, basis = [(0, 0)], pkg.PHS(3, poly_deg=1)
+    adjl = torch.from_numpy(z["adjl"]).cuda()
+    Ws, status = pkg.build_weights(ops, data, ev, adjl, basis, precision="fp32_refined", return_status=True)
+    for i, W in enumerate(Ws):
+        check_against(W, z["row_ptr"], z["col"], z["val"][i])
+    st = status.cpu().numpy()
+    assert set(np.unique(st)) <= {0, 3}
+
+
+# ---------------------------------------------------------------------------- errors
+def test_errors(pkg):
+    X = np.random.default_rng(0).uniform(0, 1, (100, 2))
+    with pytest.raises(ValueError):
+        pkg.find_neighbors(X, k=101)
+    with pytest.raises(ValueError):
+        pkg.PHS(4)
+    with pytest.raises(ValueError):
+        pkg.PHS(3, poly_deg=-2)
+    Xd = np.concatenate([X, X[:1]])  # a duplicated point makes its stencils singular
+    with pytest.raises(pkg.SingularException):
+        pkg.laplacian(Xd, k=12)
+    isb = np.zeros(100, dtype=bool)
+    isb[:3] = True
+    with pytest.raises(pkg.DimensionMismatch):
+        pkg.laplacian(X, hermite=dict(is_boundary=isb, bc=[pkg.Neumann()] * 2, normals=np.zeros((2, 2))))
+    with pytest.raises(ValueError):  # regrid has no normal form (api.jl:79-94)
+        pkg.RadialBasisOperator(pkg.Regrid(), X, hermite=dict(is_boundary=isb, bc=[pkg.Neumann()] * 3,
+                                                              normals=np.ones((3, 2))))
