@@ -64,9 +64,10 @@ typedef struct rbf_build_cfg {
     int32_t op_code[RBF_MAX_OPS]; /* enum rbf_op_code                               */
     int32_t op_dim[RBF_MAX_OPS];  /* 0-based dimension of partial derivatives       */
     int32_t precision;            /* enum rbf_precision                             */
-    int32_t refine_steps;         /* max refinement steps for FP32 paths (0: default 3) */
-    double tol;                   /* FP32 paths: accept when the FP64 residual, relative
-                                     to the right-hand side, is below tol (0: default 1e-12) */
+    int32_t refine_steps;         /* max refinement steps for FP32 paths (0: default 6) */
+    double tol;                   /* FP32 paths: accept when the correction computed from the
+                                     FP64 residual is below tol relative to the weights
+                                     (0: default 1e-9); otherwise the FP64 solve is used */
 } rbf_build_cfg;
 
 /* Hermite boundary description (src/solve/types.jl:18-42,178-182).  Boundary
@@ -87,7 +88,8 @@ typedef struct rbf_build_stats {
     int64_t n_identity_rows; /* Dirichlet eval rows                                 */
     int64_t n_fallback;      /* FP32 paths: stencils that fell back to the FP64 solve */
     int64_t n_singular;      /* stencils with an exactly singular system            */
-    double max_residual;     /* FP32 paths: largest accepted relative FP64 residual   */
+    double max_residual;     /* FP32 paths: largest accepted relative correction (error
+                                estimate of the accepted weights)                      */
     float ms_knn, ms_build, ms_total;
 } rbf_build_stats;
 

@@ -341,8 +341,8 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
     P.status = os.as<int8_t>();
     P.counters = counters.as<unsigned long long>();
     P.max_resid = reinterpret_cast<double *>(counters.as<unsigned long long>() + 8);
-    P.refine_steps = cfg->refine_steps > 0 ? cfg->refine_steps : 3;
-    P.tol = cfg->tol > 0 ? cfg->tol : 1e-12;
+    P.refine_steps = cfg->refine_steps > 0 ? cfg->refine_steps : 6;
+    P.tol = cfg->tol > 0 ? cfg->tol : 1e-9;
 
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);

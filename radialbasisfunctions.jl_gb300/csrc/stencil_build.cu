@@ -145,6 +145,7 @@ __device__ int load_stencil(const StencilParams &P, int64_t e, const WarpSmem &w
 __device__ void assemble_fp64(const StencilParams &P, const WarpSmem &w, int lane, int es, int eval_local) {
     const int k = P.k, n = P.n, nops = P.nops, ld = mat_ld(n, nops), dim = P.dim, nmon = P.nmon;
     const bool herm = eval_local != -2;
+    const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
     for (int t = lane; t < n * ld; t += 32) w.M[t] = 0.0;
     __syncwarp();
     // RBF block, upper triangle pairs (i <= j) mirrored
@@ -161,7 +162,7 @@ __device__ void assemble_fp64(const StencilParams &P, const WarpSmem &w, int lan
             v = phs_phi_r2<double>(P.phs, sq_norm(D, dim));
         } else {
             v = colloc_entry<double>(P.phs, dim, &w.X[i * 3], &w.X[j * 3], w.ptype[i], w.ptype[j], w.HA[i], w.HB[i],
-                                     &w.HN[i * 3], w.HA[j], w.HB[j], &w.HN[j * 3]);
+                                     &w.HN[i * 3], w.HA[j], w.HB[j], &w.HN[j * 3], AI);
         }
         w.M[i * ld + j] = v;
         w.M[j * ld + i] = v;
@@ -184,8 +185,10 @@ __device__ void assemble_fp64(const StencilParams &P, const WarpSmem &w, int lan
         double D[3];
         for (int d = 0; d < dim; d++) D[d] = -xi[d];  // x0 - xi in local coordinates
         for (int r = 0; r < nops; r++) {
-            double b = phs_op<double>(P.phs, P.op_code[r], P.op_dim[r], D, dim);
-            if (nr) b = w.HA[i] * b + w.HB[i] * phs_op_normal<double>(P.phs, P.op_code[r], P.op_dim[r], D, &w.HN[i * 3], dim);
+            double b = phs_op<double>(P.phs, P.op_code[r], P.op_dim[r], D, dim, AI);
+            if (nr)
+                b = w.HA[i] * b +
+                    w.HB[i] * phs_op_normal<double>(P.phs, P.op_code[r], P.op_dim[r], D, &w.HN[i * 3], dim, AI);
             w.M[i * ld + n + r] = b;
         }
     }
@@ -456,61 +459,61 @@ __global__ void build_fp32r_kernel(StencilParams P, int wpb, size_t warp_bytes) 
             continue;
         }
         assemble_fp64(P, w, lane, es, eval_local);
-        // round the matrix to FP32; |A|_max for the backward-error scale
-        float amax = 0.0f;
+        // round the matrix to FP32
         for (int t = lane; t < n * n; t += 32) {
             int i = t / n, j = t - (t / n) * n;
-            float a = (float)w.M[i * ld + j];
-            u.F[i * fld + j] = a;
-            amax = fmaxf(amax, fabsf(a));
+            u.F[i * fld + j] = (float)w.M[i * ld + j];
         }
-        for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-        const double anorm = (double)amax * n;
         __syncwarp();
         bool ok = lu_factor_fp32(u.F, u.piv, n, lane);
         bool accepted = false;
-        double eta_final = 0.0;
+        double est_final = 0.0;
         if (ok) {
-            // x0 = A32^{-1} b
+            // x0 = A32^{-1} b; then x += A32^{-1} (b - A x) with the residual in FP64.  The
+            // correction computed from the FP64 residual of x_{s-1} estimates its error; x is
+            // accepted once that correction, on the weights and on the polynomial
+            // multipliers, is below tol relative to x.
             for (int t = lane; t < n * nops; t += 32) {
                 int i = t / nops, q = t % nops;
                 u.v[t] = (float)w.M[i * ld + n + q];
                 u.x[t] = 0.0;
             }
             __syncwarp();
-            double bnorm = 0.0;
-            for (int t = lane; t < n * nops; t += 32) {
-                int i = t / nops, q = t % nops;
-                bnorm = fmax(bnorm, fabs(w.M[i * ld + n + q]));
-            }
-            for (int o = 16; o > 0; o >>= 1) bnorm = fmax(bnorm, __shfl_xor_sync(0xffffffffu, bnorm, o));
+            double dprev = 0.0;
             for (int step = 0;; step++) {
                 lu_apply_fp32(u.F, u.piv, u.v, n, nops, lane);
-                for (int t = lane; t < n * nops; t += 32) u.x[t] += (double)u.v[t];
+                double dmax = 0.0, xmax = 0.0;
+                for (int t = lane; t < n * nops; t += 32) {
+                    double d = (double)u.v[t];
+                    u.x[t] += d;
+                    if (t / nops < P.k) {
+                        dmax = fmax(dmax, fabs(d));
+                        xmax = fmax(xmax, fabs(u.x[t]));
+                    }
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+                    xmax = fmax(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
+                }
                 __syncwarp();
-                // FP64 residual r = b - A x (A symmetric: read column i as row i)
-                double rmax = 0.0, xmax = 0.0;
+                // accept when the correction is below tol and shrinking (contraction < 1/2),
+                // so that the error left after adding it is below tol as well
+                if (step > 0 && dmax <= P.tol * xmax && dmax <= 0.5 * dprev) {
+                    accepted = true;
+                    est_final = xmax > 0 ? dmax / xmax : 0.0;
+                    break;
+                }
+                dprev = dmax;
+                if (step >= P.refine_steps || !isfinite(dmax)) break;
+                // FP64 residual r = b - A x (A symmetric: read column i as row i); rows k..n-1
+                // are the polynomial-reproduction constraints P^T w = L(p)
                 for (int i = lane; i < n; i += 32) {
                     for (int q = 0; q < nops; q++) {
                         double acc = w.M[i * ld + n + q];
                         for (int j = 0; j < n; j++) acc = fma(-w.M[j * ld + i], u.x[j * nops + q], acc);
-                        u.r[i * nops + q] = acc;
-                        rmax = fmax(rmax, fabs(acc));
-                        xmax = fmax(xmax, fabs(u.x[i * nops + q]));
+                        u.v[i * nops + q] = (float)acc;
                     }
                 }
-                for (int o = 16; o > 0; o >>= 1) {
-                    rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-                    xmax = fmax(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
-                }
-                const double eta = rmax / (anorm * xmax + bnorm);
-                if (eta <= P.tol) {
-                    accepted = true;
-                    eta_final = eta;
-                    break;
-                }
-                if (step >= P.refine_steps || !isfinite(eta)) break;
-                for (int t = lane; t < n * nops; t += 32) u.v[t] = (float)u.r[t];
                 __syncwarp();
             }
         }
@@ -519,7 +522,7 @@ __global__ void build_fp32r_kernel(StencilParams P, int wpb, size_t warp_bytes) 
             if (lane == 0) {
                 if (P.status) P.status[e] = 0;
                 atomicMax(reinterpret_cast<unsigned long long *>(P.max_resid),
-                          (unsigned long long)__double_as_longlong(eta_final));
+                          (unsigned long long)__double_as_longlong(est_final));
             }
         } else {
             // fallback: the plain FP64 solve on the intact FP64 system

@@ -72,21 +72,36 @@ template <class T> __device__ __forceinline__ T sq_norm(const T *D, int dim) {
     return s;
 }
 
+// The reference guards divisions by r^b with r^b + 1e-16 (avoid_inf).  In local
+// coordinates r = s*r_xi, so the guard of an r^b denominator is 1e-16 / s^b: with it every
+// entry is exactly s^(power) times the raw-coordinate entry, including at r = 0.
+template <class T> struct AvoidInf {
+    T a1, a2, a3, a5;  // 1e-16 / s^b for b = 1, 2, 3, 5
+};
+
+template <class T> __device__ __forceinline__ AvoidInf<T> avoid_inf_scaled(int es) {
+    AvoidInf<T> a;
+    a.a1 = (T)ldexp(RBF_AVOID_INF, -es);
+    a.a2 = (T)ldexp(RBF_AVOID_INF, -2 * es);
+    a.a3 = (T)ldexp(RBF_AVOID_INF, -3 * es);
+    a.a5 = (T)ldexp(RBF_AVOID_INF, -5 * es);
+    return a;
+}
+
 // (op::L)(x, xi) with D = x - xi
-template <class T> __device__ T phs_op(int p, int op, int od, const T *D, int dim) {
+template <class T> __device__ T phs_op(int p, int op, int od, const T *D, int dim, const AvoidInf<T> &A) {
     T r2 = sq_norm(D, dim);
     if (op == RBF_OP_IDENTITY) return phs_phi_r2<T>(p, r2);
     T r = rbf_sqrt<T>(r2);
     T dd = D[od];
-    const T ai = (T)RBF_AVOID_INF;
     switch (p) {
     case 1:
-        if (op == RBF_OP_PARTIAL1) return dd / (r + ai);
-        if (op == RBF_OP_PARTIAL2) return (-(dd * dd) + r2) / (pw3(r) + ai);
-        return (T)2 / (r + ai);
+        if (op == RBF_OP_PARTIAL1) return dd / (r + A.a1);
+        if (op == RBF_OP_PARTIAL2) return (-(dd * dd) + r2) / (pw3(r) + A.a3);
+        return (T)2 / (r + A.a1);
     case 3:
         if (op == RBF_OP_PARTIAL1) return (T)3 * dd * r;
-        if (op == RBF_OP_PARTIAL2) return (T)3 * (r + (dd * dd) / (r + ai));
+        if (op == RBF_OP_PARTIAL2) return (T)3 * (r + (dd * dd) / (r + A.a1));
         return (T)12 * r;
     case 5:
         if (op == RBF_OP_PARTIAL1) return (T)5 * dd * pw3(r);
@@ -100,25 +115,25 @@ template <class T> __device__ T phs_op(int p, int op, int od, const T *D, int di
 }
 
 // (op::L)(x, xi, n): the operator applied to the normal derivative in the second argument
-template <class T> __device__ T phs_op_normal(int p, int op, int od, const T *D, const T *n, int dim) {
+template <class T>
+__device__ T phs_op_normal(int p, int op, int od, const T *D, const T *n, int dim, const AvoidInf<T> &A) {
     T r2 = sq_norm(D, dim);
     T r = rbf_sqrt<T>(r2);
     T dd = D[od], nd = n[od];
     T dn = n[0] * D[0];
     for (int d = 1; d < dim; d++) dn += n[d] * D[d];
-    const T ai = (T)RBF_AVOID_INF;
     switch (p) {
     case 1:
-        if (op == RBF_OP_PARTIAL1) return -nd / (r + ai) + dn * dd / (pw3(r) + ai);
-        if (op == RBF_OP_PARTIAL2) return ((T)2 * nd * dd + dn) / (pw3(r) + ai) - (T)3 * (dd * dd) * dn / (pw5(r) + ai);
-        return (T)2 * dn / (pw3(r) + ai);
+        if (op == RBF_OP_PARTIAL1) return -nd / (r + A.a1) + dn * dd / (pw3(r) + A.a3);
+        if (op == RBF_OP_PARTIAL2) return ((T)2 * nd * dd + dn) / (pw3(r) + A.a3) - (T)3 * (dd * dd) * dn / (pw5(r) + A.a5);
+        return (T)2 * dn / (pw3(r) + A.a3);
     case 3:
-        if (op == RBF_OP_PARTIAL1) return (T)-3 * (nd * r + dn * dd / (r + ai));
-        if (op == RBF_OP_PARTIAL2) return (T)-3 * ((T)2 * dd * nd + dn - dn * (dd * dd) / (r2 + ai)) / (r + ai);
-        return (T)-12 * dn / (r + ai);
+        if (op == RBF_OP_PARTIAL1) return (T)-3 * (nd * r + dn * dd / (r + A.a1));
+        if (op == RBF_OP_PARTIAL2) return (T)-3 * ((T)2 * dd * nd + dn - dn * (dd * dd) / (r2 + A.a2)) / (r + A.a1);
+        return (T)-12 * dn / (r + A.a1);
     case 5:
         if (op == RBF_OP_PARTIAL1) return (T)-5 * (nd * pw3(r) + (T)3 * dn * dd * r);
-        if (op == RBF_OP_PARTIAL2) return (T)-5 * ((T)6 * nd * dd * r + (T)3 * dn * (r + (dd * dd) / (r + ai)));
+        if (op == RBF_OP_PARTIAL2) return (T)-5 * ((T)6 * nd * dd * r + (T)3 * dn * (r + (dd * dd) / (r + A.a1)));
         return (T)-90 * dn * r;
     default:
         if (op == RBF_OP_PARTIAL1) return (T)-7 * (nd * pw5(r) + (T)5 * pw3(r) * dd * dn);
@@ -128,12 +143,12 @@ template <class T> __device__ T phs_op_normal(int p, int op, int od, const T *D,
 }
 
 // gradient / Hessian of phi in the first argument, D = x - xi
-template <class T> __device__ void phs_grad_hess(int p, const T *D, int dim, T *g, T *H, bool want_h) {
+template <class T>
+__device__ void phs_grad_hess(int p, const T *D, int dim, T *g, T *H, bool want_h, const AvoidInf<T> &A) {
     T r = rbf_sqrt<T>(sq_norm(D, dim));
-    const T ai = (T)RBF_AVOID_INF;
     for (int i = 0; i < dim; i++) {
         switch (p) {
-        case 1: g[i] = D[i] / (r + ai); break;
+        case 1: g[i] = D[i] / (r + A.a1); break;
         case 3: g[i] = (T)3 * D[i] * r; break;
         case 5: g[i] = (T)5 * D[i] * pw3(r); break;
         default: g[i] = (T)7 * D[i] * pw5(r); break;
@@ -145,8 +160,8 @@ template <class T> __device__ void phs_grad_hess(int p, const T *D, int dim, T *
             T dl = (i == j) ? (T)1 : (T)0;
             T v;
             switch (p) {
-            case 1: v = dl / (r + ai) - D[i] * D[j] / (pw3(r) + ai); break;
-            case 3: v = (T)3 * (dl * r + D[i] * D[j] / (r + ai)); break;
+            case 1: v = dl / (r + A.a1) - D[i] * D[j] / (pw3(r) + A.a3); break;
+            case 3: v = (T)3 * (dl * r + D[i] * D[j] / (r + A.a1)); break;
             case 5: v = (T)5 * (dl * pw3(r) + (T)3 * D[i] * D[j] * r); break;
             default: v = (T)7 * (dl * pw5(r) + (T)5 * D[i] * D[j] * pw3(r)); break;
             }
@@ -159,14 +174,14 @@ template <class T> __device__ void phs_grad_hess(int p, const T *D, int dim, T *
 // xi, xj local coordinates; ti/tj point types; a*, b* = alpha and beta/s; n* normals.
 template <class T>
 __device__ T colloc_entry(int p, int dim, const T *xi, const T *xj, int ti, int tj, T ai_, T bi_,
-                          const T *ni, T aj_, T bj_, const T *nj) {
+                          const T *ni, T aj_, T bj_, const T *nj, const AvoidInf<T> &A) {
     T D[3];
     for (int d = 0; d < dim; d++) D[d] = xi[d] - xj[d];
     T phi = phs_phi_r2<T>(p, sq_norm(D, dim));
     if (ti != PT_NR && tj != PT_NR) return phi;
     T g[3], H[9];
     bool both = (ti == PT_NR && tj == PT_NR);
-    phs_grad_hess<T>(p, D, dim, g, H, both);
+    phs_grad_hess<T>(p, D, dim, g, H, both, A);
     T di = 0, dj = 0;
     for (int d = 0; d < dim; d++) {
         di += ni[d] * g[d];

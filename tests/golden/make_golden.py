@@ -119,8 +119,83 @@ def oracle_fixtures():
                         row_ptr=W.row_ptr, col=W.col, val=W.val)
 
 
+def _truth_d2(P, x0, phs, deg, dim):
+    """Weights of d^2/dx_1^2 on one stencil with every entry evaluated in 80-digit arithmetic
+    from the double coordinates (the exact answer the FP64 builds approximate)."""
+    import mpmath
+    from oracle import oracle as O
+    mpmath.mp.dps = 80
+    k = len(P)
+    ex = O.monomial_exponents(dim, deg)
+    nm = len(ex)
+    n = k + nm
+    Pm = [[mpmath.mpf(float(v)) for v in p] for p in P]
+    x0m = [mpmath.mpf(float(v)) for v in x0]
+    A = mpmath.zeros(n, n)
+    b = mpmath.zeros(n, 1)
+    r = lambda a, c: mpmath.sqrt(sum((a[d] - c[d]) ** 2 for d in range(dim)))
+    for i in range(k):
+        for j in range(k):
+            A[i, j] = r(Pm[i], Pm[j]) ** phs
+        for m in range(nm):
+            v = mpmath.mpf(1)
+            for d in range(dim):
+                v *= Pm[i][d] ** int(ex[m][d])
+            A[i, k + m] = v
+            A[k + m, i] = v
+    for i in range(k):
+        rr = r(x0m, Pm[i])
+        dx = x0m[0] - Pm[i][0]
+        b[i] = phs * rr ** (phs - 2) + phs * (phs - 2) * rr ** (phs - 4) * dx ** 2 if rr != 0 else 0
+    for m in range(nm):
+        e = [int(v) for v in ex[m]]
+        c = e[0] * (e[0] - 1)
+        if c == 0:
+            continue
+        v = mpmath.mpf(c)
+        for d in range(dim):
+            v *= x0m[d] ** (e[d] - (2 if d == 0 else 0))
+        b[k + m] = v
+    x = mpmath.lu_solve(A, b)
+    return np.array([float(x[i]) for i in range(k)])
+
+
+def illcond_fixtures():
+    """Stencils with near-coincident points (i.i.d. clouds), where the raw-coordinate
+    reference arithmetic loses digits: the 4 stencils of each cloud where the oracle and a
+    scaled-coordinate FP64 solve disagree most, with high-precision truth weights."""
+    from oracle import oracle as O
+    out = {}
+    for name, (phs, deg, dim, k, n, seed) in {"d1_1d_phs3": (3, 2, 1, 7, 1500, 321),
+                                              "d2_2d_phs7": (7, 2, 2, 20, 1500, 722)}.items():
+        X = np.random.default_rng(seed).uniform(0, 1, (n, dim))
+        adjl = O.knn(X, X, k)
+        W = O.build(X, X, adjl, dim, phs, deg, [(O.OP_D2, 0)])
+        dis = np.zeros(n)
+        for e in range(n):
+            P = X[adjl[e]]
+            D = P - X[e]
+            s = 2.0 ** np.ceil(np.log2(np.sqrt((D ** 2).sum(1)).max()))
+            As, Bs, _ = O.assemble(dim, phs, deg, [(O.OP_D2, 0)], D / s, np.zeros(dim))
+            S = np.triu(As) + np.triu(As, 1).T
+            ws = np.linalg.solve(S, Bs[:, 0])[:k] / s ** 2
+            wo = W.val[0, W.row_ptr[e]:W.row_ptr[e + 1]]
+            dis[e] = np.abs(ws[np.argsort(adjl[e], kind="stable")] - wo).max() / np.abs(wo).max()
+        rows = np.argsort(-dis)[:4]
+        truth = np.zeros((4, k))
+        for t, e in enumerate(rows):
+            tw = _truth_d2(X[adjl[e]], X[e], phs, deg, dim)
+            truth[t] = tw[np.argsort(adjl[e], kind="stable")]  # column-sorted like the CSR row
+        out[name] = dict(points=X, adjl=adjl, rows=rows, truth=truth,
+                         oracle=np.stack([W.val[0, W.row_ptr[e]:W.row_ptr[e + 1]] for e in rows]),
+                         spec=np.array([phs, deg, dim, k]))
+    np.savez_compressed(os.path.join(HERE, "illcond_truth.npz"),
+                        **{f"{nm}__{key}": v for nm, d in out.items() for key, v in d.items()})
+
+
 if __name__ == "__main__":
     with open(os.path.join(HERE, "reference_known_answers.json"), "w") as f:
         json.dump(known_answers(), f, indent=1)
     oracle_fixtures()
+    illcond_fixtures()
     print("golden fixtures written")

@@ -122,8 +122,13 @@ def test_regrid3d_golden(pkg):
     (3, 0, 3, 10, ("lap",)), (3, -1, 2, 8, ("d1", 1)), (5, 3, 3, 40, ("lap",)), (3, 2, 1, 7, ("d2", 1)),
 ])
 def test_build_matches_oracle(pkg, orc, phs, deg, dim, k, op):
+    # quasi-uniform (jittered lattice) clouds keep every stencil well conditioned, so the
+    # reference's raw-coordinate arithmetic is itself accurate to far below the 1e-8 bar;
+    # ill-conditioned stencils are checked against high-precision truth below
     rng = np.random.default_rng(phs * 100 + deg * 10 + dim)
-    X = rng.uniform(0, 1, (1500, dim))
+    m = {1: 1500, 2: 39, 3: 12}[dim]
+    g = np.stack(np.meshgrid(*[np.arange(m)] * dim, indexing="ij"), -1).reshape(-1, dim)
+    X = (g + 0.5 + rng.uniform(-0.3, 0.3, g.shape)) / m
     adjl = orc.knn(X, X, k)
     if op[0] == "lap":
         L, ops = pkg.Laplacian(), [(orc.OP_LAP, 0)]
@@ -135,6 +140,29 @@ def test_build_matches_oracle(pkg, orc, phs, deg, dim, k, op):
     o = pkg.RadialBasisOperator(L, torch.from_numpy(X).cuda(), basis=pkg.PHS(phs, poly_deg=deg), k=k,
                                 adjl=torch.from_numpy(adjl).cuda())
     check_against(o.weights, ref.row_ptr, ref.col, ref.val[0])
+
+
+@pytest.mark.parametrize("name", ["d1_1d_phs3", "d2_2d_phs7"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
+def test_illconditioned_vs_truth(pkg, name, precision):
+    """Stencils with near-coincident points (i.i.d. clouds): the reference's raw-coordinate
+    FP64 weights carry errors up to ~3e-6 there, so they are judged against weights computed
+    with 80-digit entries and solve (tests/golden/make_golden.py).  The GPU builds must be
+    within 1e-8 of that truth (and are more accurate than the oracle)."""
+    z = np.load(os.path.join(GOLD, "illcond_truth.npz"))
+    g = {key.split("__")[1]: z[key] for key in z.files if key.startswith(name + "__")}
+    phs, deg, dim, k = map(int, g["spec"])
+    X = torch.from_numpy(g["points"]).cuda()
+    Ws = pkg.build_weights([(2, 0)], X, None, torch.from_numpy(g["adjl"]).cuda(), pkg.PHS(phs, poly_deg=deg),
+                           precision=precision)
+    v = Ws[0].val.cpu().numpy()
+    for t, e in enumerate(g["rows"]):
+        w = v[e * k:(e + 1) * k]
+        scale = np.abs(g["truth"][t]).max()
+        err = np.abs(w - g["truth"][t]).max() / scale
+        err_oracle = np.abs(g["oracle"][t] - g["truth"][t]).max() / scale
+        assert err <= 1e-8, (name, int(e), err, err_oracle)
+        assert err <= max(err_oracle, 1e-12)
 
 
 def test_apply_matches_oracle(pkg, orc):
@@ -292,6 +320,10 @@ def test_errors(pkg):
     isb[:3] = True
     with pytest.raises(pkg.DimensionMismatch):
         pkg.laplacian(X, hermite=dict(is_boundary=isb, bc=[pkg.Neumann()] * 2, normals=np.zeros((2, 2))))
+    bad = pkg.find_neighbors(X, k=12).copy()
+    bad[5, 3] = 100  # outside the data set
+    with pytest.raises(ValueError):
+        pkg.build_weights([(3, 0)], X, None, bad, pkg.PHS(3, poly_deg=2))
     with pytest.raises(ValueError):  # regrid has no normal form (api.jl:79-94)
         pkg.RadialBasisOperator(pkg.Regrid(), X, hermite=dict(is_boundary=isb, bc=[pkg.Neumann()] * 3,
                                                               normals=np.ones((3, 2))))
