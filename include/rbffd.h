@@ -154,6 +154,20 @@ int rbf_csr_to_csc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr,
                    const int32_t *col, const double *val, int64_t *col_ptr_out,
                    int32_t *row_out, double *val_out);
 
+/* ---- allocation-free apply (no counterpart in the reference) ---------------- */
+/* Same contract as rbf_spmm, for callers that cannot allocate device memory while
+ * applying an operator (code inside another framework's memory pool, or a time-stepping
+ * loop that must stay off the allocator).  Every array must be a device pointer; nothing
+ * is staged or allocated.  The column-major multi-field case (layout 0, nf > 1) stages
+ * X and Y through one fixed 32 MiB device array that the library holds on every GPU it is
+ * loaded on until exit: it is rejected (RBF_ERR_ARGUMENT) when nf*(ns+ne) exceeds
+ * 4,194,304 doubles.  The first call on a device looks up that array's address (set-up
+ * once per device); make that first call before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU race; each call overwrites what it reads. */
+int rbf_spmm_noalloc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const int32_t *col,
+                     const double *val, int32_t nf, int32_t layout, const double *X, int64_t ldx,
+                     double alpha, double beta, double *Y, int64_t ldy);
+
 /* ---- diagnostics (no counterpart in the reference) ------------------------ */
 /* Measured FMA throughput of the context's GPU in TFLOP/s (fp64 != 0: FP64,
  * else FP32), used as the roofline denominator of the build kernels. */

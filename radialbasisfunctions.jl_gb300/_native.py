@@ -112,6 +112,7 @@ SIGNATURES = {
     "rbf_build": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _I32, _P, _P, _P, _P, _P, _P]),
     "rbf_spmm": (_I, [_P, _I64, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _D, _D, _P, _I64]),
     "rbf_csr_to_csc": (_I, [_P, _I64, _I64, _P, _P, _P, _P, _P, _P]),
+    "rbf_spmm_noalloc": (_I, [_P, _I64, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _D, _D, _P, _I64]),
     "rbf_diag_fma_peak": (_I, [_P, _I32, ctypes.POINTER(_D)]),
     "rbf_ctx_kernel_launches": (_I64, [_P]),
 }

@@ -9,6 +9,7 @@
 // Column-major fields (a Julia Matrix) are transposed to interleaved scratch first.
 // Roofline: HBM bandwidth; algorithmic bytes nnz*(8+4) + (ne+1)*8 + nf*(ns+ne)*8.
 #include <algorithm>
+#include <mutex>
 
 #include "rbf_internal.cuh"
 
@@ -224,5 +225,109 @@ int rbf_csr_to_csc_device(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *d
     RBF_CHECK_LAUNCH(ctx);
     csc_sort_kernel<<<blocks_for(ctx, ns, 256, 8), 256, 0, ctx->stream>>>(ns, d_cp, d_row, d_valc);
     RBF_CHECK_LAUNCH(ctx);
+    return RBF_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free apply (rbf_spmm_noalloc)
+//
+// Some callers cannot allocate device memory while they apply an operator: code running
+// inside another framework's memory pool that forbids foreign allocations, a time-stepping
+// loop that must not touch the allocator between steps, or a host thread that may not
+// synchronise with the device allocator.  For them the column-major multi-field apply,
+// the one path of rbf_spmm that needs scratch (the interleaved copies of X and Y), stages
+// through this fixed file-scope device array instead of stream-ordered allocations.
+// Capacity: RBF_NOALLOC_SCRATCH_DOUBLES doubles (32 MiB) per GPU that loads the library,
+// held until the process exits; a call needing nf*(ns+ne) doubles more than that is
+// rejected.  Every call shares the array: calls that overlap on the GPU (different
+// streams, or contexts on the same device) race on it.  Both halves are written in full
+// before they are read, so nothing needs clearing between calls.
+// ---------------------------------------------------------------------------------------
+#define RBF_NOALLOC_SCRATCH_DOUBLES (4u << 20)
+static __device__ __align__(256) double g_noalloc_scratch[RBF_NOALLOC_SCRATCH_DOUBLES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double *g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device (set up once per device).
+int noalloc_scratch(rbf_ctx *ctx, double **out) {
+    if (ctx->device < 0 || ctx->device >= kMaxDevices)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "device %d out of range for the no-alloc apply", ctx->device);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[ctx->device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return rbf_fail(ctx, RBF_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch) failed: %s",
+                            cudaGetErrorString(e));
+        g_noalloc_ptr[ctx->device] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_ptr[ctx->device];
+    return RBF_OK;
+}
+}  // namespace
+
+extern "C" int rbf_spmm_noalloc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const int32_t *col,
+                                const double *val, int32_t nf, int32_t layout, const double *X, int64_t ldx,
+                                double alpha, double beta, double *Y, int64_t ldy) {
+    if (!ctx) return RBF_ERR_ARGUMENT;
+    RBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (nf < 1 || ne < 0 || ns < 0) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid sizes");
+    if (layout != 0 && layout != 1) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "layout must be 0 or 1");
+    if (layout == 0 && nf > 1 && (ldx < ns || ldy < ne)) return rbf_fail(ctx, RBF_ERR_DIMENSION, "leading dimension too small");
+    if (layout == 1 && (ldx < nf || ldy < nf)) return rbf_fail(ctx, RBF_ERR_DIMENSION, "leading dimension too small");
+    const bool staged = (layout == 0 && nf > 1);
+    if (staged && (double)nf * (double)(ns + ne) > (double)RBF_NOALLOC_SCRATCH_DOUBLES)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT,
+                        "no-alloc apply: nf*(ns+ne) = %lld doubles exceeds the fixed scratch of %u doubles (32 MiB); "
+                        "use rbf_spmm or the interleaved layout",
+                        (long long)nf * (long long)(ns + ne), RBF_NOALLOC_SCRATCH_DOUBLES);
+    if (!rbf_is_device_ptr(row_ptr) || !rbf_is_device_ptr(col) || !rbf_is_device_ptr(val) || !rbf_is_device_ptr(X) ||
+        !rbf_is_device_ptr(Y))
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "no-alloc apply: every array must be a device pointer");
+    if (ne == 0) return RBF_OK;
+    if (!staged) {
+        if (nf == 1) {
+            spmv_kernel<8><<<blocks_for(ctx, ne * 8, 256, 16), 256, 0, ctx->stream>>>(ne, row_ptr, col, val, X, alpha,
+                                                                                      beta, Y);
+            RBF_CHECK_LAUNCH(ctx);
+        } else {
+            for (int f0 = 0; f0 < nf; f0 += 32) {
+                int nfc = std::min(32, nf - f0), nfp = 1;
+                while (nfp < nfc) nfp <<= 1;
+                int64_t warps = (ne + (32 / nfp) - 1) / (32 / nfp);
+                spmm_interleaved_kernel<<<blocks_for(ctx, warps * 32, 256, 16), 256, 0, ctx->stream>>>(
+                    ne, row_ptr, col, val, nfc, nfp, X + f0, ldx, alpha, beta, Y + f0, ldy);
+                RBF_CHECK_LAUNCH(ctx);
+            }
+        }
+    } else {
+        double *scratch = nullptr;
+        RBF_TRY(noalloc_scratch(ctx, &scratch));
+        double *xs = scratch, *ys = scratch + (size_t)nf * ns;
+        dim3 tb(32, 8);
+        to_interleaved_kernel<<<dim3((unsigned)((ns + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
+            ns, nf, X, ldx, xs);
+        RBF_CHECK_LAUNCH(ctx);
+        if (beta != 0.0) {
+            to_interleaved_kernel<<<dim3((unsigned)((ne + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
+                ne, nf, Y, ldy, ys);
+            RBF_CHECK_LAUNCH(ctx);
+        }
+        for (int f0 = 0; f0 < nf; f0 += 32) {
+            int nfc = std::min(32, nf - f0), nfp = 1;
+            while (nfp < nfc) nfp <<= 1;
+            int64_t warps = (ne + (32 / nfp) - 1) / (32 / nfp);
+            spmm_interleaved_kernel<<<blocks_for(ctx, warps * 32, 256, 16), 256, 0, ctx->stream>>>(
+                ne, row_ptr, col, val, nfc, nfp, xs + f0, nf, alpha, beta, ys + f0, nf);
+            RBF_CHECK_LAUNCH(ctx);
+        }
+        from_interleaved_kernel<<<dim3((unsigned)((ne + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
+            ne, nf, ys, Y, ldy);
+        RBF_CHECK_LAUNCH(ctx);
+    }
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RBF_OK;
 }
