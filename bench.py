@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--n", type=int, default=0, help="override the point count (development runs)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=0, help="stencils in the CPU baseline sample")
+    p.add_argument("--profile-once", action="store_true",
+                   help="run each hot kernel once (kNN, FP64 build, FP32-refined build, apply) and exit; "
+                        "the driver for ncu captures")
     return p.parse_args()
 
 
@@ -229,6 +232,17 @@ def main():
         return ms
 
     headline = "fp32_refined"
+    if args.profile_once:
+        adjl = pkg.find_neighbors(Xd, k=k, ctx=ctx)
+        s64, s32 = pkg._native.BuildStats(), pkg._native.BuildStats()
+        W64 = pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision="fp64", ctx=ctx, stats=s64)
+        W32 = pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision=headline, ctx=ctx, stats=s32)
+        W32[-1].apply(fd)
+        torch.cuda.synchronize()
+        err = max(row_rel_err_torch(torch, a.row_ptr, k, a.val, b.val) for a, b in zip(W32, W64))
+        print(json.dumps({"profile_once": cfg["desc"], "n": n, "ms_build_fp64": s64.ms_build,
+                          "ms_build_fp32r": s32.ms_build, "fallback": s32.n_fallback, "max_diff": err}))
+        return
     launches0 = ctx.lib.rbf_ctx_kernel_launches(ctx.handle)
     clocks = ClockSampler(local)
     # ---- headline timed region
@@ -336,6 +350,9 @@ def main():
                        "parallelism": f"replicas x{world}"},
             "plain_fp64": {"value": n * world / (ms_fp64 * 1e-3), "unit": "stencils/s", "ms_per_step": ms_fp64},
             "speedup_vs_plain_fp64": ms_fp64 / ms,
+            "build_only": {"fp32_refined_ms": ms_build32, "fp64_ms": ms_build64, "speedup": ms_build64 / ms_build32,
+                           "fp32_refined_stencils_per_s": n / (ms_build32 * 1e-3),
+                           "fp64_stencils_per_s": n / (ms_build64 * 1e-3)},
             "equal_error": {"max_row_rel_weight_diff_vs_fp64": err, "bar": 1e-8, "fallback_stencils": n_fallback},
             "apply": {"value": apply_gbs, "unit": "GB/s", "ms": ms_spmv, "nnz": nnz,
                       "frac_of_hbm": apply_gbs / hbm_peak},

@@ -23,7 +23,8 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
 
-SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "stencil_build.cu", "diag.cu"]
+SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "stencil_build.cu", "stencil_refined_a.cu",
+           "stencil_refined_b.cu", "diag.cu"]
 
 
 def _nvcc():

@@ -109,13 +109,19 @@ __global__ void cell_count_kernel(GridDesc g, const double *__restrict__ x, int6
 template <int DIM>
 __global__ void cell_scatter_kernel(const double *__restrict__ x, int64_t n, const int32_t *__restrict__ cell,
                                     const int32_t *__restrict__ start, int32_t *__restrict__ fill,
-                                    double *__restrict__ sp, int32_t *__restrict__ sidx) {
+                                    double *__restrict__ sp, float4 *__restrict__ sp32, int32_t *__restrict__ sidx) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int32_t c = cell[i];
         int32_t pos = start[c] + atomicAdd(&fill[c], 1);
-        if (sp)
+        if (sp) {
+            double v[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-            for (int d = 0; d < DIM; d++) sp[(int64_t)pos * DIM + d] = x[i * DIM + d];
+            for (int d = 0; d < DIM; d++) {
+                v[d] = x[i * DIM + d];
+                sp[(int64_t)pos * DIM + d] = v[d];
+            }
+            sp32[pos] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.0f);
+        }
         sidx[pos] = (int32_t)i;
     }
 }
@@ -316,6 +322,314 @@ knn_query_kernel(GridDesc g, const double *__restrict__ sp, const int32_t *__res
     }
 }
 
+
+__device__ __forceinline__ bool fkey_less(float d1, int32_t i1, float d2, int32_t i2) {
+    return d1 < d2 || (d1 == d2 && i1 < i2);
+}
+
+__device__ __forceinline__ bool xkey_less(unsigned long long d1, int32_t i1, unsigned long long d2, int32_t i2) {
+    return d1 < d2 || (d1 == d2 && i1 < i2);
+}
+
+// FP32-key search.  Candidate keys are squared distances from the FP32 copy of the points;
+// the warp keeps the kp = k + 8 best (FP32 key, index) pairs.  The search stops once the
+// kp-th FP32 distance plus its error bound is inside the covered ball, so the kp listed
+// points are the kp nearest up to rounding.  Then the exact FP64 squared distances (dimension
+// order, no FMA) of the kp candidates are sorted with the index tie-break, and the result is
+// accepted only if the exact k-th distance is below the smallest exact distance any unlisted
+// point can have (the kp-th FP32 distance minus its error bound); otherwise the query is
+// appended to the fallback list for the exact FP64 search.
+// Error bound of an FP32 distance (u = 2^-24, M the largest coordinate magnitude):
+// |d32 - d| <= 8u (M + d).
+template <int DIM, int SLOTS>
+__global__ void __launch_bounds__(KNN_WARPS * 32)
+knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__restrict__ sidx,
+                const int32_t *__restrict__ cstart, const double *__restrict__ data, const double *__restrict__ q,
+                const int32_t *__restrict__ qorder, int64_t nq, int k, int kp, int R0, float mag, int64_t ns,
+                int32_t *__restrict__ out, int32_t *__restrict__ fb_list, int32_t *__restrict__ fb_count) {
+    __shared__ int32_t s_start[KNN_WARPS][KNN_RANGES];
+    __shared__ int32_t s_off[KNN_WARPS][KNN_RANGES + 1];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t warp0 = (int64_t)blockIdx.x * KNN_WARPS + wib;
+    const int64_t nwarps = (int64_t)gridDim.x * KNN_WARPS;
+    int32_t *my_start = s_start[wib];
+    int32_t *my_off = s_off[wib];
+    const float u8 = 8.0f * 5.9604645e-08f;
+    const int tl = (kp - 1) & 31, ts = (kp - 1) >> 5;
+
+    for (int64_t t = warp0; t < nq; t += nwarps) {
+        const int32_t qi = qorder[t];
+        double qp[DIM];
+        float qf[3] = {0.f, 0.f, 0.f};
+        float qmag = mag;
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+            qp[d] = q[(int64_t)qi * DIM + d];
+            qf[d] = (float)qp[d];
+            qmag = fmaxf(qmag, fabsf(qf[d]));
+        }
+        const float errc = u8 * qmag * 1.0001f;
+        int qc[3] = {0, 0, 0};
+        cell_of<DIM>(g, qp, qc);
+
+        float key[SLOTS];
+        int32_t kid[SLOTS];
+#pragma unroll
+        for (int s = 0; s < SLOTS; s++) {
+            key[s] = INFINITY;
+            kid[s] = 0x7fffffff;
+        }
+        float kth = INFINITY;
+        int32_t kth_id = 0x7fffffff;
+
+        int r_in = -1;
+        for (int R = R0;; R++) {
+            const int side = 2 * R + 1;
+            const int nrows = DIM == 1 ? 1 : (DIM == 2 ? side : side * side);
+            for (int row0 = 0; row0 < nrows; row0 += 32) {
+                int row = row0 + lane;
+                int32_t a0 = 0, l0 = 0, a1 = 0, l1 = 0;
+                if (row < nrows) {
+                    int dy = 0, dz = 0;
+                    if (DIM >= 2) dy = (row % side) - R;
+                    if (DIM == 3) dz = (row / side) - R;
+                    int cy = qc[1] + dy, cz = qc[2] + dz;
+                    bool inside = (DIM < 2 || (cy >= 0 && cy < g.nc[1])) && (DIM < 3 || (cz >= 0 && cz < g.nc[2]));
+                    if (inside) {
+                        int m = max(abs(dy), abs(dz));
+                        int64_t rowbase = ((int64_t)cz * g.nc[1] + cy) * g.nc[0];
+                        if (m > r_in) {
+                            int x0 = max(qc[0] - R, 0), x1 = min(qc[0] + R, g.nc[0] - 1);
+                            if (x0 <= x1) {
+                                a0 = cstart[rowbase + x0];
+                                l0 = cstart[rowbase + x1 + 1] - a0;
+                            }
+                        } else {
+                            int x0 = max(qc[0] - R, 0), x1 = min(qc[0] - r_in - 1, g.nc[0] - 1);
+                            if (x0 <= x1) {
+                                a0 = cstart[rowbase + x0];
+                                l0 = cstart[rowbase + x1 + 1] - a0;
+                            }
+                            x0 = max(qc[0] + r_in + 1, 0);
+                            x1 = min(qc[0] + R, g.nc[0] - 1);
+                            if (x0 <= x1) {
+                                a1 = cstart[rowbase + x0];
+                                l1 = cstart[rowbase + x1 + 1] - a1;
+                            }
+                        }
+                    }
+                }
+                int32_t pair = l0 + l1, incl = pair;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                int32_t excl = incl - pair;
+                my_start[2 * lane] = a0;
+                my_start[2 * lane + 1] = a1;
+                my_off[2 * lane] = excl;
+                my_off[2 * lane + 1] = excl + l0;
+                const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                __syncwarp();
+                for (int32_t f0 = 0; f0 < total; f0 += 32) {
+                    int32_t f = f0 + lane;
+                    float dd = INFINITY;
+                    int32_t id = 0x7fffffff;
+                    if (f < total) {
+                        int lo = 0, hi = KNN_RANGES - 1;
+                        while (lo < hi) {
+                            int mid = (lo + hi + 1) >> 1;
+                            if (my_off[mid] <= f) lo = mid;
+                            else hi = mid - 1;
+                        }
+                        int32_t p = my_start[lo] + (f - my_off[lo]);
+                        float4 c4 = __ldg(&sp32[p]);
+                        float dx = c4.x - qf[0];
+                        dd = dx * dx;
+                        if (DIM > 1) {
+                            float dy = c4.y - qf[1];
+                            dd = fmaf(dy, dy, dd);
+                        }
+                        if (DIM > 2) {
+                            float dz = c4.z - qf[2];
+                            dd = fmaf(dz, dz, dd);
+                        }
+                        id = __ldg(&sidx[p]);
+                    }
+                    bool pass = (f < total) && fkey_less(dd, id, kth, kth_id);
+                    unsigned m = __ballot_sync(0xffffffffu, pass);
+                    while (m) {
+                        const int src = __ffs(m) - 1;
+                        m &= m - 1;
+                        const float cd = __shfl_sync(0xffffffffu, dd, src);
+                        const int32_t ci = __shfl_sync(0xffffffffu, id, src);
+                        if (!fkey_less(cd, ci, kth, kth_id)) continue;  // warp-uniform
+                        int pos = 0;
+#pragma unroll
+                        for (int s = 0; s < SLOTS; s++)
+                            pos += __popc(__ballot_sync(0xffffffffu, fkey_less(key[s], kid[s], cd, ci)));
+                        float pk[SLOTS];
+                        int32_t pi[SLOTS];
+#pragma unroll
+                        for (int s = 0; s < SLOTS; s++) {
+                            pk[s] = __shfl_up_sync(0xffffffffu, key[s], 1);
+                            pi[s] = __shfl_up_sync(0xffffffffu, kid[s], 1);
+                            const int sp = s > 0 ? s - 1 : 0;
+                            float wk = __shfl_sync(0xffffffffu, key[sp], 31);
+                            int32_t wi = __shfl_sync(0xffffffffu, kid[sp], 31);
+                            if (lane == 0) {
+                                pk[s] = wk;
+                                pi[s] = wi;
+                            }
+                        }
+#pragma unroll
+                        for (int s = 0; s < SLOTS; s++) {
+                            int j = lane + 32 * s;
+                            if (j == pos) {
+                                key[s] = cd;
+                                kid[s] = ci;
+                            } else if (j > pos) {
+                                key[s] = pk[s];
+                                kid[s] = pi[s];
+                            }
+                        }
+                        float kv = key[0];
+                        int32_t ki = kid[0];
+#pragma unroll
+                        for (int s = 1; s < SLOTS; s++)
+                            if (s == ts) {
+                                kv = key[s];
+                                ki = kid[s];
+                            }
+                        kth = __shfl_sync(0xffffffffu, kv, tl);
+                        kth_id = __shfl_sync(0xffffffffu, ki, tl);
+                    }
+                }
+                __syncwarp();
+            }
+            double cover = INFINITY;
+            bool all_covered = true;
+#pragma unroll
+            for (int d = 0; d < DIM; d++) {
+                if (qc[d] - R > 0) {
+                    all_covered = false;
+                    cover = fmin(cover, qp[d] - (g.lo[d] + (double)(qc[d] - R) * g.h[d]));
+                }
+                if (qc[d] + R < g.nc[d] - 1) {
+                    all_covered = false;
+                    cover = fmin(cover, (g.lo[d] + (double)(qc[d] + R + 1) * g.h[d]) - qp[d]);
+                }
+            }
+            if (all_covered) break;
+            if (kth < INFINITY) {
+                const float dk = sqrtf(kth);
+                const float reach = dk + errc + u8 * dk;
+                double mg = 0.0;
+#pragma unroll
+                for (int d = 0; d < DIM; d++) mg = fmax(mg, fabs(qp[d]) + fabs(g.lo[d]) + g.h[d] * g.nc[d]);
+                const double c = cover * (1.0 - 1e-6) - 4e-15 * mg;
+                if ((double)reach < c) break;
+            }
+            r_in = R;
+        }
+
+        // exact keys of the kp candidates, then a transposition sort (they are nearly sorted)
+        unsigned long long xk[SLOTS];
+        int32_t xi[SLOTS];
+#pragma unroll
+        for (int s = 0; s < SLOTS; s++) {
+            const int j = lane + 32 * s;
+            xk[s] = ~0ull;
+            xi[s] = 0x7fffffff;
+            if (j < kp && kid[s] != 0x7fffffff) {
+                const double *pp = data + (int64_t)kid[s] * DIM;
+                double tt = __dsub_rn(qp[0], pp[0]);
+                double d2 = __dmul_rn(tt, tt);
+#pragma unroll
+                for (int d = 1; d < DIM; d++) {
+                    tt = __dsub_rn(qp[d], pp[d]);
+                    d2 = __dadd_rn(d2, __dmul_rn(tt, tt));
+                }
+                xk[s] = (unsigned long long)__double_as_longlong(d2);
+                xi[s] = kid[s];
+            }
+        }
+        for (int iter = 0; iter < 32 * SLOTS; iter++) {
+            bool swapped = false;
+#pragma unroll
+            for (int phase = 0; phase < 2; phase++) {
+                // neighbours of every position, read before any position of this phase changes
+                unsigned long long up_k[SLOTS], dn_k[SLOTS];
+                int32_t up_i[SLOTS], dn_i[SLOTS];
+#pragma unroll
+                for (int s = 0; s < SLOTS; s++) {
+                    up_k[s] = __shfl_down_sync(0xffffffffu, xk[s], 1);
+                    up_i[s] = __shfl_down_sync(0xffffffffu, xi[s], 1);
+                    dn_k[s] = __shfl_up_sync(0xffffffffu, xk[s], 1);
+                    dn_i[s] = __shfl_up_sync(0xffffffffu, xi[s], 1);
+                    const int sn = s + 1 < SLOTS ? s + 1 : s;
+                    const int spv = s > 0 ? s - 1 : 0;
+                    unsigned long long nx_k = __shfl_sync(0xffffffffu, xk[sn], 0);
+                    int32_t nx_i = __shfl_sync(0xffffffffu, xi[sn], 0);
+                    unsigned long long pv_k = __shfl_sync(0xffffffffu, xk[spv], 31);
+                    int32_t pv_i = __shfl_sync(0xffffffffu, xi[spv], 31);
+                    if (lane == 31) {
+                        up_k[s] = nx_k;
+                        up_i[s] = nx_i;
+                    }
+                    if (lane == 0) {
+                        dn_k[s] = pv_k;
+                        dn_i[s] = pv_i;
+                    }
+                }
+#pragma unroll
+                for (int s = 0; s < SLOTS; s++) {
+                    const int j = lane + 32 * s;
+                    const bool low = ((j & 1) == phase);  // j pairs with j+1, else with j-1
+                    if (low && j < 32 * SLOTS - 1) {
+                        if (xkey_less(up_k[s], up_i[s], xk[s], xi[s])) {
+                            xk[s] = up_k[s];
+                            xi[s] = up_i[s];
+                            swapped = true;
+                        }
+                    } else if (!low && j > 0) {
+                        if (xkey_less(xk[s], xi[s], dn_k[s], dn_i[s])) {
+                            xk[s] = dn_k[s];
+                            xi[s] = dn_i[s];
+                            swapped = true;
+                        }
+                    }
+                }
+            }
+            if (!__any_sync(0xffffffffu, swapped)) break;
+        }
+        // certify: exact k-th distance below the smallest exact distance of unlisted points
+        bool certified = true;
+        if ((int64_t)kp < ns) {
+            unsigned long long kk = xk[0];
+#pragma unroll
+            for (int s = 1; s < SLOTS; s++)
+                if (s == ((k - 1) >> 5)) kk = xk[s];
+            kk = __shfl_sync(0xffffffffu, kk, (k - 1) & 31);
+            const double dk_exact = sqrt(__longlong_as_double((long long)kk));
+            const float dt = sqrtf(kth);
+            const double floor_unlisted = (double)dt - (double)(errc + u8 * dt) * 1.0001;
+            certified = (kth < INFINITY) && (dk_exact < floor_unlisted);
+        }
+        if (certified) {
+#pragma unroll
+            for (int s = 0; s < SLOTS; s++) {
+                const int j = lane + 32 * s;
+                if (j < k) out[(int64_t)qi * k + j] = xi[s];
+            }
+        } else if (lane == 0) {
+            int slot = atomicAdd(fb_count, 1);
+            fb_list[slot] = qi;
+        }
+    }
+}
+
 int grid_blocks(rbf_ctx *ctx, int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
     int64_t cap = (int64_t)ctx->num_sms * 16;
@@ -390,12 +704,13 @@ int knn_dim(rbf_ctx *ctx, const double *d_data, int64_t ns, const double *d_eval
     }
     g.ncells = ncells;
 
-    DevBuf cell, count, start, fill, sp, sidx, qcell, qcount, qstart, qfill, qorder;
+    DevBuf cell, count, start, fill, sp, sp32, sidx, qcell, qcount, qstart, qfill, qorder, fb;
     RBF_TRY(cell.alloc(ctx, sizeof(int32_t) * ns));
     RBF_TRY(count.alloc(ctx, sizeof(int32_t) * (ncells + 1)));
     RBF_TRY(start.alloc(ctx, sizeof(int32_t) * (ncells + 1)));
     RBF_TRY(fill.alloc(ctx, sizeof(int32_t) * (ncells + 1)));
     RBF_TRY(sp.alloc(ctx, sizeof(double) * DIM * ns));
+    RBF_TRY(sp32.alloc(ctx, sizeof(float4) * ns));
     RBF_TRY(sidx.alloc(ctx, sizeof(int32_t) * ns));
     RBF_CUDA(ctx, cudaMemsetAsync(count.ptr, 0, sizeof(int32_t) * (ncells + 1), ctx->stream));
     RBF_CUDA(ctx, cudaMemsetAsync(fill.ptr, 0, sizeof(int32_t) * (ncells + 1), ctx->stream));
@@ -403,7 +718,8 @@ int knn_dim(rbf_ctx *ctx, const double *d_data, int64_t ns, const double *d_eval
     RBF_CHECK_LAUNCH(ctx);
     RBF_TRY(rbf_exclusive_scan_i32(ctx, count.as<int32_t>(), start.as<int32_t>(), ncells + 1, nullptr));
     cell_scatter_kernel<DIM><<<grid_blocks(ctx, ns, 256), 256, 0, ctx->stream>>>(
-        d_data, ns, cell.as<int32_t>(), start.as<int32_t>(), fill.as<int32_t>(), sp.as<double>(), sidx.as<int32_t>());
+        d_data, ns, cell.as<int32_t>(), start.as<int32_t>(), fill.as<int32_t>(), sp.as<double>(), sp32.as<float4>(),
+        sidx.as<int32_t>());
     RBF_CHECK_LAUNCH(ctx);
 
     // visit queries in cell order
@@ -418,21 +734,44 @@ int knn_dim(rbf_ctx *ctx, const double *d_data, int64_t ns, const double *d_eval
     RBF_CHECK_LAUNCH(ctx);
     RBF_TRY(rbf_exclusive_scan_i32(ctx, qcount.as<int32_t>(), qstart.as<int32_t>(), ncells + 1, nullptr));
     cell_scatter_kernel<DIM><<<grid_blocks(ctx, ne, 256), 256, 0, ctx->stream>>>(
-        d_eval, ne, qcell.as<int32_t>(), qstart.as<int32_t>(), qfill.as<int32_t>(), nullptr, qorder.as<int32_t>());
+        d_eval, ne, qcell.as<int32_t>(), qstart.as<int32_t>(), qfill.as<int32_t>(), nullptr, nullptr,
+        qorder.as<int32_t>());
     RBF_CHECK_LAUNCH(ctx);
 
-    int64_t warps_needed = ne;
-    int64_t blocks = (warps_needed + KNN_WARPS - 1) / KNN_WARPS;
+    int64_t blocks = (ne + KNN_WARPS - 1) / KNN_WARPS;
     int64_t cap = (int64_t)ctx->num_sms * 32;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    if (k <= 32)
-        knn_query_kernel<DIM, 1><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
-            g, sp.as<double>(), sidx.as<int32_t>(), start.as<int32_t>(), d_eval, qorder.as<int32_t>(), ne, k, R0, d_idx);
+    // FP32 search with an exact FP64 re-sort of k + 8 candidates; queries whose FP32
+    // margins do not certify the exact order go to the FP64 search below
+    const int kp = std::min(k + 8, 64);
+    float mag = 0.f;
+    for (int d = 0; d < DIM; d++) mag = std::max(mag, (float)std::max(std::fabs(lo[d]), std::fabs(hi[d])));
+    RBF_TRY(fb.alloc(ctx, sizeof(int32_t) * (ne + 1)));
+    RBF_CUDA(ctx, cudaMemsetAsync(fb.as<int32_t>() + ne, 0, sizeof(int32_t), ctx->stream));
+    if (kp <= 32)
+        knn_fast_kernel<DIM, 1><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
+            g, sp32.as<float4>(), sidx.as<int32_t>(), start.as<int32_t>(), d_data, d_eval, qorder.as<int32_t>(), ne,
+            k, kp, R0, mag, ns, d_idx, fb.as<int32_t>(), fb.as<int32_t>() + ne);
     else
-        knn_query_kernel<DIM, 2><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
-            g, sp.as<double>(), sidx.as<int32_t>(), start.as<int32_t>(), d_eval, qorder.as<int32_t>(), ne, k, R0, d_idx);
+        knn_fast_kernel<DIM, 2><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
+            g, sp32.as<float4>(), sidx.as<int32_t>(), start.as<int32_t>(), d_data, d_eval, qorder.as<int32_t>(), ne,
+            k, kp, R0, mag, ns, d_idx, fb.as<int32_t>(), fb.as<int32_t>() + ne);
     RBF_CHECK_LAUNCH(ctx);
+    int32_t nfb = 0;
+    RBF_CUDA(ctx, cudaMemcpyAsync(&nfb, fb.as<int32_t>() + ne, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->knn_fallback += nfb;
+    if (nfb > 0) {
+        int64_t fblocks = std::min<int64_t>((nfb + KNN_WARPS - 1) / KNN_WARPS, cap);
+        if (k <= 32)
+            knn_query_kernel<DIM, 1><<<(unsigned)fblocks, KNN_WARPS * 32, 0, ctx->stream>>>(
+                g, sp.as<double>(), sidx.as<int32_t>(), start.as<int32_t>(), d_eval, fb.as<int32_t>(), nfb, k, R0, d_idx);
+        else
+            knn_query_kernel<DIM, 2><<<(unsigned)fblocks, KNN_WARPS * 32, 0, ctx->stream>>>(
+                g, sp.as<double>(), sidx.as<int32_t>(), start.as<int32_t>(), d_eval, fb.as<int32_t>(), nfb, k, R0, d_idx);
+        RBF_CHECK_LAUNCH(ctx);
+    }
     return RBF_OK;
 }
 

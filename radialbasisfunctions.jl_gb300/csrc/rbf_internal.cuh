@@ -15,7 +15,8 @@ struct rbf_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     std::string last_error;
-    long long launches = 0;  // kernels launched through this context
+    long long launches = 0;      // kernels launched through this context
+    long long knn_fallback = 0;  // queries re-run by the exact FP64 neighbour search
 };
 
 int rbf_fail(rbf_ctx *ctx, int code, const char *fmt, ...);
