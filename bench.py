@@ -190,8 +190,7 @@ def main():
     g.build()
     pkg = g.load_package()
     ctx = pkg.Context.default(local)
-    stream = torch.cuda.current_stream()
-    ctx.set_stream(stream.cuda_stream)
+    stream = torch.cuda.current_stream()  # the package binds the library to this stream
     dev = torch.device("cuda", local)
 
     # independent seeded cloud per rank (weak scaling: per-GPU work fixed)

@@ -68,7 +68,15 @@ typedef struct rbf_build_cfg {
     double tol;                   /* FP32 paths: accept when the correction computed from the
                                      FP64 residual is below tol relative to the weights
                                      (0: default 1e-9); otherwise the FP64 solve is used */
+    int32_t flags;                /* RBF_FLAG_* bits                                 */
+    const float *seed;            /* RBF_PREC_LEARNED: predicted weights, ne x k floats in
+                                     stencil order and local units (device pointer)   */
 } rbf_build_cfg;
+
+/* flags */
+#define RBF_FLAG_STENCIL_ORDER 1  /* write each row in stencil (adjl) order, not column order */
+#define RBF_FLAG_LOCAL_UNITS 2    /* weights in the stencil's local units: w * s^q, s the power of
+                                     two above the stencil radius, q the operator order */
 
 /* Hermite boundary description (src/solve/types.jl:18-42,178-182).  Boundary
  * conditions are B u = alpha*u + beta*du/dn; Dirichlet is (1,0), Neumann (0,1).
@@ -91,6 +99,7 @@ typedef struct rbf_build_stats {
     double max_residual;     /* FP32 paths: largest accepted relative correction (error
                                 estimate of the accepted weights)                      */
     float ms_knn, ms_build, ms_total;
+    int64_t n_residuals;     /* FP32 paths: FP64 residual evaluations over all stencils  */
 } rbf_build_stats;
 
 typedef struct rbf_ctx rbf_ctx;
@@ -102,7 +111,10 @@ typedef struct rbf_ctx rbf_ctx;
 int rbf_ctx_create(int device, rbf_ctx **out);
 int rbf_ctx_destroy(rbf_ctx *ctx);
 /* Run on a caller-owned cudaStream_t (e.g. the stream of a Julia task or a torch
- * stream); NULL restores the context's own stream. */
+ * stream); NULL restores the context's own stream.  The legacy default stream is
+ * selected by its handle cudaStreamLegacy ((void *)1).  A caller whose buffers are
+ * allocated and freed in stream order on another stream (a caching allocator) must
+ * bind that stream here: the library does not order its work against other streams. */
 int rbf_ctx_set_stream(rbf_ctx *ctx, void *cuda_stream);
 const char *rbf_last_error(const rbf_ctx *ctx);
 const char *rbf_version(void);
@@ -153,6 +165,33 @@ int rbf_spmm(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const
 int rbf_csr_to_csc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr,
                    const int32_t *col, const double *val, int64_t *col_ptr_out,
                    int32_t *row_out, double *val_out);
+
+/* ---- learned stencil surrogate (no counterpart in the reference) ------------ */
+/* Kernels of the MLP that predicts stencil weights (training and inference run on
+ * them).  All arrays are device pointers; bf16 matrices are row-major with leading
+ * dimensions that are multiples of 8 and 16-byte aligned rows.
+ * rbf_mlp_gemm: C = A * B^T (+ bias), A M x K, B N x K, K a multiple of 32, FP32
+ * accumulation on the tensor cores; epi 0: none, 1: GELU, 2: multiply by GELU'(aux);
+ * writes any of Zf (FP32 before the epilogue), Cf (FP32), Cb (bf16). */
+int rbf_mlp_gemm(rbf_ctx *ctx, int32_t M, int32_t N, int32_t K, const void *A, int32_t lda, const void *B,
+                 int32_t ldb, const float *bias, int32_t epi, const float *aux, int32_t ldaux, float *Cf,
+                 int32_t ldcf, void *Cb, int32_t ldcb, float *Zf, int32_t ldz);
+int rbf_mlp_transpose(rbf_ctx *ctx, int32_t rows, int32_t cols, const void *in, int32_t ldi, void *out,
+                      int32_t ldo);
+int rbf_mlp_to_bf16(rbf_ctx *ctx, int32_t rows, int32_t cols, int32_t pad_cols, const float *in, int32_t ldi,
+                    void *out, int32_t ldo);
+/* network inputs: for every stencil the k offsets x_i - x0 (stencil order) divided by the
+ * power of two s >= the stencil radius (the solver's local units), bf16, row stride ldo.
+ * data holds n_data points; an adjl entry outside [0, n_data) is an RBF_ERR_ARGUMENT. */
+int rbf_mlp_features(rbf_ctx *ctx, const double *data, int64_t n_data, const double *eval, int32_t dim,
+                     const int32_t *adjl, int64_t ne, int32_t k, void *out, int32_t ldo);
+/* mean squared error over rows x cols and its gradient (bf16, zero in the padding) */
+int rbf_mlp_mse(rbf_ctx *ctx, int32_t rows, int32_t cols, const float *Y, int32_t ldy, const float *T,
+                int32_t ldt, void *dY, int32_t ldd, int32_t pad_cols, float *loss);
+int rbf_mlp_colsum(rbf_ctx *ctx, int32_t rows, int32_t cols, const void *in, int32_t ldi, float *out);
+/* Adam step (t = step >= 1) on FP32 parameters; p_bf16 (optional) receives their bf16 copy */
+int rbf_mlp_adam(rbf_ctx *ctx, int64_t n, float *p, const float *g, float *m, float *v, float lr, float b1,
+                 float b2, float eps, int32_t step, void *p_bf16);
 
 /* ---- allocation-free apply (no counterpart in the reference) ---------------- */
 /* Same contract as rbf_spmm, for callers that cannot allocate device memory while

@@ -80,6 +80,22 @@ class Context:
             raise RuntimeError(f"rbf_ctx_create({device}) failed with {st}: no usable CUDA device")
         self.handle = h
         self.device = device
+        self._bound = None
+
+    @property
+    def h(self):
+        """The context handle, bound first to torch's current stream on this device.
+
+        torch's caching allocator recycles a freed tensor's memory in the order of torch's
+        stream, so every library launch must be ordered on that same stream: a kernel on
+        another stream could still write memory that torch already handed to a new tensor.
+        The legacy default stream (handle 0 in torch) is passed as cudaStreamLegacy."""
+        torch = _torch()
+        s = torch.cuda.current_stream(self.device).cuda_stream or 1
+        if s != self._bound:
+            self.check(self.lib.rbf_ctx_set_stream(self.handle, ctypes.c_void_p(s)))
+            self._bound = s
+        return self.handle
 
     @classmethod
     def default(cls, device: int = 0) -> "Context":
@@ -93,7 +109,10 @@ class Context:
             _raise(st, self.lib.rbf_last_error(self.handle).decode())
 
     def set_stream(self, stream_handle: int | None):
+        """Bind a raw cudaStream_t (None: the context's own stream).  Calls through this
+        package rebind to torch's current stream; this is for direct C-ABI use."""
         self.check(self.lib.rbf_ctx_set_stream(self.handle, ctypes.c_void_p(stream_handle or 0)))
+        self._bound = stream_handle or None
 
     def __del__(self):
         try:
@@ -351,7 +370,7 @@ def find_neighbors(data, eval_points=None, k: int | None = None, *, ctx: Context
             out = _torch().empty((ne, k), dtype=_torch().int32, device=q.device)
         else:
             out = np.empty((ne, k), dtype=np.int32)
-    ctx.check(ctx.lib.rbf_knn(ctx.handle, _ptr(d), d.shape[0], _ptr(q), ne, d.shape[1], k, _ptr(out)))
+    ctx.check(ctx.lib.rbf_knn(ctx.h, _ptr(d), d.shape[0], _ptr(q), ne, d.shape[1], k, _ptr(out)))
     return out
 
 
@@ -381,7 +400,7 @@ class WeightsCSR:
         cp = torch.empty(ns + 1, dtype=torch.int64, device=dev)
         rw = torch.empty(self.nnz, dtype=torch.int32, device=dev)
         vv = torch.empty(self.nnz, dtype=torch.float64, device=dev)
-        self.ctx.check(self.ctx.lib.rbf_csr_to_csc(self.ctx.handle, ne, ns, _ptr(self.row_ptr), _ptr(self.col),
+        self.ctx.check(self.ctx.lib.rbf_csr_to_csc(self.ctx.h, ne, ns, _ptr(self.row_ptr), _ptr(self.col),
                                                    _ptr(self.val), _ptr(cp), _ptr(rw), _ptr(vv)))
         return cp, rw, vv
 
@@ -424,7 +443,7 @@ def _spmm(W: WeightsCSR, x, y=None, alpha=1.0, beta=0.0, layout="colmajor"):
             yb.copy_(yy.T if lay == 0 else yy)
     if nf == 1:
         ldx = ldy = 1
-    ctx.check(ctx.lib.rbf_spmm(ctx.handle, ne, ns, _ptr(W.row_ptr), _ptr(W.col), _ptr(W.val), nf, lay, _ptr(xb),
+    ctx.check(ctx.lib.rbf_spmm(ctx.h, ne, ns, _ptr(W.row_ptr), _ptr(W.col), _ptr(W.val), nf, lay, _ptr(xb),
                                ldx, float(alpha), float(beta), _ptr(yb), ldy))
     res = yb.T if lay == 0 else yb
     res = res.reshape(out_shape)
@@ -459,7 +478,7 @@ def _hermite_arrays(hermite, ns, dim):
 
 
 def build_weights(ops, data, eval_points, adjl, basis, hermite=None, precision="fp64", *, ctx=None,
-                  refine_steps=0, tol=0.0, return_status=False, stats=None):
+                  refine_steps=0, tol=0.0, return_status=False, stats=None, flags=0, seed=None):
     """Weights of `ops` (list of (op_code, op_dim)) on stencils adjl; returns a list of WeightsCSR.
 
     The drop-in for _build_weights (src/solve/api.jl:26-35, 167-196)."""
@@ -485,6 +504,10 @@ def build_weights(ops, data, eval_points, adjl, basis, hermite=None, precision="
     cfg.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     cfg.refine_steps = refine_steps
     cfg.tol = tol
+    cfg.flags = flags
+    if seed is not None:
+        seed = seed.to(torch.float32).contiguous()
+        cfg.seed = seed.data_ptr()
     herm = _hermite_arrays(hermite, ns, dim)
     hs = None
     keep = []
@@ -494,13 +517,13 @@ def build_weights(ops, data, eval_points, adjl, basis, hermite=None, precision="
         keep.append(herm)
     row_ptr = torch.empty(ne + 1, dtype=torch.int64, device=dev)
     nnz = ctypes.c_int64(0)
-    ctx.check(ctx.lib.rbf_build_count(ctx.handle, ns, ne, k, ctypes.byref(hs) if hs else None, _ptr(row_ptr),
+    ctx.check(ctx.lib.rbf_build_count(ctx.h, ns, ne, k, ctypes.byref(hs) if hs else None, _ptr(row_ptr),
                                       ctypes.byref(nnz)))
     col = torch.empty(nnz.value, dtype=torch.int32, device=dev)
     val = torch.empty((len(ops), nnz.value), dtype=torch.float64, device=dev)
     status = torch.empty(ne, dtype=torch.int8, device=dev) if return_status else None
     st = _native.BuildStats() if stats is None else stats
-    ctx.check(ctx.lib.rbf_build(ctx.handle, ctypes.byref(cfg), _ptr(d), ns, _ptr(q), ne, _ptr(a), k,
+    ctx.check(ctx.lib.rbf_build(ctx.h, ctypes.byref(cfg), _ptr(d), ns, _ptr(q), ne, _ptr(a), k,
                                 ctypes.byref(hs) if hs else None, _ptr(row_ptr), _ptr(col), _ptr(val),
                                 _ptr(status), ctypes.byref(st)))
     Ws = [WeightsCSR(row_ptr, col, val[i], (ne, ns), ctx) for i in range(len(ops))]

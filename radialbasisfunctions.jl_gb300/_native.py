@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
               "-Xptxas", "-warn-spills"]
 
 SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "stencil_build.cu", "stencil_refined_a.cu",
-           "stencil_refined_b.cu", "diag.cu"]
+           "stencil_refined_b.cu", "diag.cu", "mlp.cu"]
 
 
 def _nvcc():
@@ -81,7 +81,8 @@ class BuildCfg(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_int32), ("phs", ctypes.c_int32), ("poly_deg", ctypes.c_int32),
                 ("nops", ctypes.c_int32), ("op_code", ctypes.c_int32 * RBF_MAX_OPS),
                 ("op_dim", ctypes.c_int32 * RBF_MAX_OPS), ("precision", ctypes.c_int32),
-                ("refine_steps", ctypes.c_int32), ("tol", ctypes.c_double)]
+                ("refine_steps", ctypes.c_int32), ("tol", ctypes.c_double), ("flags", ctypes.c_int32),
+                ("seed", ctypes.c_void_p)]
 
 
 class Hermite(ctypes.Structure):
@@ -93,7 +94,7 @@ class BuildStats(ctypes.Structure):
     _fields_ = [("n_stencils", ctypes.c_int64), ("n_identity_rows", ctypes.c_int64),
                 ("n_fallback", ctypes.c_int64), ("n_singular", ctypes.c_int64),
                 ("max_residual", ctypes.c_double), ("ms_knn", ctypes.c_float),
-                ("ms_build", ctypes.c_float), ("ms_total", ctypes.c_float)]
+                ("ms_build", ctypes.c_float), ("ms_total", ctypes.c_float), ("n_residuals", ctypes.c_int64)]
 
 
 # exported entry points and their signatures (checked by the CPU tests against include/rbffd.h)
@@ -116,6 +117,14 @@ SIGNATURES = {
     "rbf_spmm_noalloc": (_I, [_P, _I64, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _D, _D, _P, _I64]),
     "rbf_diag_fma_peak": (_I, [_P, _I32, ctypes.POINTER(_D)]),
     "rbf_ctx_kernel_launches": (_I64, [_P]),
+    "rbf_mlp_gemm": (_I, [_P, _I32, _I32, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32]),
+    "rbf_mlp_transpose": (_I, [_P, _I32, _I32, _P, _I32, _P, _I32]),
+    "rbf_mlp_features": (_I, [_P, _P, _I64, _P, _I32, _P, _I64, _I32, _P, _I32]),
+    "rbf_mlp_to_bf16": (_I, [_P, _I32, _I32, _I32, _P, _I32, _P, _I32]),
+    "rbf_mlp_mse": (_I, [_P, _I32, _I32, _P, _I32, _P, _I32, _P, _I32, _I32, _P]),
+    "rbf_mlp_colsum": (_I, [_P, _I32, _I32, _P, _I32, _P]),
+    "rbf_mlp_adam": (_I, [_P, _I64, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                          _I32, _P]),
 }
 
 _lib = None

@@ -371,6 +371,15 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
         const float errc = u8 * qmag * 1.0001f;
         int qc[3] = {0, 0, 0};
         cell_of<DIM>(g, qp, qc);
+        float lof[3], hf[3];
+        float gmag = qmag;
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+            lof[d] = (float)g.lo[d];
+            hf[d] = (float)g.h[d];
+            gmag = fmaxf(gmag, fabsf(lof[d]) + hf[d] * (float)g.nc[d]);
+        }
+        const float slackf = 16.0f * 5.9604645e-08f * gmag + 1e-30f;
 
         float key[SLOTS];
         int32_t kid[SLOTS];
@@ -508,28 +517,26 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                 }
                 __syncwarp();
             }
-            double cover = INFINITY;
+            // distance to the outside of the scanned block, in FP32: every face position and
+            // the query carry a rounding error below u*mag, covered by the slack below
+            float cover = INFINITY;
             bool all_covered = true;
 #pragma unroll
             for (int d = 0; d < DIM; d++) {
                 if (qc[d] - R > 0) {
                     all_covered = false;
-                    cover = fmin(cover, qp[d] - (g.lo[d] + (double)(qc[d] - R) * g.h[d]));
+                    cover = fminf(cover, qf[d] - fmaf((float)(qc[d] - R), hf[d], lof[d]));
                 }
                 if (qc[d] + R < g.nc[d] - 1) {
                     all_covered = false;
-                    cover = fmin(cover, (g.lo[d] + (double)(qc[d] + R + 1) * g.h[d]) - qp[d]);
+                    cover = fminf(cover, fmaf((float)(qc[d] + R + 1), hf[d], lof[d]) - qf[d]);
                 }
             }
             if (all_covered) break;
             if (kth < INFINITY) {
                 const float dk = sqrtf(kth);
                 const float reach = dk + errc + u8 * dk;
-                double mg = 0.0;
-#pragma unroll
-                for (int d = 0; d < DIM; d++) mg = fmax(mg, fabs(qp[d]) + fabs(g.lo[d]) + g.h[d] * g.nc[d]);
-                const double c = cover * (1.0 - 1e-6) - 4e-15 * mg;
-                if ((double)reach < c) break;
+                if (reach < cover * (1.0f - 1e-5f) - slackf) break;
             }
             r_in = R;
         }
@@ -612,10 +619,13 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
             for (int s = 1; s < SLOTS; s++)
                 if (s == ((k - 1) >> 5)) kk = xk[s];
             kk = __shfl_sync(0xffffffffu, kk, (k - 1) & 31);
-            const double dk_exact = sqrt(__longlong_as_double((long long)kk));
+            // exact k-th squared distance rounded up vs the squared lower bound of any unlisted
+            // point's distance rounded down (no FP64 square roots)
+            const float dk2_up = __double2float_ru(__longlong_as_double((long long)kk));
             const float dt = sqrtf(kth);
-            const double floor_unlisted = (double)dt - (double)(errc + u8 * dt) * 1.0001;
-            certified = (kth < INFINITY) && (dk_exact < floor_unlisted);
+            const float floor_unlisted = dt - (errc + u8 * dt) * 1.0001f;
+            certified = (kth < INFINITY) && (floor_unlisted > 0.0f) &&
+                        (dk2_up < __fmul_rd(floor_unlisted, floor_unlisted) * (1.0f - 1e-6f));
         }
         if (certified) {
 #pragma unroll

@@ -343,6 +343,15 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
     P.max_resid = reinterpret_cast<double *>(counters.as<unsigned long long>() + 8);
     P.refine_steps = cfg->refine_steps > 0 ? cfg->refine_steps : 6;
     P.tol = cfg->tol > 0 ? cfg->tol : 1e-9;
+    P.flags = cfg->flags;
+    P.seed = cfg->seed;
+    if (cfg->precision == RBF_PREC_LEARNED) {
+        if (!cfg->seed || !rbf_is_device_ptr(cfg->seed))
+            return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the learned build needs a device pointer to the predicted weights");
+        if (cfg->nops != 1) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the learned build predicts one operator");
+    } else {
+        P.seed = nullptr;
+    }
 
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
@@ -351,10 +360,10 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
     int st;
     if (cfg->precision == RBF_PREC_FP64)
         st = rbf_build_fp64_launch(ctx, P);
-    else if (cfg->precision == RBF_PREC_FP32_REFINED)
+    else if (cfg->precision == RBF_PREC_FP32_REFINED || cfg->precision == RBF_PREC_LEARNED)
         st = rbf_build_fp32_launch(ctx, P);
     else
-        st = rbf_fail(ctx, RBF_ERR_UNSUPPORTED, "precision mode %d is driven from the host (learned seed)", cfg->precision);
+        st = rbf_fail(ctx, RBF_ERR_ARGUMENT, "unknown precision mode %d", cfg->precision);
     cudaEventRecord(ev1, ctx->stream);
     if (st != RBF_OK) {
         cudaEventDestroy(ev0);
@@ -382,6 +391,7 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
         stats->ms_build = ms;
         stats->ms_knn = 0.f;
         stats->ms_total = ms;
+        stats->n_residuals = (int64_t)hc[4];
     }
     if (hc[1]) return rbf_fail(ctx, RBF_ERR_NOT_FOUND, "evaluation point not found in stencil data (%llu stencils)", hc[1]);
     if (hc[0]) return rbf_fail(ctx, RBF_ERR_SINGULAR, "%llu stencil system(s) are singular", hc[0]);

@@ -15,7 +15,7 @@
 
 namespace {
 
-template <int TPR>
+template <int TPR, int U>
 __global__ void __launch_bounds__(256) spmv_kernel(int64_t ne, const int64_t *__restrict__ rp,
                                                    const int32_t *__restrict__ col,
                                                    const double *__restrict__ val,
@@ -29,15 +29,24 @@ __global__ void __launch_bounds__(256) spmv_kernel(int64_t ne, const int64_t *__
     for (int64_t r0 = first; r0 < ne; r0 += groups) {
         const int64_t r = r0 + (threadIdx.x & 31) / TPR;
         const bool live = r < ne;
-        const int64_t a = live ? rp[r] : 0, b = live ? rp[r + 1] : 0;
-        double s0 = 0.0, s1 = 0.0;
-        int64_t p = a + sub;
-        for (; p + TPR < b; p += 2 * TPR) {
-            s0 = fma(__ldg(&val[p]), __ldg(&x[__ldg(&col[p])]), s0);
-            s1 = fma(__ldg(&val[p + TPR]), __ldg(&x[__ldg(&col[p + TPR])]), s1);
+        const int64_t a = live ? __ldg(&rp[r]) : 0, b = live ? __ldg(&rp[r + 1]) : 0;
+        double s = 0.0;
+        // U entries per lane per chunk: all column and value loads issue first, then all
+        // gathers, so each lane has U independent gathers in flight
+        for (int64_t p0 = a + sub; p0 < b; p0 += (int64_t)U * TPR) {
+            int32_t c[U];
+            double v[U], xv[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int64_t p = p0 + (int64_t)u * TPR;
+                c[u] = p < b ? __ldg(&col[p]) : -1;
+                v[u] = p < b ? __ldg(&val[p]) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) xv[u] = c[u] >= 0 ? __ldg(&x[c[u]]) : 0.0;
+#pragma unroll
+            for (int u = 0; u < U; u++) s = fma(v[u], xv[u], s);
         }
-        if (p < b) s0 = fma(__ldg(&val[p]), __ldg(&x[__ldg(&col[p])]), s0);
-        double s = s0 + s1;
 #pragma unroll
         for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
         if (sub == 0 && live) y[r] = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * y[r]);
@@ -163,8 +172,8 @@ int rbf_spmm_device(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *d_rp, c
     if (ne == 0 || nf == 0) return RBF_OK;
     if (nf == 1) {
         const int TPR = 8;
-        spmv_kernel<TPR><<<blocks_for(ctx, ne * TPR, 256, 16), 256, 0, ctx->stream>>>(ne, d_rp, d_col, d_val, d_X,
-                                                                                      alpha, beta, d_Y);
+        spmv_kernel<TPR, 4><<<blocks_for(ctx, ne * TPR, 256, 16), 256, 0, ctx->stream>>>(ne, d_rp, d_col, d_val, d_X,
+                                                                                         alpha, beta, d_Y);
         RBF_CHECK_LAUNCH(ctx);
         return RBF_OK;
     }
@@ -290,8 +299,8 @@ extern "C" int rbf_spmm_noalloc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int6
     if (ne == 0) return RBF_OK;
     if (!staged) {
         if (nf == 1) {
-            spmv_kernel<8><<<blocks_for(ctx, ne * 8, 256, 16), 256, 0, ctx->stream>>>(ne, row_ptr, col, val, X, alpha,
-                                                                                      beta, Y);
+            spmv_kernel<8, 4><<<blocks_for(ctx, ne * 8, 256, 16), 256, 0, ctx->stream>>>(ne, row_ptr, col, val, X, alpha,
+                                                                                         beta, Y);
             RBF_CHECK_LAUNCH(ctx);
         } else {
             for (int f0 = 0; f0 < nf; f0 += 32) {

@@ -122,6 +122,7 @@ __global__ void build_fp32r_kernel(StencilParams P, int wpb, size_t warp_bytes) 
                 if (step >= P.refine_steps || !isfinite(dmaxf)) break;
                 // FP64 residual r = b - A x (A symmetric: read column i as row i); rows k..n-1
                 // are the polynomial-reproduction constraints P^T w = L(p)
+                if (lane == 0) atomicAdd(&P.counters[4], 1ull);
                 for (int i = lane; i < n; i += 32) {
                     for (int q = 0; q < nops; q++) {
                         double acc = w.M[i * ld + n + q];

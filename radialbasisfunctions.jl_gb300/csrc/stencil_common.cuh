@@ -43,9 +43,12 @@ struct StencilParams {
     double *val;
     int8_t *status;
     unsigned long long *counters;  // [0] singular [1] eval-not-found [2] fallback [3] identity rows
+                                   // [4] FP64 residual evaluations (FP32 paths)
     double *max_resid;             // largest accepted relative residual (FP32 paths)
     int refine_steps;
     double tol;
+    int flags;          // RBF_FLAG_*
+    const float *seed;  // learned seed (ne x k, stencil order, local units) or nullptr
 };
 
 template <class T> __device__ __forceinline__ T rbf_sqrt(T x);

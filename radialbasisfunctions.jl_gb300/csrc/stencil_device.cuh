@@ -264,16 +264,23 @@ __device__ void scatter_row(const StencilParams &P, int64_t e, const WarpSmem &w
                             const double *sol, int sol_ld, int sol_stride) {
     const int k = P.k;
     const int64_t base = P.row_ptr[e];
+    const bool sorted = !(P.flags & RBF_FLAG_STENCIL_ORDER);
+    const bool local = (P.flags & RBF_FLAG_LOCAL_UNITS) != 0;
     for (int i = lane; i < k; i += 32) {
         const int ci = w.cols[i];
-        int rank = 0;
-        for (int j = 0; j < k; j++) {
-            int cj = w.cols[j];
-            rank += (cj < ci) || (cj == ci && j < i);
+        int rank = i;
+        if (sorted) {
+            rank = 0;
+            for (int j = 0; j < k; j++) {
+                int cj = w.cols[j];
+                rank += (cj < ci) || (cj == ci && j < i);
+            }
         }
         P.col[base + rank] = ci;
-        for (int r = 0; r < P.nops; r++)
-            P.val[r * P.nnz + base + rank] = ldexp(sol[i * sol_ld + r * sol_stride], -es * P.op_order[r]);
+        for (int r = 0; r < P.nops; r++) {
+            const double v = sol[i * sol_ld + r * sol_stride];
+            P.val[r * P.nnz + base + rank] = local ? v : ldexp(v, -es * P.op_order[r]);
+        }
     }
 }
 

@@ -327,3 +327,30 @@ def test_errors(pkg):
     with pytest.raises(ValueError):  # regrid has no normal form (api.jl:79-94)
         pkg.RadialBasisOperator(pkg.Regrid(), X, hermite=dict(is_boundary=isb, bc=[pkg.Neumann()] * 3,
                                                               normals=np.ones((3, 2))))
+
+
+# ---------------------------------------------------------------------------- streams
+def test_calls_follow_torch_stream(pkg):
+    """Under a side torch stream the library runs on that stream (the caching allocator's
+    stream order covers its buffers): kNN, build and apply give the default-stream result,
+    and freeing the inputs right after each call is safe."""
+    rng = np.random.default_rng(4)
+    X = torch.from_numpy(rng.uniform(0, 1, (30000, 3))).cuda()
+    f = torch.sin(4 * X[:, 0]) * X[:, 1]
+    adjl0 = pkg.find_neighbors(X, k=30)
+    W0 = pkg.build_weights([(3, 0)], X, None, adjl0, pkg.PHS(3, poly_deg=2))[0]
+    y0 = W0.apply(f)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        outs = []
+        for rep in range(3):
+            Xs = X.clone()
+            adjl = pkg.find_neighbors(Xs, k=30)
+            W = pkg.build_weights([(3, 0)], Xs, None, adjl, pkg.PHS(3, poly_deg=2))[0]
+            outs.append((adjl, W.val, W.apply(f.clone())))
+            del Xs, W
+    s.synchronize()
+    for adjl, val, y in outs:
+        assert torch.equal(adjl, adjl0)
+        assert torch.equal(val, W0.val)
+        assert torch.equal(y, y0)
