@@ -10,11 +10,15 @@ A step is one pass of the hot path over the cloud: k-NN stencils, the weight bui
   e2e    : the same metric through the public API with host inputs and a host result
            (points and field copied in, Laplacian of the field copied out, every step)
 
-The headline build is the FP32-factorised, FP64-refined solve; the plain FP64 build is
-timed beside it and the max row-relative weight difference between them is reported
-(equal-error requirement: <= 1e-8).  `--impl reference` times the CPU oracle (a C
-restatement of the reference algorithm: grid kNN + raw-coordinate assembly + rook
-Bunch-Kaufman, OpenMP on all host cores) on a bounded sample of the same workload.
+The headline build is the learned + FP32-refined solve: an MLP (trained before the timed
+region on 2,000,000 plain-FP64 solver stencils) predicts each stencil's weights from its
+scaled offsets, the prediction seeds the FP32-factorised, FP64-refined solve, and stencils
+whose refinement does not converge fall back to the FP64 solve.  The plain FP64 build and
+the unseeded refined build are timed beside it, and the max row-relative weight difference
+against the plain FP64 weights is reported (equal-error requirement: <= 1e-8).
+`--impl reference` times the CPU oracle (a C restatement of the reference algorithm: grid
+kNN + raw-coordinate assembly + rook Bunch-Kaufman, OpenMP on all host cores) on a bounded
+sample of the same workload.
 """
 import argparse
 import json
@@ -35,13 +39,27 @@ METRIC = "stencils/s built (learned+FP32-refined vs plain FP64, equal err); appl
 
 CONFIGS = {
     # name: (dim, N, phs, poly_deg, k, ops, field description)
-    "lap3d_4M": dict(dim=3, n=4_000_000, phs=3, deg=2, k=30, ops=[(3, 0)], dist="uniform",
-                     desc="3D Laplacian, N=4,000,000 uniform in [0,1]^3, PHS3 deg 2, k=30 (40x40 systems)"),
+    "lap3d_4M": dict(dim=3, n=4_000_000, phs=3, deg=2, k=30, ops=[(3, 0)], dist="uniform", learned=True,
+                     desc="3D Laplacian, N=4,000,000 uniform in [0,1]^3, PHS3 deg 2, k=30 (40x40 systems); "
+                          "learned seed: MLP 90->256->256->256->30 GELU, bf16/FP32-acc, trained on 2,000,000 "
+                          "solver stencils (uniform + linear +/-20% density-gradient clouds)"),
     "lap2d_10k": dict(dim=2, n=10_000, phs=3, deg=2, k=20, ops=[(3, 0)], dist="uniform",
                       desc="2D Laplacian, N=10,000 uniform in [0,1]^2, PHS3 deg 2, k=20 (26x26 systems)"),
     "gradlap3d_1M": dict(dim=3, n=1_000_000, phs=5, deg=2, k=40, ops=[(1, 0), (1, 1), (1, 2), (3, 0)],
                          dist="lattice", desc="3D gradient+Laplacian, 100^3 jittered lattice, PHS5 deg 2, k=40"),
 }
+
+
+PEAKS = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+    os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+
+# DRAM bytes (read + write) per stencil of the headline build kernel, from one ncu capture of
+# that kernel at N = 1,000,000 (3D Laplacian, k = 30); traffic grows with the stencil count.
+KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": 481.4}
+
+
+def peaks_bf16():
+    return PEAKS.get("bf16_tflops", 1900.0)
 
 
 def parse():
@@ -54,6 +72,9 @@ def parse():
     p.add_argument("--n", type=int, default=0, help="override the point count (development runs)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=0, help="stencils in the CPU baseline sample")
+    p.add_argument("--train-stencils", type=int, default=2_000_000, help="solver stencils the surrogate trains on")
+    p.add_argument("--train-epochs", type=int, default=12)
+    p.add_argument("--no-learned", action="store_true", help="headline without the learned seed")
     p.add_argument("--profile-once", action="store_true",
                    help="run each hot kernel once (kNN, FP64 build, FP32-refined build, apply) and exit; "
                         "the driver for ncu captures")
@@ -201,9 +222,23 @@ def main():
     basis = pkg.PHS(cfg["phs"], poly_deg=cfg["deg"])
     k = cfg["k"]
 
+    learned_on = bool(cfg.get("learned")) and not args.no_learned and len(cfg["ops"]) == 1
+    headline = "learned" if learned_on else "fp32_refined"
+    L = None
+    model = None
+    training = None
+    if learned_on:
+        from importlib import import_module
+        L = import_module(pkg.__name__ + ".learned")
+
+    def build(precision, X, adjl, stats=None):
+        if precision == "learned":
+            return L.build_learned(model, cfg["ops"], X, adjl, basis, ctx=ctx, stats=stats)
+        return pkg.build_weights(cfg["ops"], X, None, adjl, basis, precision=precision, ctx=ctx, stats=stats)
+
     def step(precision, X=Xd, f=fd):
         adjl = pkg.find_neighbors(X, k=k, ctx=ctx)
-        Ws = pkg.build_weights(cfg["ops"], X, None, adjl, basis, precision=precision, ctx=ctx)
+        Ws = build(precision, X, adjl)
         y = Ws[-1].apply(f)
         return adjl, Ws, y
 
@@ -230,19 +265,40 @@ def main():
             ms = float(t.item())
         return ms
 
-    headline = "fp32_refined"
+    if learned_on:
+        # ---- surrogate training (untimed): plain FP64 solves on independent seeded clouds,
+        # half uniform, half with a linear +/-20% density gradient; held-out uniform stencils
+        # measure the surrogate's weight error before and after training
+        t0 = time.perf_counter()
+        nt = args.train_stencils
+        Xb, T = L.training_set(nt // 2, nt - nt // 2, k, cfg["dim"], basis, cfg["ops"], seed=5000 + rank, ctx=ctx)
+        Xv, Tv = L.training_set(50_000, 0, k, cfg["dim"], basis, cfg["ops"], seed=9000 + rank, ctx=ctx)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        untrained = L.StencilMLP(k, cfg["dim"], ctx=ctx, seed=0, out_scale=float(T.std()))
+        u_max, u_med = L.surrogate_error(untrained, Xv, Tv)
+        model, hist = L.train_surrogate(Xb, T, k, cfg["dim"], epochs=args.train_epochs, batch=4096, lr=2e-3, ctx=ctx)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        e_max, e_med = L.surrogate_error(model, Xv, Tv)
+        training = {"stencils": nt, "epochs": args.train_epochs, "batch": 4096, "data_s": t1 - t0,
+                    "train_s": t2 - t1, "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1],
+                    "heldout_row_rel_err_median": {"untrained": u_med, "trained": e_med},
+                    "heldout_row_rel_err_max": {"untrained": u_max, "trained": e_max},
+                    "dims": model.dims}
+        del Xb, T, Xv, Tv, untrained
+
     if args.profile_once:
         adjl = pkg.find_neighbors(Xd, k=k, ctx=ctx)
         s64, s32 = pkg._native.BuildStats(), pkg._native.BuildStats()
-        W64 = pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision="fp64", ctx=ctx, stats=s64)
-        W32 = pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision=headline, ctx=ctx, stats=s32)
+        W64 = build("fp64", Xd, adjl, s64)
+        W32 = build(headline, Xd, adjl, s32)
         W32[-1].apply(fd)
         torch.cuda.synchronize()
         err = max(row_rel_err_torch(torch, a.row_ptr, k, a.val, b.val) for a, b in zip(W32, W64))
-        print(json.dumps({"profile_once": cfg["desc"], "n": n, "ms_build_fp64": s64.ms_build,
-                          "ms_build_fp32r": s32.ms_build, "fallback": s32.n_fallback, "max_diff": err}))
+        print(json.dumps({"profile_once": cfg["desc"], "n": n, "headline": headline, "ms_build_fp64": s64.ms_build,
+                          "ms_build_headline": s32.ms_build, "fallback": s32.n_fallback, "max_diff": err}))
         return
-    launches0 = ctx.lib.rbf_ctx_kernel_launches(ctx.handle)
     clocks = ClockSampler(local)
     # ---- headline timed region
     for _ in range(args.warmup):
@@ -265,56 +321,74 @@ def main():
         ms = float(t.item())
     value = n * world / (ms * 1e-3)
 
-    # ---- plain FP64 beside it, same workload
+    # ---- the same step with the plain FP64 build (and without the learned seed) beside it
     ms_fp64 = timed(lambda: step("fp64"), max(1, args.steps // 2), 1)
-    # ---- equal-error check: refined vs plain GPU weights, max row-relative difference
+    ms_fp32r = timed(lambda: step("fp32_refined"), max(1, args.steps // 2), 1) if learned_on else ms
+
+    # ---- equal-error check against the plain GPU build (max row-relative weight difference)
     adjl = pkg.find_neighbors(Xd, k=k, ctx=ctx)
-    W64 = pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision="fp64", ctx=ctx)
-    st = pkg._native.BuildStats()
-    W32 = pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision=headline, ctx=ctx, stats=st)
-    err = max(row_rel_err_torch(torch, a.row_ptr, k, a.val, b.val) for a, b in zip(W32, W64))
-    n_fallback = int(st.n_fallback)
-    # ---- per-kernel timings (device-resident, events on the launching stream)
     st64 = pkg._native.BuildStats()
-    pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision="fp64", ctx=ctx, stats=st64)
-    ms_build32 = float(st.ms_build)
-    ms_build64 = float(st64.ms_build)
+    W64 = build("fp64", Xd, adjl, st64)
+    st_h = pkg._native.BuildStats()
+    W_h = build(headline, Xd, adjl, st_h)
+    err = max(row_rel_err_torch(torch, a.row_ptr, k, a.val, b.val) for a, b in zip(W_h, W64))
+    rms = max(float(((a.val - b.val) ** 2).mean().sqrt() / (b.val ** 2).mean().sqrt()) for a, b in zip(W_h, W64))
+    # operator-on-test-function: both operators applied to the field, relative max difference
+    y64, yh = W64[-1].apply(fd), W_h[-1].apply(fd)
+    op_err = float((yh - y64).abs().max() / y64.abs().max())
+    st32 = st_h
+    err32 = err
+    if learned_on:
+        st32 = pkg._native.BuildStats()
+        W32 = build("fp32_refined", Xd, adjl, st32)
+        err32 = max(row_rel_err_torch(torch, a.row_ptr, k, a.val, b.val) for a, b in zip(W32, W64))
+        del W32
+    del W64, W_h
+    # ---- per-stage timings (device-resident, events on the launching stream)
+    ms_b_h = timed(lambda: build(headline, Xd, adjl), 3, 1)
+    ms_b_32 = timed(lambda: build("fp32_refined", Xd, adjl), 3, 1) if learned_on else ms_b_h
+    ms_b_64 = timed(lambda: build("fp64", Xd, adjl), 2, 1)
     ms_knn = timed(lambda: pkg.find_neighbors(Xd, k=k, ctx=ctx), 3, 1)
-    W = W32[-1]
-    y = torch.empty(n, dtype=torch.float64, device=dev)
+    mlp = None
+    if learned_on:
+        feats = model.features(Xd, None, adjl)
+        ms_feat = timed(lambda: model.features(Xd, None, adjl), 3, 1)
+        ms_mlp = timed(lambda: model.predict(feats), 3, 1)
+        fl = 2 * (model.din * model.dims[1] + sum(a * b for a, b in zip(model.dims[1:-2], model.dims[2:-1]))
+                  + model.dims[-2] * model.dout)
+        tf = fl * n / (ms_mlp * 1e-3) / 1e12
+        mlp = {"ms_features": ms_feat, "ms_forward": ms_mlp, "flops_per_stencil": fl, "tflops": tf,
+               "bf16_peak_tflops": peaks_bf16(), "frac_of_bf16_peak": tf / peaks_bf16(),
+               "kernel": "gemm_bf16_kernel (mma.sync m16n8k16, 64x64 tiles)"}
+        del feats
+    W = build(headline, Xd, adjl)[-1]
     ms_spmv = timed(lambda: W.apply(fd), 10, 3)
     nnz = W.nnz
+    # algorithmic bytes of one apply: val (8 B) + col (4 B) per entry, row_ptr (8 B) per row,
+    # the field read once and the result written once
     apply_bytes = nnz * 12 + (n + 1) * 8 + 2 * n * 8
     apply_gbs = apply_bytes / (ms_spmv * 1e-3) / 1e9
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    hbm_src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in peaks else "fallback"
+    del W
+    hbm_peak = PEAKS.get("hbm_gbs", 6800.0)
+    hbm_src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in PEAKS else "fallback"
     fp64_peak = pkg.ctypes.c_double(0.0)
-    ctx.check(ctx.lib.rbf_diag_fma_peak(ctx.handle, 1, pkg.ctypes.byref(fp64_peak)))
+    ctx.check(ctx.lib.rbf_diag_fma_peak(ctx.h, 1, pkg.ctypes.byref(fp64_peak)))
     fp32_peak = pkg.ctypes.c_double(0.0)
-    ctx.check(ctx.lib.rbf_diag_fma_peak(ctx.handle, 0, pkg.ctypes.byref(fp32_peak)))
+    ctx.check(ctx.lib.rbf_diag_fma_peak(ctx.h, 0, pkg.ctypes.byref(fp32_peak)))
     nsys = k + math.comb(cfg["deg"] + cfg["dim"], cfg["dim"])
     R = len(cfg["ops"])
     # algorithmic FLOPs of the reference algorithm per stencil: symmetric factor n^3/3,
     # solve 2 n^2 R, assembly ~10 flops per phi / L(phi) evaluation
     flops_stencil = nsys ** 3 / 3 + 2 * nsys ** 2 * R + 10 * (k * (k + 1) / 2 + R * k)
-    kernels = {"knn_query": ms_knn, "build_fp32r": ms_build32, "spmv": ms_spmv}
-    dom = max(kernels, key=kernels.get)
-    if dom == "spmv":
-        roof = {"kernel": "spmv_kernel", "bound": "hbm", "achieved": apply_gbs, "peak": hbm_peak, "unit": "GB/s",
-                "frac": apply_gbs / hbm_peak, "traffic": None, "peak_source": hbm_src}
-    elif dom == "build_fp32r":
-        ach = flops_stencil * n / (ms_build32 * 1e-3) / 1e12
-        roof = {"kernel": "build_fp32r_kernel", "bound": "fp32 pipe", "achieved": ach, "peak": fp32_peak.value,
-                "unit": "TFLOP/s", "frac": ach / fp32_peak.value, "traffic": None,
-                "peak_source": "FFMA loop measured in this run (rbf_diag_fma_peak)",
-                "flops_per_stencil": flops_stencil}
-    else:
-        kb = (2 * n * cfg["dim"] * 8 + n * k * 4)
-        ach = kb / (ms_knn * 1e-3) / 1e9
-        roof = {"kernel": "knn (grid build + knn_query_kernel)", "bound": "hbm", "achieved": ach, "peak": hbm_peak,
-                "unit": "GB/s", "frac": ach / hbm_peak, "traffic": None, "peak_source": hbm_src}
+    ms_kernel = float(st_h.ms_build)
+    ach = flops_stencil * n / (ms_kernel * 1e-3) / 1e12
+    kname = f"build_refined_reg_kernel<{nsys},{R}>" + (" (learned seed)" if learned_on else "")
+    roof = {"kernel": kname, "bound": "fp64 pipe", "achieved": ach, "peak": fp64_peak.value, "unit": "TFLOP/s",
+            "frac": ach / fp64_peak.value, "traffic": KERNEL_TRAFFIC_PER_STENCIL.get(headline, 0) * n or None,
+            "flops": f"reference FP64 algorithm count per stencil ({flops_stencil:.0f}: n^3/3 + 2n^2R + assembly)",
+            "peak_source": "FP64 FMA loop measured in this run (rbf_diag_fma_peak)",
+            "fp32_pipe": {"peak": fp32_peak.value, "frac": ach / fp32_peak.value},
+            "traffic_source": "ncu dram__bytes_read+write of the same kernel at N=1M, scaled by stencils"}
 
     # ---- e2e through the public API: host points in, host Laplacian of a host field out
     X_pin = torch.from_numpy(X_h).pin_memory()
@@ -324,7 +398,7 @@ def main():
     def e2e_step():
         Xg = X_pin.to(dev, non_blocking=True)
         adj = pkg.find_neighbors(Xg, k=k, ctx=ctx)
-        Ws = pkg.build_weights(cfg["ops"], Xg, None, adj, basis, precision=headline, ctx=ctx)
+        Ws = build(headline, Xg, adj)
         yy = Ws[-1].apply(f_pin.to(dev, non_blocking=True))
         y_pin.copy_(yy, non_blocking=True)
 
@@ -340,22 +414,39 @@ def main():
                "sample": f"{sample} stencils: grid kNN over all {n} points + raw-coordinate rook-BK build"}
 
     if rank == 0:
+        res = lambda s: float(s.n_residuals) / max(1, int(s.n_stencils))
         line = {
             "metric": METRIC, "value": value, "unit": "stencils/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 factor + f64 refinement", "data": "synthetic (seeded)",
-            "config": {"workload": cfg["desc"], "n": n, "k": k, "step": "kNN + build (CSR) + one apply",
+            "vs_baseline": None,
+            "dtype": ("bf16 surrogate seed + " if learned_on else "") + "f32 factor + f64 refinement",
+            "data": "synthetic (seeded)",
+            "config": {"workload": cfg["desc"], "n": n, "k": k, "headline": headline,
+                       "step": "kNN + " + ("features + MLP + " if learned_on else "") + "build (CSR) + one apply",
                        "l2": "inputs larger than L2 (CSR 12 B/nnz x nnz, adjacency 4 B x N x k)",
                        "parallelism": f"replicas x{world}"},
             "plain_fp64": {"value": n * world / (ms_fp64 * 1e-3), "unit": "stencils/s", "ms_per_step": ms_fp64},
+            "fp32_refined_unseeded": {"value": n * world / (ms_fp32r * 1e-3), "unit": "stencils/s",
+                                      "ms_per_step": ms_fp32r},
             "speedup_vs_plain_fp64": ms_fp64 / ms,
-            "build_only": {"fp32_refined_ms": ms_build32, "fp64_ms": ms_build64, "speedup": ms_build64 / ms_build32,
-                           "fp32_refined_stencils_per_s": n / (ms_build32 * 1e-3),
-                           "fp64_stencils_per_s": n / (ms_build64 * 1e-3)},
-            "equal_error": {"max_row_rel_weight_diff_vs_fp64": err, "bar": 1e-8, "fallback_stencils": n_fallback},
+            "build_only": {"headline_ms": ms_b_h, "fp32_refined_ms": ms_b_32, "fp64_ms": ms_b_64,
+                           "speedup_headline_vs_fp64": ms_b_64 / ms_b_h,
+                           "headline_stencils_per_s": n / (ms_b_h * 1e-3),
+                           "fp64_stencils_per_s": n / (ms_b_64 * 1e-3),
+                           "kernel_ms": {"headline": ms_kernel, "fp32_refined": float(st32.ms_build),
+                                         "fp64": float(st64.ms_build)}},
+            "equal_error": {"max_row_rel_weight_diff_vs_fp64": err, "rms_rel_weight_diff": rms,
+                            "operator_on_test_function_rel_diff": op_err, "bar": 1e-8,
+                            "fallback_stencils": int(st_h.n_fallback),
+                            "fp32_refined_unseeded_max_diff": err32},
+            "refinement": {"residuals_per_stencil": res(st_h), "unseeded_residuals_per_stencil": res(st32),
+                           "fallback_unseeded": int(st32.n_fallback),
+                           "seed_rel_err_mean_judged_by_solve": float(st_h.seed_rel_err_mean) if learned_on else None},
+            "surrogate": training, "mlp": mlp,
             "apply": {"value": apply_gbs, "unit": "GB/s", "ms": ms_spmv, "nnz": nnz,
-                      "frac_of_hbm": apply_gbs / hbm_peak},
-            "kernels_ms": {"knn": ms_knn, "build_fp32r": ms_build32, "build_fp64": ms_build64, "spmv": ms_spmv},
+                      "frac_of_hbm": apply_gbs / hbm_peak, "peak_source": hbm_src},
+            "kernels_ms": {"knn": ms_knn, "build_headline": ms_kernel, "build_fp64": float(st64.ms_build),
+                           "spmv": ms_spmv},
             "peaks": {"fp64_tflops_measured": fp64_peak.value, "fp32_tflops_measured": fp32_peak.value,
                       "hbm_gbs": hbm_peak},
             "roofline": roof,

@@ -70,7 +70,11 @@ typedef struct rbf_build_cfg {
                                      (0: default 1e-9); otherwise the FP64 solve is used */
     int32_t flags;                /* RBF_FLAG_* bits                                 */
     const float *seed;            /* RBF_PREC_LEARNED: predicted weights, ne x k floats in
-                                     stencil order and local units (device pointer)   */
+                                     stencil order and local units (device pointer); the
+                                     starting point of the refinement where the register
+                                     kernels serve the system size (3k >= n), otherwise
+                                     unused (the first FP32 solve reaches the same error
+                                     floor from any start)                            */
 } rbf_build_cfg;
 
 /* flags */
@@ -100,6 +104,9 @@ typedef struct rbf_build_stats {
                                 estimate of the accepted weights)                      */
     float ms_knn, ms_build, ms_total;
     int64_t n_residuals;     /* FP32 paths: FP64 residual evaluations over all stencils  */
+    double seed_rel_err_mean; /* RBF_PREC_LEARNED: mean over seeded stencils of
+                                 min(1, |x1 - seed| / |x1|), x1 the weights after the first
+                                 FP32 solve -- the seed's error as judged by the solver   */
 } rbf_build_stats;
 
 typedef struct rbf_ctx rbf_ctx;

@@ -94,7 +94,8 @@ class BuildStats(ctypes.Structure):
     _fields_ = [("n_stencils", ctypes.c_int64), ("n_identity_rows", ctypes.c_int64),
                 ("n_fallback", ctypes.c_int64), ("n_singular", ctypes.c_int64),
                 ("max_residual", ctypes.c_double), ("ms_knn", ctypes.c_float),
-                ("ms_build", ctypes.c_float), ("ms_total", ctypes.c_float), ("n_residuals", ctypes.c_int64)]
+                ("ms_build", ctypes.c_float), ("ms_total", ctypes.c_float), ("n_residuals", ctypes.c_int64),
+                ("seed_rel_err_mean", ctypes.c_double)]
 
 
 # exported entry points and their signatures (checked by the CPU tests against include/rbffd.h)

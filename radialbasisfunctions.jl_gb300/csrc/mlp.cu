@@ -257,42 +257,58 @@ int rbf_mlp_adam(rbf_ctx *ctx, int64_t n, float *p, const float *g, float *m, fl
 }  // extern "C"
 
 namespace {
+// double -> float on the integer pipe (mantissa truncated; bf16 inputs need far less)
+__device__ __forceinline__ float trunc_to_float(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int e = (int)((b >> 52) & 0x7ffu) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+}
+
 // Network inputs of one stencil: the offsets x_i - x0 of its k points (stencil order, i.e.
 // sorted by distance) in the local units of the solver (divided by the power of two s >=
-// the stencil radius), as bf16, padded with zeros to ldo.  One warp per stencil.
+// the stencil radius), as bf16, padded with zeros to ldo.  One warp per stencil.  Only the
+// subtraction runs in FP64 (cancellation); the rest is FP32, which is far more accurate than
+// the bf16 result (the FP64 pipe of this part is ~70x slower than FP32).
 __global__ void features_kernel(const double *__restrict__ data, const double *__restrict__ eval, int dim,
                                 const int32_t *__restrict__ adjl, int64_t ne, int k, __nv_bfloat16 *__restrict__ out,
                                 int ldo) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < ne; e += nw) {
-        double x0[3] = {0, 0, 0};
-        for (int d = 0; d < dim; d++) x0[d] = eval[e * dim + d];
-        double dv[2][3];
-        double r2max = 0.0;
+        float dv[2][3];
+        float r2max = 0.0f;
 #pragma unroll
         for (int s = 0; s < 2; s++) {
             const int i = lane + 32 * s;
-            for (int d = 0; d < 3; d++) dv[s][d] = 0.0;
+#pragma unroll
+            for (int d = 0; d < 3; d++) dv[s][d] = 0.0f;
             if (i < k) {
-                const int32_t g = adjl[e * k + i];
-                double r2 = 0.0;
+                const int32_t g = __ldg(&adjl[e * k + i]);
+                float r2 = 0.0f;
                 for (int d = 0; d < dim; d++) {
-                    dv[s][d] = data[(int64_t)g * dim + d] - x0[d];
-                    r2 += dv[s][d] * dv[s][d];
+                    dv[s][d] = trunc_to_float(__ldg(&data[(int64_t)g * dim + d]) - __ldg(&eval[e * dim + d]));
+                    r2 = fmaf(dv[s][d], dv[s][d], r2);
                 }
-                r2max = fmax(r2max, r2);
+                r2max = fmaxf(r2max, r2);
             }
         }
-        for (int o = 16; o > 0; o >>= 1) r2max = fmax(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r2max = fmaxf(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
         int es = 0;
-        if (r2max > 0.0) frexp(sqrt(r2max), &es);
+        if (r2max > 0.0f) frexpf(sqrtf(r2max), &es);
+        // 2^-es as an exact float (es within the normal range; otherwise ldexpf)
+        const bool pow_ok = es > -126 && es < 127;
+        const float sc = pow_ok ? __int_as_float((127 - es) << 23) : 1.0f;
         __nv_bfloat16 *row = out + (size_t)e * ldo;
 #pragma unroll
         for (int s = 0; s < 2; s++) {
             const int i = lane + 32 * s;
             if (i < k)
-                for (int d = 0; d < dim; d++) row[i * dim + d] = __float2bfloat16_rn((float)ldexp(dv[s][d], -es));
+                for (int d = 0; d < dim; d++)
+                    row[i * dim + d] = __float2bfloat16_rn(pow_ok ? dv[s][d] * sc : ldexpf(dv[s][d], -es));
         }
         for (int c = k * dim + lane; c < ldo; c += 32) row[c] = __float2bfloat16_rn(0.0f);
     }

@@ -392,6 +392,7 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
         stats->ms_knn = 0.f;
         stats->ms_total = ms;
         stats->n_residuals = (int64_t)hc[4];
+        stats->seed_rel_err_mean = hc[6] ? (double)hc[5] * 1e-6 / (double)hc[6] : 0.0;
     }
     if (hc[1]) return rbf_fail(ctx, RBF_ERR_NOT_FOUND, "evaluation point not found in stencil data (%llu stencils)", hc[1]);
     if (hc[0]) return rbf_fail(ctx, RBF_ERR_SINGULAR, "%llu stencil system(s) are singular", hc[0]);

@@ -107,18 +107,22 @@ __global__ void build_fp32r_kernel(StencilParams P, int wpb, size_t warp_bytes) 
                     xmaxf = fmaxf(xmaxf, __shfl_xor_sync(0xffffffffu, xmaxf, o));
                 }
                 __syncwarp();
-                // accept when the correction is below tol and shrinking (contraction < 1/2),
-                // so that the error left after adding it is below tol as well
                 // the first correction measures the FP32 solve's error, about cond(A) * 2^-24;
                 // past 1e-3 (cond ~ 1e5) the double-float entries (~2^-44) could move the
-                // weights by more than 1e-9, so such a stencil takes the FP64 path
-                if (step == 1 && !(dmaxf <= 1e-3f * xmaxf)) break;
-                if (step > 0 && dmaxf <= tolf * xmaxf && dmaxf <= 0.5f * dprev) {
-                    accepted = true;
-                    est_final = xmaxf > 0.0f ? (double)(dmaxf / xmaxf) : 0.0;
-                    break;
+                // weights by more than 1e-9, so such a stencil takes the FP64 path.  |d_s|
+                // estimates the error before a correction: accept once it is below tol and
+                // shrinking, so that the error left after adding it is below tol as well.
+                if (step == 0) {
+                    dprev = xmaxf;
+                } else {
+                    if (step == 1 && !(dmaxf <= 1e-3f * dprev)) break;
+                    if (dmaxf <= tolf * xmaxf && dmaxf <= 0.5f * dprev) {
+                        accepted = true;
+                        est_final = xmaxf > 0.0f ? (double)(dmaxf / xmaxf) : 0.0;
+                        break;
+                    }
+                    dprev = dmaxf;
                 }
-                dprev = dmaxf;
                 if (step >= P.refine_steps || !isfinite(dmaxf)) break;
                 // FP64 residual r = b - A x (A symmetric: read column i as row i); rows k..n-1
                 // are the polynomial-reproduction constraints P^T w = L(p)

@@ -44,6 +44,8 @@ struct StencilParams {
     int8_t *status;
     unsigned long long *counters;  // [0] singular [1] eval-not-found [2] fallback [3] identity rows
                                    // [4] FP64 residual evaluations (FP32 paths)
+                                   // [5] sum of 1e6 * min(1, |x1 - seed| / |x1|) over seeded
+                                   //     stencils, [6] their number
     double *max_resid;             // largest accepted relative residual (FP32 paths)
     int refine_steps;
     double tol;
