@@ -200,6 +200,48 @@ int rbf_mlp_colsum(rbf_ctx *ctx, int32_t rows, int32_t cols, const void *in, int
 int rbf_mlp_adam(rbf_ctx *ctx, int64_t n, float *p, const float *g, float *m, float *v, float lr, float b1,
                  float b2, float eps, int32_t step, void *p_bf16);
 
+/* ---- batched build of uneven stencils (no counterpart in the reference) ------ */
+/* Ragged stencils: the neighbours of eval point e are adj_idx[adj_ptr[e] .. adj_ptr[e+1])
+ * (adj_ptr[0] = 0, 1 <= length <= RBF_MAX_STENCIL, ne + 1 entries), first entry the
+ * nearest as find_neighbors orders them.  rbf_build_count_ragged is rbf_build_count for
+ * them (Dirichlet eval rows hold 1 entry, every other row its stencil's length). */
+int rbf_build_count_ragged(rbf_ctx *ctx, int64_t ns, int64_t ne, const int64_t *adj_ptr,
+                           const rbf_hermite *herm, int64_t *row_ptr_out, int64_t *nnz_out);
+/* Builds every stencil of a ragged batch in one persistent launch.  Stencils are binned
+ * by size class (stencil length k, polynomial degree: system size n = k + nmon) and each
+ * class runs with the tile shape the autotuner chose for it: one warp per stencil, or the
+ * whole 128-thread block on one stencil.  poly_deg_per (optional, ne entries in -1..6)
+ * overrides cfg->poly_deg per stencil.  precision: RBF_PREC_FP64 or RBF_PREC_FP32_REFINED.
+ * tune: 0 cached choices (a heuristic for classes never tuned), 1 autotune the classes
+ * not tuned yet (timing both tiles on up to 16384 stencils of each class with at least
+ * 1024), 2 re-tune every class.  Output layout and errors as rbf_build. */
+int rbf_build_batched(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns,
+                      const double *eval, int64_t ne, const int64_t *adj_ptr, const int32_t *adj_idx,
+                      const int8_t *poly_deg_per, const rbf_hermite *herm, const int64_t *row_ptr,
+                      int32_t *col, double *val, int8_t *status_out, rbf_build_stats *stats,
+                      int32_t tune);
+/* The context's tuning table, one line per size class (tile chosen and trial times). */
+int rbf_tuning_report(rbf_ctx *ctx, char *buf, int64_t len);
+
+/* ---- build -> apply in one CUDA graph (no counterpart in the reference) ------ */
+/* A time loop over moving points (update_weights! then the operator call,
+ * src/operators/operators.jl:589-602, 217-218) re-builds the weights on fixed stencils and
+ * applies them every step.  A plan captures that pair -- counter reset, build kernel, SpMV
+ * y = W[op_index] x -- once into a CUDA graph on device buffers fixed at creation (every
+ * pointer must be a device pointer; row_ptr from rbf_build_count, uniform stencils, no
+ * boundary, precision FP64 or FP32-refined).  rbf_plan_launch enqueues the graph on the
+ * context's stream; coordinates in data/eval and the field x may be rewritten in place
+ * between launches.  rbf_plan_counters reads the last launch's singular / fallback /
+ * FP64-residual counts (synchronising the stream). */
+typedef struct rbf_plan rbf_plan;
+int rbf_plan_create(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns,
+                    const double *eval, int64_t ne, const int32_t *adjl, int32_t k,
+                    const int64_t *row_ptr, int32_t *col, double *val, int32_t op_index,
+                    const double *x, double *y, rbf_plan **out);
+int rbf_plan_launch(rbf_plan *plan);
+int rbf_plan_counters(rbf_plan *plan, int64_t *singular, int64_t *fallback, int64_t *residuals);
+int rbf_plan_destroy(rbf_plan *plan);
+
 /* ---- allocation-free apply (no counterpart in the reference) ---------------- */
 /* Same contract as rbf_spmm, for callers that cannot allocate device memory while
  * applying an operator (code inside another framework's memory pool, or a time-stepping

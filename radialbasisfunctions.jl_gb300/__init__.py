@@ -36,6 +36,7 @@ __all__ = [
     "find_neighbors", "autoselect_k", "Laplacian", "Partial", "Jacobian", "Regrid", "Operators",
     "laplacian", "partial", "gradient", "jacobian", "regrid", "RadialBasisOperator", "WeightsCSR",
     "weights", "update_weights", "mul", "DimensionMismatch", "SingularException", "Context", "build_library",
+    "build_weights", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph",
 ]
 
 build_library = _native.build_library
@@ -530,6 +531,153 @@ def build_weights(ops, data, eval_points, adjl, basis, hermite=None, precision="
     if return_status:
         return Ws, status
     return Ws
+
+
+# ------------------------------------------------------------------------------ batched (uneven) build
+def ragged_stencils(adjl, k_per):
+    """Ragged adjacency (adj_ptr, adj_idx) keeping the k_per[e] nearest of each row of a
+    uniform neighbour list adjl (rows sorted by distance, as find_neighbors returns them)."""
+    torch = _torch()
+    a = adjl if _is_torch(adjl) else torch.from_numpy(np.ascontiguousarray(adjl, dtype=np.int32))
+    kp = k_per if _is_torch(k_per) else torch.as_tensor(np.asarray(k_per), dtype=torch.int64)
+    kp = kp.to(a.device, torch.int64)
+    if kp.numel() != a.shape[0] or int(kp.min()) < 1 or int(kp.max()) > a.shape[1]:
+        raise ValueError("k_per must hold one stencil size in 1..k per row of adjl")
+    keep = torch.arange(a.shape[1], device=a.device)[None, :] < kp[:, None]
+    adj_idx = a[keep].to(torch.int32).contiguous()
+    adj_ptr = torch.zeros(a.shape[0] + 1, dtype=torch.int64, device=a.device)
+    adj_ptr[1:] = torch.cumsum(kp, 0)
+    return adj_ptr, adj_idx
+
+
+def build_weights_batched(ops, data, eval_points, adj_ptr, adj_idx, basis, hermite=None, precision="fp64", *,
+                          poly_deg=None, tune=1, ctx=None, refine_steps=0, tol=0.0, return_status=False,
+                          stats=None, flags=0):
+    """Weights of `ops` on ragged stencils (the neighbours of eval point e are
+    adj_idx[adj_ptr[e]:adj_ptr[e+1]]), with an optional polynomial degree per stencil
+    (poly_deg, int8 array; basis.poly_deg otherwise), all in one persistent launch binned by
+    system size with autotuned tile shapes (tune: 0 cached/heuristic, 1 tune new classes,
+    2 re-tune).  Returns a list of WeightsCSR like build_weights."""
+    torch = _torch()
+    d = _points(data)
+    q = d if eval_points is None else _points(eval_points, "eval_points")
+    ns, dim = d.shape
+    ne = q.shape[0]
+    ctx = ctx or Context.default(_device_of(d, q, adj_idx))
+    dev = torch.device("cuda", ctx.device)
+
+    def arr(x, dtype_t, dtype_n):
+        if _is_torch(x):
+            return x.to(dtype_t).contiguous()
+        return np.ascontiguousarray(np.asarray(x, dtype=dtype_n))
+
+    ap = arr(adj_ptr, torch.int64, np.int64)
+    ai = arr(adj_idx, torch.int32, np.int32)
+    if ap.shape[0] != ne + 1:
+        raise DimensionMismatch("adj_ptr must have N_eval + 1 entries")
+    pd = None if poly_deg is None else arr(poly_deg, torch.int8, np.int8)
+    if pd is not None and pd.shape[0] != ne:
+        raise DimensionMismatch("poly_deg must have one entry per eval point")
+    cfg = _native.BuildCfg()
+    cfg.dim, cfg.phs, cfg.poly_deg, cfg.nops = dim, basis.order, basis.poly_deg, len(ops)
+    for i, (c, od) in enumerate(ops):
+        cfg.op_code[i] = c
+        cfg.op_dim[i] = od
+    cfg.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    cfg.refine_steps = refine_steps
+    cfg.tol = tol
+    cfg.flags = flags
+    herm = _hermite_arrays(hermite, ns, dim)
+    hs = None
+    if herm is not None:
+        isb, al, be, nr = herm
+        hs = _native.Hermite(isb.ctypes.data, al.ctypes.data, be.ctypes.data, nr.ctypes.data, len(al))
+    row_ptr = torch.empty(ne + 1, dtype=torch.int64, device=dev)
+    nnz = ctypes.c_int64(0)
+    ctx.check(ctx.lib.rbf_build_count_ragged(ctx.h, ns, ne, _ptr(ap), ctypes.byref(hs) if hs else None,
+                                             _ptr(row_ptr), ctypes.byref(nnz)))
+    col = torch.empty(nnz.value, dtype=torch.int32, device=dev)
+    val = torch.empty((len(ops), nnz.value), dtype=torch.float64, device=dev)
+    status = torch.empty(ne, dtype=torch.int8, device=dev) if return_status else None
+    st = _native.BuildStats() if stats is None else stats
+    ctx.check(ctx.lib.rbf_build_batched(ctx.h, ctypes.byref(cfg), _ptr(d), ns, _ptr(q), ne, _ptr(ap), _ptr(ai),
+                                        _ptr(pd), ctypes.byref(hs) if hs else None, _ptr(row_ptr), _ptr(col),
+                                        _ptr(val), _ptr(status), ctypes.byref(st), int(tune)))
+    Ws = [WeightsCSR(row_ptr, col, val[i], (ne, ns), ctx) for i in range(len(ops))]
+    if return_status:
+        return Ws, status
+    return Ws
+
+
+class BuildApplyGraph:
+    """Weight build on fixed stencils followed by y = W x, captured once in a CUDA graph
+    (rbf_plan_*).  data/eval_points/x are device tensors the graph reads in place: write new
+    coordinates or a new field into them, then call replay() -- one graph launch on torch's
+    current stream rebuilds the weights (into .weights) and applies them (into .y)."""
+
+    def __init__(self, op, data, eval_points, adjl, basis, x, precision="fp64", op_index=0, ctx=None,
+                 refine_steps=0, tol=0.0):
+        torch = _torch()
+        ops = [op] if isinstance(op, tuple) else list(op)
+        self.data = data
+        self.eval = data if eval_points is None else eval_points
+        for t, nm in ((data, "data"), (self.eval, "eval_points"), (x, "x")):
+            if not (_is_torch(t) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+                raise ValueError(f"{nm} must be a contiguous float64 CUDA tensor (the graph reads it in place)")
+        if not (_is_torch(adjl) and adjl.is_cuda and adjl.dtype == torch.int32 and adjl.is_contiguous()):
+            raise ValueError("adjl must be a contiguous int32 CUDA tensor")
+        ns, dim = data.shape
+        ne, k = adjl.shape
+        self.ctx = ctx or Context.default(data.device.index or 0)
+        dev = data.device
+        self.x = x
+        self.adjl = adjl
+        self.row_ptr = torch.empty(ne + 1, dtype=torch.int64, device=dev)
+        nnz = ctypes.c_int64(0)
+        self.ctx.check(self.ctx.lib.rbf_build_count(self.ctx.h, ns, ne, k, None, _ptr(self.row_ptr), ctypes.byref(nnz)))
+        self.col = torch.empty(nnz.value, dtype=torch.int32, device=dev)
+        self.val = torch.empty((len(ops), nnz.value), dtype=torch.float64, device=dev)
+        self.y = torch.empty(ne, dtype=torch.float64, device=dev)
+        cfg = _native.BuildCfg()
+        cfg.dim, cfg.phs, cfg.poly_deg, cfg.nops = dim, basis.order, basis.poly_deg, len(ops)
+        for i, (c, od) in enumerate(ops):
+            cfg.op_code[i] = c
+            cfg.op_dim[i] = od
+        cfg.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        cfg.refine_steps = refine_steps
+        cfg.tol = tol
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.rbf_plan_create(self.ctx.h, ctypes.byref(cfg), _ptr(data), ns, _ptr(self.eval), ne,
+                                                    _ptr(adjl), k, _ptr(self.row_ptr), _ptr(self.col), _ptr(self.val),
+                                                    op_index, _ptr(x), _ptr(self.y), ctypes.byref(h)))
+        self.plan = h
+        self.weights = [WeightsCSR(self.row_ptr, self.col, self.val[i], (ne, ns), self.ctx) for i in range(len(ops))]
+
+    def replay(self):
+        self.ctx.h  # bind the plan's context to torch's current stream
+        self.ctx.check(self.ctx.lib.rbf_plan_launch(self.plan))
+        return self.y
+
+    def counters(self):
+        s, f, r = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        self.ctx.check(self.ctx.lib.rbf_plan_counters(self.plan, ctypes.byref(s), ctypes.byref(f), ctypes.byref(r)))
+        return {"singular": s.value, "fallback": f.value, "residuals": r.value}
+
+    def __del__(self):
+        try:
+            if getattr(self, "plan", None):
+                self.ctx.lib.rbf_plan_destroy(self.plan)
+                self.plan = None
+        except Exception:
+            pass
+
+
+def tuning_report(ctx=None):
+    """The batched build's tuning table of a context: one line per size class."""
+    ctx = ctx or Context.default(0)
+    buf = ctypes.create_string_buffer(1 << 16)
+    ctx.check(ctx.lib.rbf_tuning_report(ctx.handle, buf, len(buf)))
+    return buf.value.decode()
 
 
 # ------------------------------------------------------------------------------ operator object

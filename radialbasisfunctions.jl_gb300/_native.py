@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
               "-Xptxas", "-warn-spills"]
 
 SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "stencil_build.cu", "stencil_refined_a.cu",
-           "stencil_refined_b.cu", "diag.cu", "mlp.cu"]
+           "stencil_refined_b.cu", "batched.cu", "plan.cu", "diag.cu", "mlp.cu"]
 
 
 def _nvcc():
@@ -120,6 +120,13 @@ SIGNATURES = {
     "rbf_ctx_kernel_launches": (_I64, [_P]),
     "rbf_mlp_gemm": (_I, [_P, _I32, _I32, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32]),
     "rbf_mlp_transpose": (_I, [_P, _I32, _I32, _P, _I32, _P, _I32]),
+    "rbf_build_count_ragged": (_I, [_P, _I64, _I64, _P, _P, _P, _P]),
+    "rbf_build_batched": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I32]),
+    "rbf_tuning_report": (_I, [_P, ctypes.c_char_p, _I64]),
+    "rbf_plan_create": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _I32, _P, _P, _P, _I32, _P, _P, _P]),
+    "rbf_plan_launch": (_I, [_P]),
+    "rbf_plan_counters": (_I, [_P, _P, _P, _P]),
+    "rbf_plan_destroy": (_I, [_P]),
     "rbf_mlp_features": (_I, [_P, _P, _I64, _P, _I32, _P, _I64, _I32, _P, _I32]),
     "rbf_mlp_to_bf16": (_I, [_P, _I32, _I32, _I32, _P, _I32, _P, _I32]),
     "rbf_mlp_mse": (_I, [_P, _I32, _I32, _P, _I32, _P, _I32, _P, _I32, _I32, _P]),

@@ -10,6 +10,12 @@
 
 int rbf_build_fp64_launch(rbf_ctx *ctx, const StencilParams &P);
 int rbf_build_fp32_launch(rbf_ctx *ctx, const StencilParams &P);
+int rbf_batched_classify(rbf_ctx *ctx, int64_t ne, int dim, const int64_t *d_adj_ptr, const int8_t *d_degs,
+                         int def_deg, int16_t *d_key, std::vector<unsigned long long> &hist, int *err);
+int rbf_batched_scatter(rbf_ctx *ctx, int64_t ne, const int16_t *d_key, const std::vector<int> &class_of_key,
+                        const std::vector<unsigned long long> &class_start, int32_t *d_slots);
+int rbf_batched_tune(rbf_ctx *ctx, std::vector<BinDesc> &bins, bool boundary, int tune);
+int rbf_batched_run(rbf_ctx *ctx, std::vector<BinDesc> &bins);
 
 int rbf_fail(rbf_ctx *ctx, int code, const char *fmt, ...) {
     char buf[1024];
@@ -131,6 +137,21 @@ int op_order(int code) {
     }
 }
 
+// Operator codes of a build configuration into P (op_code, op_dim, op_order).
+int set_operators(rbf_ctx *ctx, const rbf_build_cfg *cfg, StencilParams &P) {
+    const int dim = cfg->dim;
+    for (int r = 0; r < cfg->nops; r++) {
+        int c = cfg->op_code[r];
+        if (c < RBF_OP_IDENTITY || c > RBF_OP_LAPLACIAN) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "unknown operator code %d", c);
+        if ((c == RBF_OP_PARTIAL1 || c == RBF_OP_PARTIAL2) && (cfg->op_dim[r] < 0 || cfg->op_dim[r] >= dim))
+            return rbf_fail(ctx, RBF_ERR_ARGUMENT, "partial derivative dimension %d out of range", cfg->op_dim[r]);
+        P.op_code[r] = c;
+        P.op_dim[r] = (c == RBF_OP_PARTIAL1 || c == RBF_OP_PARTIAL2) ? cfg->op_dim[r] : 0;
+        P.op_order[r] = op_order(c);
+    }
+    return RBF_OK;
+}
+
 int check_ctx(rbf_ctx *ctx) {
     if (!ctx) return RBF_ERR_ARGUMENT;
     int cur = -1;
@@ -176,6 +197,29 @@ int bind_boundary(rbf_ctx *ctx, const rbf_hermite *h, int64_t ns, int dim, Bound
 }
 
 }  // namespace
+
+// Basis, operator and precision fields of P for a plan (P.k set by the caller).
+int rbf_plan_params(rbf_ctx *ctx, const rbf_build_cfg *cfg, StencilParams &P) {
+    const int dim = cfg->dim;
+    if (dim < 1 || dim > 3) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "dim must be 1, 2 or 3 (got %d)", dim);
+    if (!(cfg->phs == 1 || cfg->phs == 3 || cfg->phs == 5 || cfg->phs == 7))
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "n must be 1, 3, 5, or 7 (got n=%d)", cfg->phs);
+    if (cfg->poly_deg < -1) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "poly_deg must be >= -1 (got %d)", cfg->poly_deg);
+    if (cfg->nops < 1 || cfg->nops > RBF_MAX_OPS) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "nops must be in 1..%d", RBF_MAX_OPS);
+    RBF_TRY(set_operators(ctx, cfg, P));
+    P.nmon = monomial_exponents(dim, cfg->poly_deg, P.exps);
+    if (P.k + P.nmon > RBF_MAX_SYSTEM)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "k + number of monomials (%d) exceeds %d", P.k + P.nmon, RBF_MAX_SYSTEM);
+    P.dim = dim;
+    P.phs = cfg->phs;
+    P.poly_deg = cfg->poly_deg;
+    P.n = P.k + P.nmon;
+    P.nops = cfg->nops;
+    P.refine_steps = cfg->refine_steps > 0 ? cfg->refine_steps : 6;
+    P.tol = cfg->tol > 0 ? cfg->tol : 1e-9;
+    P.flags = cfg->flags;
+    return RBF_OK;
+}
 
 extern "C" {
 
@@ -279,15 +323,7 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
     P.nmon = monomial_exponents(dim, cfg->poly_deg, P.exps);
     if (k + P.nmon > RBF_MAX_SYSTEM)
         return rbf_fail(ctx, RBF_ERR_ARGUMENT, "k + number of monomials (%d) exceeds %d", k + P.nmon, RBF_MAX_SYSTEM);
-    for (int r = 0; r < cfg->nops; r++) {
-        int c = cfg->op_code[r];
-        if (c < RBF_OP_IDENTITY || c > RBF_OP_LAPLACIAN) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "unknown operator code %d", c);
-        if ((c == RBF_OP_PARTIAL1 || c == RBF_OP_PARTIAL2) && (cfg->op_dim[r] < 0 || cfg->op_dim[r] >= dim))
-            return rbf_fail(ctx, RBF_ERR_ARGUMENT, "partial derivative dimension %d out of range", cfg->op_dim[r]);
-        P.op_code[r] = c;
-        P.op_dim[r] = (c == RBF_OP_PARTIAL1 || c == RBF_OP_PARTIAL2) ? cfg->op_dim[r] : 0;
-        P.op_order[r] = op_order(c);
-    }
+    RBF_TRY(set_operators(ctx, cfg, P));
     if (herm && herm->is_boundary && ne > ns)
         return rbf_fail(ctx, RBF_ERR_DIMENSION, "Hermite builds evaluate at the data points (ne <= ns)");
     BoundaryDev b;
@@ -452,6 +488,211 @@ int rbf_csr_to_csc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr,
     RBF_TRY(ro.finish(ctx));
     RBF_TRY(vo.finish(ctx));
     RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
+int rbf_build_count_ragged(rbf_ctx *ctx, int64_t ns, int64_t ne, const int64_t *adj_ptr, const rbf_hermite *herm,
+                           int64_t *row_ptr_out, int64_t *nnz_out) {
+    RBF_TRY(check_ctx(ctx));
+    if (ne < 0 || ns < 1 || !adj_ptr) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid sizes or null adjacency");
+    if (herm && herm->is_boundary && ne > ns)
+        return rbf_fail(ctx, RBF_ERR_DIMENSION, "Hermite builds evaluate at the data points (ne <= ns)");
+    BoundaryDev b;
+    RBF_TRY(bind_boundary(ctx, herm, ns, 1, b));
+    InArray ap;
+    RBF_TRY(ap.bind(ctx, adj_ptr, sizeof(int64_t) * (ne + 1)));
+    OutArray rp;
+    RBF_TRY(rp.bind(ctx, row_ptr_out, sizeof(int64_t) * (ne + 1)));
+    int64_t nnz = 0;
+    RBF_TRY(rbf_count_rows_device(ctx, ne, 0, b.any ? b.isb.as<uint8_t>() : nullptr, b.any ? b.g2b.as<int32_t>() : nullptr,
+                                  b.any ? b.alpha.as<double>() : nullptr, b.any ? b.beta.as<double>() : nullptr,
+                                  rp.as<int64_t>(), &nnz, ap.as<int64_t>()));
+    RBF_TRY(rp.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (nnz_out) *nnz_out = nnz;
+    return RBF_OK;
+}
+
+int rbf_build_batched(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns, const double *eval,
+                      int64_t ne, const int64_t *adj_ptr, const int32_t *adj_idx, const int8_t *poly_deg_per,
+                      const rbf_hermite *herm, const int64_t *row_ptr, int32_t *col, double *val, int8_t *status_out,
+                      rbf_build_stats *stats, int32_t tune) {
+    RBF_TRY(check_ctx(ctx));
+    if (!cfg || !adj_ptr) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null configuration or adjacency");
+    const int dim = cfg->dim;
+    if (dim < 1 || dim > 3) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "dim must be 1, 2 or 3 (got %d)", dim);
+    if (!(cfg->phs == 1 || cfg->phs == 3 || cfg->phs == 5 || cfg->phs == 7))
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "n must be 1, 3, 5, or 7 (got n=%d)", cfg->phs);
+    if (cfg->poly_deg < -1)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "poly_deg must be >= -1 (got %d)", cfg->poly_deg);
+    if (cfg->nops < 1 || cfg->nops > RBF_MAX_OPS) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "nops must be in 1..%d", RBF_MAX_OPS);
+    if (cfg->precision != RBF_PREC_FP64 && cfg->precision != RBF_PREC_FP32_REFINED)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "batched builds are plain FP64 or FP32-refined");
+    if (ns < 1 || ns >= INT32_MAX || ne >= INT32_MAX || ne < 0) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "point counts must be < 2^31");
+    if (tune < 0 || tune > 2) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "tune must be 0, 1 or 2");
+    StencilParams P;
+    memset(&P, 0, sizeof P);
+    RBF_TRY(set_operators(ctx, cfg, P));
+    if (herm && herm->is_boundary && ne > ns)
+        return rbf_fail(ctx, RBF_ERR_DIMENSION, "Hermite builds evaluate at the data points (ne <= ns)");
+    BoundaryDev b;
+    RBF_TRY(bind_boundary(ctx, herm, ns, dim, b));
+    if (b.any_nr)
+        for (int r = 0; r < cfg->nops; r++)
+            if (P.op_code[r] == RBF_OP_IDENTITY)  // _check_normal_form_support, src/solve/api.jl:79-94
+                return rbf_fail(ctx, RBF_ERR_UNSUPPORTED,
+                                "Neumann/Robin boundary conditions require the operator's basis action to support "
+                                "the normal-derivative form; the identity (regrid) has none");
+    InArray d, q, ap, ai, dg, rp;
+    RBF_TRY(d.bind(ctx, data, sizeof(double) * ns * dim));
+    RBF_TRY(q.bind(ctx, eval, sizeof(double) * ne * dim));
+    RBF_TRY(ap.bind(ctx, adj_ptr, sizeof(int64_t) * (ne + 1)));
+    int64_t ends[2] = {0, 0};
+    RBF_CUDA(ctx, cudaMemcpyAsync(&ends[0], ap.as<int64_t>(), sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaMemcpyAsync(&ends[1], ap.as<int64_t>() + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ends[0] != 0 || ends[1] < 0 || ends[1] > (int64_t)RBF_MAX_STENCIL * ne)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "adj_ptr must start at 0 and hold at most %d neighbours per stencil",
+                        RBF_MAX_STENCIL);
+    RBF_TRY(ai.bind(ctx, adj_idx, sizeof(int32_t) * ends[1]));
+    if (poly_deg_per) RBF_TRY(dg.bind(ctx, poly_deg_per, (size_t)ne));
+    RBF_TRY(rp.bind(ctx, row_ptr, sizeof(int64_t) * (ne + 1)));
+    bool idx_ok = true;
+    RBF_TRY(rbf_check_indices(ctx, ai.as<int32_t>(), ends[1], (int32_t)ns, &idx_ok));
+    if (!idx_ok) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "adj_idx holds indices outside [0, %lld)", (long long)ns);
+    // size classes
+    DevBuf keys;
+    RBF_TRY(keys.alloc(ctx, sizeof(int16_t) * (size_t)std::max<int64_t>(ne, 1)));
+    std::vector<unsigned long long> hist;
+    int err = 0;
+    RBF_TRY(rbf_batched_classify(ctx, ne, dim, ap.as<int64_t>(), poly_deg_per ? dg.as<int8_t>() : nullptr,
+                                 cfg->poly_deg, keys.as<int16_t>(), hist, &err));
+    if (err & 8) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "adj_ptr must be non-decreasing");
+    if (err & 1) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "stencil sizes must be in 1..%d", RBF_MAX_STENCIL);
+    if (err & 4) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "polynomial degrees must be in -1..6");
+    if (err & 2)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "a stencil's k + number of monomials exceeds %d", RBF_MAX_SYSTEM);
+    int64_t nnz = 0;
+    RBF_CUDA(ctx, cudaMemcpyAsync(&nnz, rp.as<int64_t>() + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (nnz < 0 || nnz > ends[1]) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "row_ptr is not the layout of this build");
+    OutArray oc, ov, os;
+    RBF_TRY(oc.bind(ctx, col, sizeof(int32_t) * nnz));
+    RBF_TRY(ov.bind(ctx, val, sizeof(double) * nnz * cfg->nops));
+    RBF_TRY(os.bind(ctx, status_out, (size_t)ne));
+    DevBuf counters;
+    RBF_TRY(counters.alloc(ctx, sizeof(unsigned long long) * 8 + sizeof(double)));
+    RBF_CUDA(ctx, cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long) * 8 + sizeof(double), ctx->stream));
+    P.dim = dim;
+    P.phs = cfg->phs;
+    P.nops = cfg->nops;
+    P.ne = ne;
+    P.ns = ns;
+    P.nnz = nnz;
+    P.data = d.as<double>();
+    P.eval = q.as<double>();
+    P.adjl = ai.as<int32_t>();
+    P.adj_ptr = ap.as<int64_t>();
+    P.isb = b.any ? b.isb.as<uint8_t>() : nullptr;
+    P.g2b = b.any ? b.g2b.as<int32_t>() : nullptr;
+    P.alpha = b.any ? b.alpha.as<double>() : nullptr;
+    P.beta = b.any ? b.beta.as<double>() : nullptr;
+    P.normals = b.any ? b.normals.as<double>() : nullptr;
+    P.row_ptr = rp.as<int64_t>();
+    P.col = oc.as<int32_t>();
+    P.val = ov.as<double>();
+    P.status = os.as<int8_t>();
+    P.counters = counters.as<unsigned long long>();
+    P.max_resid = reinterpret_cast<double *>(counters.as<unsigned long long>() + 8);
+    P.refine_steps = cfg->refine_steps > 0 ? cfg->refine_steps : 6;
+    P.tol = cfg->tol > 0 ? cfg->tol : 1e-9;
+    P.flags = cfg->flags;
+    P.seed = nullptr;
+    // one descriptor per size class, largest system first
+    std::vector<BinDesc> bins;
+    for (int key = 0; key < kRbfBatchKeys; key++) {
+        if (!hist[key]) continue;
+        BinDesc B;
+        memset(&B, 0, sizeof B);
+        B.P = P;
+        B.P.k = key / 8;
+        B.P.poly_deg = key % 8 - 1;
+        B.P.nmon = monomial_exponents(dim, B.P.poly_deg, B.P.exps);
+        B.P.n = B.P.k + B.P.nmon;
+        B.count = (int64_t)hist[key];
+        B.precision = cfg->precision;
+        bins.push_back(B);
+    }
+    std::stable_sort(bins.begin(), bins.end(), [](const BinDesc &a, const BinDesc &c) { return a.P.n > c.P.n; });
+    std::vector<int> class_of_key(kRbfBatchKeys, -1);
+    std::vector<unsigned long long> class_start(bins.size() + 1, 0ull);
+    for (size_t c = 0; c < bins.size(); c++) {
+        class_of_key[bins[c].P.k * 8 + bins[c].P.poly_deg + 1] = (int)c;
+        class_start[c + 1] = class_start[c] + (unsigned long long)bins[c].count;
+    }
+    DevBuf slots;
+    RBF_TRY(slots.alloc(ctx, sizeof(int32_t) * (size_t)std::max<int64_t>(ne, 1)));
+    RBF_TRY(rbf_batched_scatter(ctx, ne, keys.as<int16_t>(), class_of_key, class_start, slots.as<int32_t>()));
+    for (size_t c = 0; c < bins.size(); c++) bins[c].slots = slots.as<int32_t>() + class_start[c];
+    RBF_TRY(rbf_batched_tune(ctx, bins, b.any, tune));
+    cudaEvent_t ev0, ev1;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    cudaEventRecord(ev0, ctx->stream);
+    const int st = rbf_batched_run(ctx, bins);
+    cudaEventRecord(ev1, ctx->stream);
+    if (st != RBF_OK) {
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+        return st;
+    }
+    unsigned long long hc[8];
+    double hres = 0.0;
+    RBF_CUDA(ctx, cudaMemcpyAsync(hc, counters.ptr, sizeof hc, cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaMemcpyAsync(&hres, P.max_resid, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_TRY(oc.finish(ctx));
+    RBF_TRY(ov.finish(ctx));
+    RBF_TRY(os.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    if (stats) {
+        stats->n_identity_rows = (int64_t)hc[3];
+        stats->n_stencils = ne - (int64_t)hc[3];
+        stats->n_singular = (int64_t)hc[0];
+        stats->n_fallback = (int64_t)hc[2];
+        stats->max_residual = hres;
+        stats->ms_build = ms;
+        stats->ms_knn = 0.f;
+        stats->ms_total = ms;
+        stats->n_residuals = (int64_t)hc[4];
+        stats->seed_rel_err_mean = 0.0;
+    }
+    if (hc[1]) return rbf_fail(ctx, RBF_ERR_NOT_FOUND, "evaluation point not found in stencil data (%llu stencils)", hc[1]);
+    if (hc[0]) return rbf_fail(ctx, RBF_ERR_SINGULAR, "%llu stencil system(s) are singular", hc[0]);
+    return RBF_OK;
+}
+
+int rbf_tuning_report(rbf_ctx *ctx, char *buf, int64_t len) {
+    if (!ctx || !buf || len < 1) return RBF_ERR_ARGUMENT;
+    std::string out;
+    char line[256];
+    for (const auto &kv : ctx->tune) {
+        const unsigned long long k = kv.first;
+        const rbf_tune_entry &t = kv.second;
+        snprintf(line, sizeof line,
+                 "precision=%s dim=%llu phs=%llu nops=%llu k=%llu degree=%lld boundary=%llu op=%llu: tile=%s "
+                 "(warp %.3f ms, block %.3f ms, sample %lld)\n",
+                 (k & 15) == RBF_PREC_FP64 ? "fp64" : "fp32_refined", (k >> 4) & 15, (k >> 8) & 15, (k >> 12) & 15,
+                 (k >> 16) & 255, (long long)((k >> 24) & 15) - 1, (k >> 28) & 1, (k >> 32) & 15,
+                 t.tile ? "block" : "warp", t.ms_warp, t.ms_block, t.sample);
+        out += line;
+    }
+    const size_t m = std::min<size_t>(out.size(), (size_t)len - 1);
+    memcpy(buf, out.data(), m);
+    buf[m] = 0;
     return RBF_OK;
 }
 

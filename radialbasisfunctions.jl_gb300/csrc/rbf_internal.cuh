@@ -5,9 +5,20 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <string>
 
 #include "rbffd.h"
+
+// Size-class keys of the batched build: k * 8 + (polynomial degree + 1), k <= 64.
+constexpr int kRbfBatchKeys = 65 * 8;
+
+// One tuned size class of the batched build: the tile shape chosen and the trial timings.
+struct rbf_tune_entry {
+    int tile = 0;  // 0: one warp per stencil, 1: the whole block on one stencil
+    float ms_warp = 0.f, ms_block = 0.f;
+    long long sample = 0;
+};
 
 struct rbf_ctx {
     int device = 0;
@@ -17,6 +28,7 @@ struct rbf_ctx {
     std::string last_error;
     long long launches = 0;      // kernels launched through this context
     long long knn_fallback = 0;  // queries re-run by the exact FP64 neighbour search
+    std::map<unsigned long long, rbf_tune_entry> tune;  // batched build: size class -> tile
 };
 
 int rbf_fail(rbf_ctx *ctx, int code, const char *fmt, ...);
@@ -98,7 +110,7 @@ struct StencilParams;  // stencil.cuh
 
 int rbf_count_rows_device(rbf_ctx *ctx, int64_t ne, int k, const uint8_t *d_isb,
                           const int32_t *d_g2b, const double *d_alpha, const double *d_beta,
-                          int64_t *d_row_ptr, int64_t *nnz);
+                          int64_t *d_row_ptr, int64_t *nnz, const int64_t *d_adj_ptr = nullptr);
 
 int rbf_boundary_map_device(rbf_ctx *ctx, int64_t n, const uint8_t *d_isb, int32_t *d_g2b,
                             int64_t *n_boundary);

@@ -111,10 +111,11 @@ int exclusive_scan(rbf_ctx *ctx, const T *d_in, T *d_out, int64_t n, T *d_total_
 // every other row holds k (src/solve/execution.jl:39-69).
 __global__ void row_counts_kernel(int64_t ne, int k, const uint8_t *__restrict__ isb,
                                   const int32_t *__restrict__ g2b, const double *__restrict__ alpha,
-                                  const double *__restrict__ beta, int64_t *__restrict__ cnt) {
+                                  const double *__restrict__ beta, int64_t *__restrict__ cnt,
+                                  const int64_t *__restrict__ adj_ptr) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne;
          e += (int64_t)gridDim.x * blockDim.x) {
-        int64_t c = k;
+        int64_t c = adj_ptr ? adj_ptr[e + 1] - adj_ptr[e] : k;
         if (isb && isb[e]) {
             int32_t b = g2b[e];
             if (alpha[b] == 1.0 && beta[b] == 0.0) c = 1;
@@ -182,12 +183,14 @@ int rbf_boundary_map_device(rbf_ctx *ctx, int64_t n, const uint8_t *d_isb, int32
 }
 
 int rbf_count_rows_device(rbf_ctx *ctx, int64_t ne, int k, const uint8_t *d_isb, const int32_t *d_g2b,
-                          const double *d_alpha, const double *d_beta, int64_t *d_row_ptr, int64_t *nnz) {
+                          const double *d_alpha, const double *d_beta, int64_t *d_row_ptr, int64_t *nnz,
+                          const int64_t *d_adj_ptr) {
     DevBuf cnt;
     RBF_TRY(cnt.alloc(ctx, sizeof(int64_t) * (ne + 1)));
     int blocks = (int)std::min<int64_t>((ne + 255) / 256, (int64_t)ctx->num_sms * 8);
     if (blocks < 1) blocks = 1;
-    row_counts_kernel<<<blocks, 256, 0, ctx->stream>>>(ne, k, d_isb, d_g2b, d_alpha, d_beta, cnt.as<int64_t>());
+    row_counts_kernel<<<blocks, 256, 0, ctx->stream>>>(ne, k, d_isb, d_g2b, d_alpha, d_beta, cnt.as<int64_t>(),
+                                                     d_adj_ptr);
     RBF_CHECK_LAUNCH(ctx);
     RBF_CUDA(ctx, cudaMemsetAsync(cnt.as<int64_t>() + ne, 0, sizeof(int64_t), ctx->stream));
     // scan over ne+1 entries so that row_ptr[ne] is the total

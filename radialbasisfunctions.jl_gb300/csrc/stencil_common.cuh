@@ -51,6 +51,17 @@ struct StencilParams {
     double tol;
     int flags;          // RBF_FLAG_*
     const float *seed;  // learned seed (ne x k, stencil order, local units) or nullptr
+    const int64_t *adj_ptr;  // ragged adjacency: neighbours of e at adjl[adj_ptr[e] ..], or nullptr
+};
+
+// One size class (stencil size k, polynomial degree) of a batched build of uneven stencils.
+struct BinDesc {
+    StencilParams P;        // k, n, nmon and monomial exponents of the class; shared arrays
+    const int32_t *slots;   // the class's stencils (eval point indices), count entries
+    int64_t count;
+    int64_t item_start;     // first work item of the class in the persistent kernel's queue
+    int tile;               // 0: one warp per stencil (4 per block), 1: the block on one stencil
+    int precision;          // RBF_PREC_FP64 or RBF_PREC_FP32_REFINED
 };
 
 template <class T> __device__ __forceinline__ T rbf_sqrt(T x);

@@ -48,8 +48,9 @@ __device__ int load_stencil(const StencilParams &P, int64_t e, const WarpSmem &w
     for (int d = 0; d < dim; d++) x0[d] = P.eval[e * dim + d];
     double r2max = 0.0;
     bool anyb = false;
+    const int32_t *nbr = P.adj_ptr ? P.adjl + P.adj_ptr[e] : P.adjl + e * k;
     for (int i = lane; i < k; i += 32) {
-        int g = P.adjl[e * k + i];
+        int g = nbr[i];
         w.cols[i] = g;
         double r2 = 0.0;
         for (int d = 0; d < dim; d++) {
@@ -370,8 +371,9 @@ __device__ __forceinline__ double df_to_double(dfl a) { return widen(a.hi) + wid
 // Interior stencils: Phi and P in double-float.  M gets the FP64 system (hi + lo, for the
 // residual and the fallback), F the FP32 factor matrix (hi).  Right-hand sides in FP64.
 // Hermite stencils (a small minority) take the FP64 assembly and are rounded to F.
+// pairs (optional): the upper-triangle pairs (i <= j) in order, packed as i | j << 8.
 __device__ void assemble_refined(const StencilParams &P, const WarpSmem &w, const Warp32 &u, int lane, int es,
-                                 int eval_local) {
+                                 int eval_local, const uint16_t *pairs = nullptr) {
     // u.F == nullptr: only the FP64 system is needed (the register kernels narrow it)
     const int k = P.k, n = P.n, nops = P.nops, ld = mat_ld(n, nops), fld = f32_ld(n), dim = P.dim, nmon = P.nmon;
     if (eval_local != -2) {  // Hermite stencil
@@ -398,10 +400,17 @@ __device__ void assemble_refined(const StencilParams &P, const WarpSmem &w, cons
     __syncwarp();
     const int npairs = k * (k + 1) / 2;
     for (int p = lane; p < npairs; p += 32) {
-        int j = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
-        while (j * (j + 1) / 2 > p) j--;
-        while ((j + 1) * (j + 2) / 2 <= p) j++;
-        const int i = p - j * (j + 1) / 2;
+        int i, j;
+        if (pairs) {
+            const unsigned pk = pairs[p];
+            i = (int)(pk & 0xffu);
+            j = (int)(pk >> 8);
+        } else {
+            j = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+            while (j * (j + 1) / 2 > p) j--;
+            while ((j + 1) * (j + 2) / 2 <= p) j++;
+            i = p - j * (j + 1) / 2;
+        }
         dfl r2 = {0.0f, 0.0f};
         for (int d = 0; d < dim; d++) {
             dfl dd = ts(u.XH[i * 3 + d], -u.XH[j * 3 + d]);
@@ -503,6 +512,144 @@ __device__ bool lu_factor_fp32(float *F, int *piv, int n, int lane) {
             }
         }
         __syncwarp();
+    }
+    return true;
+}
+
+// ---- block-cooperative factorisations (block-per-stencil tiles of the batched build) ----
+// The whole thread block (G threads, G a multiple of 32, every thread calling) factorises
+// one system in shared memory.  Each matrix entry receives the same FMA sequence and the
+// pivot is the same (largest magnitude, lowest row on ties) as in the one-warp versions
+// above, so the results are bit-identical to them.  redv/redi: G/32 scratch slots.
+template <class T>
+__device__ __forceinline__ void block_argmax(T &bv, int &br, T *redv, int *redi, int tid, int G) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const T ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int orr = __shfl_xor_sync(0xffffffffu, br, o);
+        if (ov > bv || (ov == bv && orr < br)) {
+            bv = ov;
+            br = orr;
+        }
+    }
+    if ((tid & 31) == 0) {
+        redv[tid >> 5] = bv;
+        redi[tid >> 5] = br;
+    }
+    __syncthreads();
+    bv = redv[0];
+    br = redi[0];
+    for (int w = 1; w < G / 32; w++)
+        if (redv[w] > bv || (redv[w] == bv && redi[w] < br)) {
+            bv = redv[w];
+            br = redi[w];
+        }
+}
+
+__device__ bool lu_solve_fp64_block(double *M, int n, int nops, int tid, int G, double *redv, int *redi) {
+    const int ld = mat_ld(n, nops), W = n + nops;
+    for (int c = 0; c < n; c++) {
+        double bv = -1.0;
+        int br = n;
+        for (int r = c + tid; r < n; r += G) {
+            const double v = fabs(M[r * ld + c]);
+            if (v > bv) {
+                bv = v;
+                br = r;
+            }
+        }
+        block_argmax(bv, br, redv, redi, tid, G);
+        if (!(bv > 0.0) || !isfinite(bv)) {
+            __syncthreads();
+            return false;
+        }
+        if (br != c)
+            for (int cc = c + tid; cc < W; cc += G) {
+                const double a = M[c * ld + cc];
+                M[c * ld + cc] = M[br * ld + cc];
+                M[br * ld + cc] = a;
+            }
+        __syncthreads();
+        const double inv = 1.0 / M[c * ld + c];
+        for (int r = c + 1 + tid; r < n; r += G) M[r * ld + c] *= inv;
+        __syncthreads();
+        const int rows = n - c - 1, cols = W - c - 1;
+        if (rows > 0) {
+            const int total = rows * cols;
+            int r = tid / cols, cc = tid % cols;
+            const int dr = G / cols, dc = G % cols;
+            const double *prow = M + c * ld + c + 1;
+            for (int t = tid; t < total; t += G) {
+                double *row = M + (c + 1 + r) * ld;
+                row[c + 1 + cc] = fma(-row[c], prow[cc], row[c + 1 + cc]);
+                r += dr;
+                cc += dc;
+                if (cc >= cols) {
+                    cc -= cols;
+                    r++;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    for (int c = n - 1; c >= 0; c--) {
+        if (tid < nops) M[c * ld + n + tid] = M[c * ld + n + tid] / M[c * ld + c];
+        __syncthreads();
+        const int total = c * nops;
+        for (int t = tid; t < total; t += G) {
+            const int r = t / nops, q = t - (t / nops) * nops;
+            M[r * ld + n + q] = fma(-M[r * ld + c], M[c * ld + n + q], M[r * ld + n + q]);
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+__device__ bool lu_factor_fp32_block(float *F, int *piv, int n, int tid, int G, float *redv, int *redi) {
+    const int ld = f32_ld(n);
+    for (int c = 0; c < n; c++) {
+        float bv = -1.0f;
+        int br = n;
+        for (int r = c + tid; r < n; r += G) {
+            const float v = fabsf(F[r * ld + c]);
+            if (v > bv) {
+                bv = v;
+                br = r;
+            }
+        }
+        block_argmax(bv, br, redv, redi, tid, G);
+        if (!(bv > 0.0f) || !isfinite(bv)) {
+            __syncthreads();
+            return false;
+        }
+        if (tid == 0) piv[c] = br;
+        if (br != c)
+            for (int cc = tid; cc < n; cc += G) {
+                const float a = F[c * ld + cc];
+                F[c * ld + cc] = F[br * ld + cc];
+                F[br * ld + cc] = a;
+            }
+        __syncthreads();
+        const float inv = 1.0f / F[c * ld + c];
+        for (int r = c + 1 + tid; r < n; r += G) F[r * ld + c] *= inv;
+        __syncthreads();
+        const int rows = n - c - 1, cols = n - c - 1;
+        if (rows > 0) {
+            const int total = rows * cols;
+            int r = tid / cols, cc = tid % cols;
+            const int dr = G / cols, dc = G % cols;
+            const float *prow = F + c * ld + c + 1;
+            for (int t = tid; t < total; t += G) {
+                float *row = F + (c + 1 + r) * ld;
+                row[c + 1 + cc] = fmaf(-row[c], prow[cc], row[c + 1 + cc]);
+                r += dr;
+                cc += dc;
+                if (cc >= cols) {
+                    cc -= cols;
+                    r++;
+                }
+            }
+        }
+        __syncthreads();
     }
     return true;
 }

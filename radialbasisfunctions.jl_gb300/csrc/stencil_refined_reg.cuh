@@ -113,11 +113,10 @@ __device__ bool reglu_factor(RegLU<N, R> &L, float *rowbuf, int *piv, float *rcp
         // replaced by 63 - row, so one max-reduction also breaks near-ties to the lower row)
         unsigned key = 0u;
 #pragma unroll
-        for (int s = 0; s < ROWS; s++)
-            if (L.step[s] == N + 1) {
-                const unsigned kk = (__float_as_uint(fabsf(L.a[s][c])) & ~63u) | (unsigned)(63 - (lane + 32 * s));
-                key = max(key, kk);
-            }
+        for (int s = 0; s < ROWS; s++) {
+            const unsigned kk = (__float_as_uint(fabsf(L.a[s][c])) & ~63u) | (unsigned)(63 - (lane + 32 * s));
+            key = max(key, L.step[s] == N + 1 ? kk : 0u);
+        }
         key = __reduce_max_sync(0xffffffffu, key);
         const int brow = 63 - (int)(key & 63u);
         const int pl = brow & 31, ps = brow >> 5;
@@ -138,29 +137,34 @@ __device__ bool reglu_factor(RegLU<N, R> &L, float *rowbuf, int *piv, float *rcp
         __syncwarp();
         const float pvt = rowbuf[c];
         ok &= (pvt != 0.0f) && isfinite(pvt);
-        const float inv = 1.0f / pvt;
+        // correctly rounded reciprocal without the division's slow path (a zero or
+        // non-finite pivot has already failed the factorisation)
+        const float inv = __frcp_rn(pvt);
         if (lane == 0) {
             piv[c] = brow;
             rcp[c] = inv;
         }
+        // elimination; up to 40 rows it is branch-free: rows already used as pivots (and
+        // padding rows) get a zero multiplier, which leaves them unchanged (larger systems
+        // keep the branch, which needs fewer live registers)
 #pragma unroll
-        for (int s = 0; s < ROWS; s++)
-            if (L.step[s] == N + 1) {
-                const float l = L.a[s][c] * inv;
-                L.a[s][c] = l;
+        for (int s = 0; s < ROWS; s++) {
+            const bool act = L.step[s] == N + 1;
+            if constexpr (N > 40)
+                if (!act) continue;
+            const float l = act ? L.a[s][c] * inv : 0.0f;
+            L.a[s][c] = act ? l : L.a[s][c];
 #pragma unroll
-                for (int q4 = (c + 1) / 4; q4 < (W + 3) / 4; q4++) {
-                    const float4 v = reinterpret_cast<const float4 *>(rowbuf)[q4];
-                    const float vv[4] = {v.x, v.y, v.z, v.w};
+            for (int q4 = (c + 1) / 4; q4 < (W + 3) / 4; q4++) {
+                const float4 v = reinterpret_cast<const float4 *>(rowbuf)[q4];
+                const float vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-                    for (int t = 0; t < 4; t++) {
-                        constexpr int dummy = 0;
-                        (void)dummy;
-                        const int cc = 4 * q4 + t;
-                        if (cc > c && cc < W) L.a[s][cc < W ? cc : 0] = fmaf(-l, vv[t], L.a[s][cc < W ? cc : 0]);
-                    }
+                for (int t = 0; t < 4; t++) {
+                    const int cc = 4 * q4 + t;
+                    if (cc > c && cc < W) L.a[s][cc < W ? cc : 0] = fmaf(-l, vv[t], L.a[s][cc < W ? cc : 0]);
                 }
             }
+        }
         __syncwarp();
     });
     return ok;
@@ -239,6 +243,14 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
     const int ld = mat_ld(N, R);
     float *rowbuf = rs.rowbuf;
     float *xs = u.v;  // N x R floats
+    // upper-triangle pair table of the RBF block, shared by the block's warps
+    uint16_t *pairs = reinterpret_cast<uint16_t *>(smem + wpb * warp_bytes);
+    for (int p = threadIdx.x; p < P.k * (P.k + 1) / 2; p += blockDim.x) {
+        int j = 0;
+        while ((j + 1) * (j + 2) / 2 <= p) j++;
+        pairs[p] = (uint16_t)((p - j * (j + 1) / 2) | (j << 8));
+    }
+    __syncthreads();
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
     for (int64_t e = (int64_t)blockIdx.x * wpb + wib; e < P.ne; e += nwarps) {
         int es = 0, eval_local = -2;
@@ -247,7 +259,7 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
             __syncwarp();
             continue;
         }
-        assemble_refined(P, w, u, lane, es, eval_local);
+        assemble_refined(P, w, u, lane, es, eval_local, pairs);
         float *rcp = rs.rcp;
         RegLU<N, R> L;
 #pragma unroll
@@ -423,7 +435,7 @@ template <int N, int R>
 int launch_refined_reg(rbf_ctx *ctx, const StencilParams &P) {
     const size_t wb = reg_smem_bytes(P.n, P.k, P.nops);
     const int wpb = 4;
-    const size_t smem = wb * wpb;
+    const size_t smem = wb * wpb + sizeof(uint16_t) * (size_t)(P.k * (P.k + 1) / 2);
     RBF_CUDA(ctx, cudaFuncSetAttribute(build_refined_reg_kernel<N, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
     int per_sm = 0;
