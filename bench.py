@@ -361,8 +361,24 @@ def main():
                "bf16_peak_tflops": peaks_bf16(), "frac_of_bf16_peak": tf / peaks_bf16(),
                "kernel": "gemm_bf16_kernel (mma.sync m16n8k16, 64x64 tiles)"}
         del feats
+    def kernel_ms(fn, reps=10):
+        """Median device time of the library work inside fn (CUDA events recorded by the
+        library around its kernels, rbf_ctx_set_timing)."""
+        ctx.lib.rbf_ctx_set_timing(ctx.h, 1)
+        fn()
+        vals = []
+        for _ in range(reps):
+            fn()
+            v = pkg.ctypes.c_float(0.0)
+            ctx.lib.rbf_ctx_last_ms(ctx.h, pkg.ctypes.byref(v))
+            vals.append(v.value)
+        ctx.lib.rbf_ctx_set_timing(ctx.h, 0)
+        return statistics.median(vals)
+
     W = build(headline, Xd, adjl)[-1]
-    ms_spmv = timed(lambda: W.apply(fd), 10, 3)
+    ms_spmv_api = timed(lambda: W.apply(fd), 10, 3)
+    ms_spmv = kernel_ms(lambda: W.apply(fd))
+    ms_knn_kernel = kernel_ms(lambda: pkg.find_neighbors(Xd, k=k, ctx=ctx), 3)
     nnz = W.nnz
     # algorithmic bytes of one apply: val (8 B) + col (4 B) per entry, row_ptr (8 B) per row,
     # the field read once and the result written once
@@ -389,6 +405,21 @@ def main():
             "peak_source": "FP64 FMA loop measured in this run (rbf_diag_fma_peak)",
             "fp32_pipe": {"peak": fp32_peak.value, "frac": ach / fp32_peak.value},
             "traffic_source": "ncu dram__bytes_read+write of the same kernel at N=1M, scaled by stencils"}
+
+    # ---- the same workload after reorder_points (Morton order, the reference's locality
+    # utility applied once): the apply's gathers become local
+    perm, Xo = pkg.reorder_points(Xd, k, ctx=ctx)
+    fo = fd[perm.long()].contiguous()
+    adj_o = pkg.find_neighbors(Xo, k=k, ctx=ctx)
+    Wo = build(headline, Xo, adj_o)[-1]
+    ms_spmv_o = kernel_ms(lambda: Wo.apply(fo))
+    gbs_o = apply_bytes / (ms_spmv_o * 1e-3) / 1e9
+    ms_step_o = timed(lambda: step(headline, Xo, fo), max(1, args.steps // 2), 1)
+    ms_reorder = timed(lambda: pkg.reorder_points(Xd, k, ctx=ctx), 3, 1)
+    reordered = {"ms_reorder_points": ms_reorder, "ms_per_step": ms_step_o,
+                 "stencils_per_s": n * world / (ms_step_o * 1e-3),
+                 "apply": {"value": gbs_o, "unit": "GB/s", "ms": ms_spmv_o, "frac_of_hbm": gbs_o / hbm_peak}}
+    del Wo, adj_o, Xo, fo
 
     # ---- e2e through the public API: host points in, host Laplacian of a host field out
     X_pin = torch.from_numpy(X_h).pin_memory()
@@ -443,10 +474,12 @@ def main():
                            "fallback_unseeded": int(st32.n_fallback),
                            "seed_rel_err_mean_judged_by_solve": float(st_h.seed_rel_err_mean) if learned_on else None},
             "surrogate": training, "mlp": mlp,
-            "apply": {"value": apply_gbs, "unit": "GB/s", "ms": ms_spmv, "nnz": nnz,
-                      "frac_of_hbm": apply_gbs / hbm_peak, "peak_source": hbm_src},
-            "kernels_ms": {"knn": ms_knn, "build_headline": ms_kernel, "build_fp64": float(st64.ms_build),
-                           "spmv": ms_spmv},
+            "apply": {"value": apply_gbs, "unit": "GB/s", "ms": ms_spmv, "ms_per_call_api": ms_spmv_api,
+                      "nnz": nnz, "frac_of_hbm": apply_gbs / hbm_peak, "peak_source": hbm_src,
+                      "bytes": "nnz*12 + (ne+1)*8 + 2*n*8 per apply; ms = kernel time (library CUDA events)"},
+            "reordered": reordered,
+            "kernels_ms": {"knn": ms_knn_kernel, "knn_per_call_api": ms_knn, "build_headline": ms_kernel,
+                           "build_fp64": float(st64.ms_build), "spmv": ms_spmv},
             "peaks": {"fp64_tflops_measured": fp64_peak.value, "fp32_tflops_measured": fp32_peak.value,
                       "hbm_gbs": hbm_peak},
             "roofline": roof,

@@ -123,6 +123,10 @@ int rbf_ctx_destroy(rbf_ctx *ctx);
  * allocated and freed in stream order on another stream (a caching allocator) must
  * bind that stream here: the library does not order its work against other streams. */
 int rbf_ctx_set_stream(rbf_ctx *ctx, void *cuda_stream);
+/* Benchmark hook: with timing on, rbf_knn and rbf_spmm record CUDA events around their
+ * device work (staging copies excluded) and rbf_ctx_last_ms returns its duration. */
+int rbf_ctx_set_timing(rbf_ctx *ctx, int32_t on);
+int rbf_ctx_last_ms(rbf_ctx *ctx, float *ms);
 const char *rbf_last_error(const rbf_ctx *ctx);
 const char *rbf_version(void);
 
@@ -199,6 +203,15 @@ int rbf_mlp_colsum(rbf_ctx *ctx, int32_t rows, int32_t cols, const void *in, int
 /* Adam step (t = step >= 1) on FP32 parameters; p_bf16 (optional) receives their bf16 copy */
 int rbf_mlp_adam(rbf_ctx *ctx, int64_t n, float *p, const float *g, float *m, float *v, float lr, float b1,
                  float b2, float eps, int32_t step, void *p_bf16);
+
+/* ---- locality reordering ------------------------------------------------------ */
+/* Replaces reorder_points!(x, k) (src/utils.jl:45-55, a SymRCM ordering of the stencil
+ * graph): a permutation perm_out[n] with x_new[i] = x[perm_out[i]] that orders the points
+ * along a Morton curve over a grid of about two points per cell (within a cell by original
+ * index), so that stencils gather nearby entries in the apply.  data_out (optional, n x
+ * dim) receives the permuted points. */
+int rbf_reorder_points(rbf_ctx *ctx, const double *data, int64_t n, int32_t dim, int32_t *perm_out,
+                       double *data_out);
 
 /* ---- batched build of uneven stencils (no counterpart in the reference) ------ */
 /* Ragged stencils: the neighbours of eval point e are adj_idx[adj_ptr[e] .. adj_ptr[e+1])

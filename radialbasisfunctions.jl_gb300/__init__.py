@@ -36,7 +36,7 @@ __all__ = [
     "find_neighbors", "autoselect_k", "Laplacian", "Partial", "Jacobian", "Regrid", "Operators",
     "laplacian", "partial", "gradient", "jacobian", "regrid", "RadialBasisOperator", "WeightsCSR",
     "weights", "update_weights", "mul", "DimensionMismatch", "SingularException", "Context", "build_library",
-    "build_weights", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph",
+    "build_weights", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph", "reorder_points",
 ]
 
 build_library = _native.build_library
@@ -531,6 +531,28 @@ def build_weights(ops, data, eval_points, adjl, basis, hermite=None, precision="
     if return_status:
         return Ws, status
     return Ws
+
+
+def reorder_points(data, k=None, ctx=None):
+    """reorder_points!(x, k) (src/utils.jl:45-55): returns (perm, x[perm]) with the points
+    ordered along a Morton curve for locality (0-based perm; the reference's SymRCM order
+    is another locality order with the same contract).  k is accepted for the reference's
+    signature and not needed."""
+    torch = _torch()
+    d = _points(data)
+    n, dim = d.shape
+    ctx = ctx or Context.default(_device_of(d))
+    if _is_torch(d) and d.is_cuda:
+        perm = torch.empty(n, dtype=torch.int32, device=d.device)
+        out = torch.empty_like(d)
+    elif _is_torch(d):
+        perm = torch.empty(n, dtype=torch.int32)
+        out = torch.empty_like(d)
+    else:
+        perm = np.empty(n, dtype=np.int32)
+        out = np.empty_like(d)
+    ctx.check(ctx.lib.rbf_reorder_points(ctx.h, _ptr(d), n, dim, _ptr(perm), _ptr(out)))
+    return perm, out
 
 
 # ------------------------------------------------------------------------------ batched (uneven) build

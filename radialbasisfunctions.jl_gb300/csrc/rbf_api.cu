@@ -254,6 +254,18 @@ int rbf_ctx_destroy(rbf_ctx *ctx) {
     return RBF_OK;
 }
 
+int rbf_ctx_set_timing(rbf_ctx *ctx, int32_t on) {
+    if (!ctx) return RBF_ERR_ARGUMENT;
+    ctx->timing = on != 0;
+    return RBF_OK;
+}
+
+int rbf_ctx_last_ms(rbf_ctx *ctx, float *ms) {
+    if (!ctx || !ms) return RBF_ERR_ARGUMENT;
+    *ms = ctx->last_ms;
+    return RBF_OK;
+}
+
 int rbf_ctx_set_stream(rbf_ctx *ctx, void *s) {
     if (!ctx) return RBF_ERR_ARGUMENT;
     ctx->stream = s ? static_cast<cudaStream_t>(s) : ctx->own_stream;
@@ -276,7 +288,21 @@ int rbf_knn(rbf_ctx *ctx, const double *data, int64_t ns, const double *eval, in
     RBF_TRY(d.bind(ctx, data, sizeof(double) * ns * dim));
     RBF_TRY(q.bind(ctx, eval, sizeof(double) * ne * dim));
     RBF_TRY(o.bind(ctx, idx_out, sizeof(int32_t) * ne * k));
-    RBF_TRY(rbf_knn_device(ctx, d.as<double>(), ns, q.as<double>(), ne, dim, k, o.as<int32_t>()));
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (ctx->timing) {
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, ctx->stream);
+    }
+    const int kst = rbf_knn_device(ctx, d.as<double>(), ns, q.as<double>(), ne, dim, k, o.as<int32_t>());
+    if (ctx->timing) {
+        cudaEventRecord(t1, ctx->stream);
+        cudaEventSynchronize(t1);
+        cudaEventElapsedTime(&ctx->last_ms, t0, t1);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
+    RBF_TRY(kst);
     RBF_TRY(o.finish(ctx));
     RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RBF_OK;
@@ -461,8 +487,22 @@ int rbf_spmm(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const
     OutArray y;
     RBF_TRY(y.bind(ctx, Y, ybytes));
     if (y.host && beta != 0.0) RBF_CUDA(ctx, cudaMemcpyAsync(y.dptr, Y, ybytes, cudaMemcpyHostToDevice, ctx->stream));
-    RBF_TRY(rbf_spmm_device(ctx, ne, ns, rp.as<int64_t>(), c.as<int32_t>(), v.as<double>(), nf, layout, x.as<double>(),
-                            nf == 1 ? 1 : ldx, alpha, beta, y.as<double>(), nf == 1 ? 1 : ldy));
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (ctx->timing) {
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, ctx->stream);
+    }
+    const int sst = rbf_spmm_device(ctx, ne, ns, rp.as<int64_t>(), c.as<int32_t>(), v.as<double>(), nf, layout,
+                                    x.as<double>(), nf == 1 ? 1 : ldx, alpha, beta, y.as<double>(), nf == 1 ? 1 : ldy);
+    if (ctx->timing) {
+        cudaEventRecord(t1, ctx->stream);
+        cudaEventSynchronize(t1);
+        cudaEventElapsedTime(&ctx->last_ms, t0, t1);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
+    RBF_TRY(sst);
     RBF_TRY(y.finish(ctx));
     RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RBF_OK;

@@ -29,6 +29,8 @@ struct rbf_ctx {
     long long launches = 0;      // kernels launched through this context
     long long knn_fallback = 0;  // queries re-run by the exact FP64 neighbour search
     std::map<unsigned long long, rbf_tune_entry> tune;  // batched build: size class -> tile
+    bool timing = false;  // record CUDA events around the device work of knn / spmm
+    float last_ms = 0.f;  // duration of the last timed device work
 };
 
 int rbf_fail(rbf_ctx *ctx, int code, const char *fmt, ...);

@@ -53,6 +53,98 @@ __global__ void __launch_bounds__(256) spmv_kernel(int64_t ne, const int64_t *__
     }
 }
 
+// Single field with paired loads: a row's entries are read two at a time (int2 columns,
+// double2 values; an odd row start takes one scalar head entry first), which halves the
+// load instructions per nonzero.  Lane sub of a row handles pairs sub, sub + TPR, ... (U per
+// chunk), and each lane works on S rows at once (S independent load chains in flight).
+// Rows are taken in contiguous ranges, so that in a locality order the x values an SM
+// gathers stay in its L1: per warp (BLOCK_RANGE false), or per block with its warps
+// interleaved in the range (BLOCK_RANGE true: all warps of a block share one window of x).
+template <int TPR, int U, int S, bool BLOCK_RANGE>
+__global__ void __launch_bounds__(256) spmv_pair_kernel(int64_t ne, const int64_t *__restrict__ rp,
+                                                        const int32_t *__restrict__ col,
+                                                        const double *__restrict__ val,
+                                                        const double *__restrict__ x, double alpha, double beta,
+                                                        double *__restrict__ y) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int sub = threadIdx.x % TPR;
+    constexpr int RPW = 32 / TPR;
+    const int64_t steps = (ne + RPW - 1) / RPW;
+    int64_t st0, st_end, st_inc;
+    if constexpr (BLOCK_RANGE) {
+        const int64_t per = (steps + gridDim.x - 1) / gridDim.x;
+        st0 = blockIdx.x * per + (threadIdx.x >> 5);
+        st_end = min(steps, (int64_t)(blockIdx.x + 1) * per);
+        st_inc = blockDim.x >> 5;
+    } else {
+        const int64_t warp = tid >> 5, nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+        const int64_t per = (steps + nwarps - 1) / nwarps;
+        st0 = warp * per;
+        st_end = min(steps, (warp + 1) * per);
+        st_inc = 1;
+    }
+    for (int64_t st = st0; st < st_end; st += S * st_inc) {
+        int64_t r[S], a[S], b[S];
+        double acc[S];
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int64_t stt = st + t * st_inc;
+            r[t] = stt < st_end ? stt * RPW + (threadIdx.x & 31) / TPR : ne;
+            const bool live = r[t] < ne;
+            a[t] = live ? __ldg(&rp[r[t]]) : 0;
+            b[t] = live ? __ldg(&rp[r[t] + 1]) : 0;
+            acc[t] = 0.0;
+            if ((a[t] & 1) && a[t] < b[t]) {  // odd start: one scalar entry so the pairs are aligned
+                if (sub == 0) acc[t] = __ldg(&val[a[t]]) * __ldg(&x[__ldg(&col[a[t]])]);
+                a[t]++;
+            }
+        }
+        for (int64_t off = 2 * sub;; off += (int64_t)2 * TPR * U) {
+            bool any = false;
+#pragma unroll
+            for (int t = 0; t < S; t++) any |= a[t] + off < b[t];
+            if (!any) break;
+            int2 c[S][U];
+            double2 v[S][U];
+#pragma unroll
+            for (int t = 0; t < S; t++)
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int64_t q = a[t] + off + (int64_t)2 * TPR * u;
+                    if (q + 1 < b[t]) {
+                        c[t][u] = __ldg(reinterpret_cast<const int2 *>(col + q));
+                        v[t][u] = __ldg(reinterpret_cast<const double2 *>(val + q));
+                    } else if (q < b[t]) {
+                        c[t][u] = make_int2(__ldg(&col[q]), -1);
+                        v[t][u] = make_double2(__ldg(&val[q]), 0.0);
+                    } else {
+                        c[t][u] = make_int2(-1, -1);
+                        v[t][u] = make_double2(0.0, 0.0);
+                    }
+                }
+            double xa[S][U], xb[S][U];
+#pragma unroll
+            for (int t = 0; t < S; t++)
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    xa[t][u] = c[t][u].x >= 0 ? __ldg(&x[c[t][u].x]) : 0.0;
+                    xb[t][u] = c[t][u].y >= 0 ? __ldg(&x[c[t][u].y]) : 0.0;
+                }
+#pragma unroll
+            for (int t = 0; t < S; t++)
+#pragma unroll
+                for (int u = 0; u < U; u++) acc[t] = fma(v[t][u].y, xb[t][u], fma(v[t][u].x, xa[t][u], acc[t]));
+        }
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            double sm = acc[t];
+#pragma unroll
+            for (int o = TPR / 2; o > 0; o >>= 1) sm += __shfl_down_sync(0xffffffffu, sm, o, TPR);
+            if (sub == 0 && r[t] < ne) y[r[t]] = (beta == 0.0) ? alpha * sm : fma(alpha, sm, beta * y[r[t]]);
+        }
+    }
+}
+
 // lanes = fields (nf <= 32), 32/nfp rows per warp, nfp = nf rounded up to a power of two
 __global__ void __launch_bounds__(256) spmm_interleaved_kernel(int64_t ne, const int64_t *__restrict__ rp,
                                                                const int32_t *__restrict__ col,
@@ -166,17 +258,25 @@ int blocks_for(rbf_ctx *ctx, int64_t work, int threads, int per_sm) {
 
 }  // namespace
 
+// One field: the paired-load kernel (4 lanes per row, 4 pairs per lane, block row ranges:
+// the fastest of the shapes measured on GB300) when the arrays allow 8/16-byte loads.
+static int spmv_launch(rbf_ctx *ctx, int64_t ne, const int64_t *d_rp, const int32_t *d_col, const double *d_val,
+                const double *d_X, double alpha, double beta, double *d_Y) {
+    if ((((uintptr_t)d_col) & 7) == 0 && (((uintptr_t)d_val) & 15) == 0)
+        spmv_pair_kernel<4, 4, 1, true><<<blocks_for(ctx, ne * 4, 256, 8), 256, 0, ctx->stream>>>(
+            ne, d_rp, d_col, d_val, d_X, alpha, beta, d_Y);
+    else
+        spmv_kernel<8, 4><<<blocks_for(ctx, ne * 8, 256, 16), 256, 0, ctx->stream>>>(ne, d_rp, d_col, d_val, d_X,
+                                                                                    alpha, beta, d_Y);
+    RBF_CHECK_LAUNCH(ctx);
+    return RBF_OK;
+}
+
 int rbf_spmm_device(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *d_rp, const int32_t *d_col,
                     const double *d_val, int nf, int layout, const double *d_X, int64_t ldx, double alpha,
                     double beta, double *d_Y, int64_t ldy) {
     if (ne == 0 || nf == 0) return RBF_OK;
-    if (nf == 1) {
-        const int TPR = 8;
-        spmv_kernel<TPR, 4><<<blocks_for(ctx, ne * TPR, 256, 16), 256, 0, ctx->stream>>>(ne, d_rp, d_col, d_val, d_X,
-                                                                                         alpha, beta, d_Y);
-        RBF_CHECK_LAUNCH(ctx);
-        return RBF_OK;
-    }
+    if (nf == 1) return spmv_launch(ctx, ne, d_rp, d_col, d_val, d_X, alpha, beta, d_Y);
     const double *Xi = d_X;
     double *Yi = d_Y;
     int64_t lx = ldx, ly = ldy;
@@ -299,9 +399,7 @@ extern "C" int rbf_spmm_noalloc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int6
     if (ne == 0) return RBF_OK;
     if (!staged) {
         if (nf == 1) {
-            spmv_kernel<8, 4><<<blocks_for(ctx, ne * 8, 256, 16), 256, 0, ctx->stream>>>(ne, row_ptr, col, val, X, alpha,
-                                                                                         beta, Y);
-            RBF_CHECK_LAUNCH(ctx);
+            RBF_TRY(spmv_launch(ctx, ne, row_ptr, col, val, X, alpha, beta, Y));
         } else {
             for (int f0 = 0; f0 < nf; f0 += 32) {
                 int nfc = std::min(32, nf - f0), nfp = 1;

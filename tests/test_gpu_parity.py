@@ -354,3 +354,32 @@ def test_calls_follow_torch_stream(pkg):
         assert torch.equal(adjl, adjl0)
         assert torch.equal(val, W0.val)
         assert torch.equal(y, y0)
+
+
+# ---------------------------------------------------------------------------- reorder_points
+def test_reorder_points(pkg):
+    """reorder_points! contract (test/utils.jl:61-78): a permutation with x_new = x[perm];
+    deterministic; neighbours end up close in index; the operator on the reordered cloud is
+    the original one with rows and columns permuted."""
+    rng = np.random.default_rng(9)
+    n = 200000
+    X = torch.from_numpy(rng.uniform(0, 1, (n, 3))).cuda()
+    perm, Xr = pkg.reorder_points(X, 20)
+    p = perm.long()
+    assert torch.equal(torch.sort(p).values, torch.arange(n, device=p.device))
+    assert torch.equal(Xr, X[p])
+    perm2, _ = pkg.reorder_points(X)
+    assert torch.equal(perm, perm2)
+    a0 = pkg.find_neighbors(X, k=20).long()
+    a1 = pkg.find_neighbors(Xr, k=20).long()
+    spread0 = (a0 - torch.arange(n, device=a0.device)[:, None]).abs().float().median()
+    spread1 = (a1 - torch.arange(n, device=a1.device)[:, None]).abs().float().median()
+    assert float(spread1) < 0.01 * float(spread0), (float(spread0), float(spread1))
+    basis = pkg.PHS(3, poly_deg=2)
+    f = torch.sin(3 * X[:, 0]) * X[:, 2]
+    y0 = pkg.build_weights([(3, 0)], X, None, a0.int(), basis)[0].apply(f)
+    y1 = pkg.build_weights([(3, 0)], Xr, None, a1.int(), basis)[0].apply(f[p])
+    assert float((y1 - y0[p]).abs().max() / y0.abs().max()) < 1e-10
+    Xh = rng.uniform(0, 1, (1000, 2))
+    ph, Xhr = pkg.reorder_points(Xh)
+    assert np.array_equal(np.sort(ph), np.arange(1000)) and np.array_equal(Xhr, Xh[ph])
