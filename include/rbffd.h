@@ -196,6 +196,15 @@ int rbf_mlp_to_bf16(rbf_ctx *ctx, int32_t rows, int32_t cols, int32_t pad_cols, 
  * data holds n_data points; an adjl entry outside [0, n_data) is an RBF_ERR_ARGUMENT. */
 int rbf_mlp_features(rbf_ctx *ctx, const double *data, int64_t n_data, const double *eval, int32_t dim,
                      const int32_t *adjl, int64_t ne, int32_t k, void *out, int32_t ldo);
+/* The same product on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor
+ * memory): C = act(A * B^T + bias), act GELU (gelu_on) or identity, exactly one of Cf (FP32)
+ * or Cb (bf16) with row stride ldc (16-byte aligned rows).  K a multiple of 32.  Used for
+ * the surrogate's inference. */
+int rbf_mlp_gemm_tc(rbf_ctx *ctx, int32_t M, int32_t N, int32_t K, const void *A, int32_t lda, const void *B,
+                    int32_t ldb, const float *bias, int32_t gelu_on, float *Cf, void *Cb, int32_t ldc);
+/* *failed = 1 if a tensor-core GEMM since the last call gave up waiting on its pipeline
+ * (its output is then incomplete); synchronises the context's stream. */
+int rbf_mlp_tc_status(rbf_ctx *ctx, int32_t *failed);
 /* mean squared error over rows x cols and its gradient (bf16, zero in the padding) */
 int rbf_mlp_mse(rbf_ctx *ctx, int32_t rows, int32_t cols, const float *Y, int32_t ldy, const float *T,
                 int32_t ldt, void *dY, int32_t ldd, int32_t pad_cols, float *loss);

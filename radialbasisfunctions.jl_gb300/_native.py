@@ -24,7 +24,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
               "-Xptxas", "-warn-spills"]
 
 SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "stencil_build.cu", "stencil_refined_a.cu",
-           "stencil_refined_b.cu", "batched.cu", "plan.cu", "reorder.cu", "diag.cu", "mlp.cu"]
+           "stencil_refined_b.cu", "batched.cu", "plan.cu", "reorder.cu", "diag.cu", "mlp.cu",
+           "mlp_tc.cu"]
 
 
 def _nvcc():
@@ -130,6 +131,8 @@ SIGNATURES = {
     "rbf_reorder_points": (_I, [_P, _P, _I64, _I32, _P, _P]),
     "rbf_ctx_set_timing": (_I, [_P, _I32]),
     "rbf_ctx_last_ms": (_I, [_P, _P]),
+    "rbf_mlp_gemm_tc": (_I, [_P, _I32, _I32, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _P, _I32]),
+    "rbf_mlp_tc_status": (_I, [_P, _P]),
     "rbf_mlp_features": (_I, [_P, _P, _I64, _P, _I32, _P, _I64, _I32, _P, _I32]),
     "rbf_mlp_to_bf16": (_I, [_P, _I32, _I32, _I32, _P, _I32, _P, _I32]),
     "rbf_mlp_mse": (_I, [_P, _I32, _I32, _P, _I32, _P, _I32, _P, _I32, _I32, _P]),

@@ -79,6 +79,18 @@ class StencilMLP:
                                           Cb.stride(0) if Cb is not None else 0, _p(Zf),
                                           Zf.stride(0) if Zf is not None else 0))
 
+    def _gemm_tc(self, A, B, M, N, K, bias=None, gelu=False, Cf=None, Cb=None):
+        out = Cf if Cf is not None else Cb
+        self._check(self.lib.rbf_mlp_gemm_tc(self.ctx.h, M, N, K, _p(A), A.stride(0), _p(B), B.stride(0), _p(bias),
+                                             1 if gelu else 0, _p(Cf), _p(Cb), out.stride(0)))
+
+    def tc_status(self):
+        """Raise if a tensor-core GEMM gave up waiting on its pipeline (synchronises)."""
+        f = ctypes.c_int32(0)
+        self._check(self.lib.rbf_mlp_tc_status(self.ctx.h, ctypes.byref(f)))
+        if f.value:
+            raise RuntimeError("a tensor-core GEMM of the surrogate did not complete")
+
     def _transpose(self, X):
         torch = _torch()
         rows, cols = X.shape
@@ -97,14 +109,27 @@ class StencilMLP:
         return out
 
     # ------------------------------------------------------------------ forward / backward
-    def forward(self, Xb, keep=False):
+    def forward(self, Xb, keep=False, tensor_cores=True):
         """Xb: bf16 inputs (B x pad(din)).  Returns FP32 outputs (B x pad(dout)) in network units;
-        with keep=True also the pre-activations and activations needed by backward()."""
+        with keep=True also the pre-activations and activations needed by backward().  Without
+        keep, the layers run on the tcgen05 GEMM (tensor_cores) or the mma.sync GEMM."""
         torch = _torch()
         B = Xb.shape[0]
+        L = len(self.W)
+        if not keep and tensor_cores:
+            a = Xb
+            for i in range(L):
+                fout, fin = self.W[i].shape
+                if i < L - 1:
+                    h = torch.empty((B, fout), dtype=torch.bfloat16, device=self.dev)
+                    self._gemm_tc(a, self.Wb[i], B, fout, fin, bias=self.b[i], gelu=True, Cb=h)
+                    a = h
+                else:
+                    y = torch.empty((B, fout), dtype=torch.float32, device=self.dev)
+                    self._gemm_tc(a, self.Wb[i], B, fout, fin, bias=self.b[i], gelu=False, Cf=y)
+            return y
         acts, zs = [Xb], []
         a = Xb
-        L = len(self.W)
         for i in range(L):
             fout, fin = self.W[i].shape
             if i < L - 1:
@@ -157,13 +182,16 @@ class StencilMLP:
                                               lr, b1, b2, eps, self.t, _p(pb)))
         return loss
 
-    def predict(self, Xb, batch=1 << 20):
-        """Predicted weights (B x k, FP32, local units) for bf16 inputs, in chunks."""
+    def predict(self, Xb, batch=1 << 20, tensor_cores=True):
+        """Predicted weights (B x k, FP32, local units) for bf16 inputs, in chunks (tcgen05
+        GEMMs by default; the call checks that they completed)."""
         torch = _torch()
         out = torch.empty((Xb.shape[0], self.dout), dtype=torch.float32, device=self.dev)
         for s in range(0, Xb.shape[0], batch):
-            y = self.forward(Xb[s:s + batch])
+            y = self.forward(Xb[s:s + batch], tensor_cores=tensor_cores)
             out[s:s + batch] = y[:, :self.dout] * self.out_scale
+        if tensor_cores:
+            self.tc_status()
         return out
 
     # ------------------------------------------------------------------ checkpoint

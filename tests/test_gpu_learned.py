@@ -123,3 +123,42 @@ def test_learned_build_equals_fp64(pkg):
         d = (W.val - W64.val).abs().reshape(-1, 30).amax(1) / W64.val.abs().reshape(-1, 30).amax(1)
         assert float(d.max()) <= 1e-8, (trained, float(d.max()))
         assert set(np.unique(status.cpu().numpy())) <= {0, 3}
+
+
+@pytest.mark.parametrize("M,N,K", [(300, 256, 96), (128, 32, 256), (1000, 96, 32), (257, 64, 64)])
+@pytest.mark.parametrize("gelu,bf16_out", [(False, False), (True, True)])
+def test_tc_gemm_equals_mma_sync(pkg, M, N, K, gelu, bf16_out):
+    """The tcgen05 GEMM (TMEM accumulators) equals the mma.sync GEMM bit for bit on operands
+    whose products and sums are exact (small integers), incl. row/column tails, the bias and
+    the GELU epilogue, and it reports no pipeline timeout."""
+    L = pkg.learned
+    model = L.StencilMLP(k=30, dim=3, hidden=(64,), seed=0)
+    rng = np.random.default_rng(M + N + K)
+    A = torch.from_numpy(rng.integers(-4, 5, (M, K)).astype(np.float32)).cuda().to(torch.bfloat16)
+    B = torch.from_numpy(rng.integers(-4, 5, (N, K)).astype(np.float32)).cuda().to(torch.bfloat16)
+    bias = torch.from_numpy(rng.integers(-8, 9, N).astype(np.float32)).cuda()
+    if bf16_out:
+        C0 = torch.empty((M, N), dtype=torch.bfloat16, device="cuda")
+        C1 = torch.empty_like(C0)
+        model._gemm(A, B, M, N, K, bias=bias, epi=1 if gelu else 0, Cb=C0)
+        model._gemm_tc(A, B, M, N, K, bias=bias, gelu=gelu, Cb=C1)
+    else:
+        C0 = torch.empty((M, N), dtype=torch.float32, device="cuda")
+        C1 = torch.empty_like(C0)
+        model._gemm(A, B, M, N, K, bias=bias, epi=1 if gelu else 0, Cf=C0)
+        model._gemm_tc(A, B, M, N, K, bias=bias, gelu=gelu, Cf=C1)
+    model.tc_status()
+    assert torch.equal(C0, C1)
+
+
+def test_predict_tensor_cores(pkg):
+    """Inference on the tensor cores agrees with the mma.sync forward (bf16 activations)."""
+    L = pkg.learned
+    model = L.StencilMLP(k=30, dim=3, seed=4, out_scale=3.0)
+    rng = np.random.default_rng(8)
+    X = np.zeros((5000, model.dims[0]), dtype=np.float32)
+    X[:, :90] = rng.uniform(-1, 1, (5000, 90))
+    Xb = torch.from_numpy(X).cuda().to(torch.bfloat16)
+    p_tc = model.predict(Xb)
+    p_ms = model.predict(Xb, tensor_cores=False)
+    assert float((p_tc - p_ms).abs().max() / p_ms.abs().max()) < 2e-2
