@@ -198,8 +198,8 @@ int rbf_mlp_features(rbf_ctx *ctx, const double *data, int64_t n_data, const dou
                      const int32_t *adjl, int64_t ne, int32_t k, void *out, int32_t ldo);
 /* The same product on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor
  * memory): C = act(A * B^T + bias), act GELU (gelu_on) or identity, exactly one of Cf (FP32)
- * or Cb (bf16) with row stride ldc (16-byte aligned rows).  K a multiple of 32.  Used for
- * the surrogate's inference. */
+ * or Cb (bf16) with row stride ldc (16-byte aligned rows), bias (optional) 16-byte aligned.
+ * K a multiple of 32.  Used for the surrogate's inference. */
 int rbf_mlp_gemm_tc(rbf_ctx *ctx, int32_t M, int32_t N, int32_t K, const void *A, int32_t lda, const void *B,
                     int32_t ldb, const float *bias, int32_t gelu_on, float *Cf, void *Cb, int32_t ldc);
 /* *failed = 1 if a tensor-core GEMM since the last call gave up waiting on its pipeline

@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY (the checker of the GPU kernels; never on the product path).
 
 Float64 NumPy restatement of the network the rbf_mlp_* kernels run: y = W_L g(... g(W_1 x + b_1)
-...) + b_L with the exact (erf) GELU g, MSE loss mean((y - t)^2) over the real output columns,
+...) + b_L with the GELU g in its tanh form, MSE loss mean((y - t)^2) over the real output columns,
 and its gradients by reverse-mode differentiation.  The GPU keeps matrices, activations and
 back-propagated signals in bf16; the same roundings are applied here at the same places
 (`bf16` below), so the two differ only by FP32-vs-FP64 accumulation.
@@ -22,13 +22,15 @@ def bf16(a):
 
 
 def gelu(z):
-    from scipy.special import erf
-    return 0.5 * z * (1.0 + erf(z / math.sqrt(2.0)))
+    """GELU in its tanh form (Hendrycks & Gimpel), the activation of the surrogate."""
+    u = math.sqrt(2.0 / math.pi) * (z + 0.044715 * z ** 3)
+    return 0.5 * z * (1.0 + np.tanh(u))
 
 
 def gelu_grad(z):
-    from scipy.special import erf
-    return 0.5 * (1.0 + erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2 * math.pi)
+    c = math.sqrt(2.0 / math.pi)
+    t = np.tanh(c * (z + 0.044715 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * c * (1.0 + 3 * 0.044715 * z * z)
 
 
 def forward_backward(X, W, b, T, dout):

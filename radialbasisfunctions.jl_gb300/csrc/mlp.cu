@@ -4,7 +4,7 @@
 // GEMM: C[M x N] = A[M x K] * B[N x K]^T with A and B bf16, K contiguous in both (the
 // [out x in] layout of a weight matrix), FP32 accumulation on the tensor cores through
 // mma.sync m16n8k16.  One 64x64 tile per block of 4 warps (each warp 32x32 = 2 x 4
-// fragments), K staged through shared memory 32 at a time.  Epilogues: + bias, GELU,
+// fragments), K staged through shared memory 32 at a time.  Epilogues: + bias, GELU (tanh form, mlp_common.cuh),
 // or multiplication by GELU'(aux) for the backward pass; outputs FP32 and/or bf16.
 // K must be a multiple of 32 and leading dimensions multiples of 8 (inputs are padded).
 #include <cuda_bf16.h>
@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "mlp_common.cuh"
 #include "rbf_internal.cuh"
 
 namespace {
@@ -24,13 +25,6 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
         "{%0,%1,%2,%3};\n"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
-__device__ __forceinline__ float gelu_grad(float z) {
-    const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
-    const float pdf = 0.39894228040143268f * __expf(-0.5f * z * z);
-    return cdf + z * pdf;
 }
 
 enum { EPI_NONE = 0, EPI_GELU = 1, EPI_GELU_GRAD = 2 };

@@ -2,7 +2,8 @@
 //
 // C[M x N] = act(A[M x K] * B[N x K]^T + bias): A the bf16 activations (K contiguous), B a
 // bf16 weight matrix in its [out x in] layout (K contiguous), FP32 accumulation in tensor
-// memory (TMEM), epilogue + bias, GELU or identity, bf16 or FP32 output.
+// memory (TMEM), epilogue + bias, GELU (tanh form, mlp_common.cuh) or identity, bf16 or
+// FP32 output.
 //
 // One CTA of 128 threads computes a 128 x BN tile.  K is consumed 32 at a time through a
 // 4-stage ring in shared memory: every thread copies 16-byte chunks two k-blocks ahead with
@@ -19,6 +20,7 @@
 
 #include <algorithm>
 
+#include "mlp_common.cuh"
 #include "rbf_internal.cuh"
 
 namespace {
@@ -60,8 +62,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     }
     return false;
 }
-
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
 
 template <int BN>
 __global__ void __launch_bounds__(TC_THREADS) gemm_tc_kernel(int M, int N, int K, const __nv_bfloat16 *__restrict__ A,
@@ -180,11 +180,23 @@ __global__ void __launch_bounds__(TC_THREADS) gemm_tc_kernel(int M, int N, int K
             const int col = n0 + c0;
             if (row < M && col < N) {
                 float o[16];
+                if (bias && col + 16 <= N) {
 #pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    const float z = __uint_as_float(v[j]) + (bias && col + j < N ? bias[col + j] : 0.0f);
-                    o[j] = gelu_on ? gelu(z) : z;
+                    for (int j = 0; j < 4; j++) {
+                        const float4 bv = __ldg(reinterpret_cast<const float4 *>(bias + col) + j);
+                        o[4 * j] = __uint_as_float(v[4 * j]) + bv.x;
+                        o[4 * j + 1] = __uint_as_float(v[4 * j + 1]) + bv.y;
+                        o[4 * j + 2] = __uint_as_float(v[4 * j + 2]) + bv.z;
+                        o[4 * j + 3] = __uint_as_float(v[4 * j + 3]) + bv.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        o[j] = __uint_as_float(v[j]) + (bias && col + j < N ? bias[col + j] : 0.0f);
                 }
+                if (gelu_on)
+#pragma unroll
+                    for (int j = 0; j < 16; j++) o[j] = gelu(o[j]);
                 if (Cb) {
                     __nv_bfloat16 *dst = Cb + (size_t)row * ldc + col;
                     if (col + 16 <= N) {
@@ -243,6 +255,7 @@ int rbf_mlp_gemm_tc(rbf_ctx *ctx, int32_t M, int32_t N, int32_t K, const void *A
     if (lda % 8 || ldb % 8 || lda < K || ldb < K || ((uintptr_t)A & 15) || ((uintptr_t)B & 15))
         return rbf_fail(ctx, RBF_ERR_ARGUMENT, "gemm_tc: operands need 16-byte aligned rows (ld multiple of 8, >= K)");
     if ((Cf == nullptr) == (Cb == nullptr)) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "gemm_tc: give exactly one output");
+    if (bias && ((uintptr_t)bias & 15)) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "gemm_tc: bias must be 16-byte aligned");
     if (ldc < N || (Cb && ((ldc % 8) || ((uintptr_t)Cb & 15))) || (Cf && ((ldc % 4) || ((uintptr_t)Cf & 15))))
         return rbf_fail(ctx, RBF_ERR_ARGUMENT, "gemm_tc: output rows must be 16-byte aligned");
     if (M == 0) return RBF_OK;
