@@ -6,17 +6,23 @@
 // FP32 output.
 //
 // One CTA of 128 threads computes a 128 x BN tile.  K is consumed 32 at a time through a
-// 4-stage ring in shared memory: every thread copies 16-byte chunks two k-blocks ahead with
-// cp.async into the canonical no-swizzle K-major layout (8 x 16-byte core matrices, the
-// two core matrices of a 16-wide K slice adjacent: LBO = 128 B, 8-row groups 512 B apart:
-// SBO), then one thread issues two tcgen05.mma (M = 128, N = BN, K = 16 each) and commits
-// them to the stage's mbarrier, which releases the stage for refilling.  After the last
-// commit, each warp reads its 32 TMEM lanes (rows) with tcgen05.ld and runs the epilogue.
+// 4-stage ring in shared memory filled by TMA: a stage holds, for A and for B, four boxes of
+// 8 K-elements (16 bytes) x all tile rows, which is the canonical no-swizzle K-major layout
+// of tcgen05 directly (8 x 16-byte core matrices; core matrices along K one box apart:
+// LBO; 8-row groups 128 bytes apart: SBO).  One thread runs the pipeline: it arms a stage's
+// "full" mbarrier with the expected bytes and issues its 8 box loads, waits for a stage to
+// land, issues two tcgen05.mma (M = 128, N = BN, K = 16 each) and commits them to the
+// stage's "empty" mbarrier, which it waits on before refilling the stage.  Rows past M
+// (and past N) are zero-filled by TMA.  After the last commit, each warp reads its 32 TMEM
+// lanes (rows) with tcgen05.ld, runs the epilogue into a shared tile, and the block writes
+// the tile out row by row (coalesced).
 //
 // Every mbarrier wait is bounded: on a timeout the block agrees (a barrier reduction),
-// stops issuing, drains its copies, frees its TMEM and records the failure in a device
-// error word that the host reads (rbf_mlp_tc_status).
+// stops issuing, frees its TMEM and records the failure in a device error word that the
+// host reads (rbf_mlp_tc_status).
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 
@@ -45,9 +51,16 @@ __host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, bool valid) {
-    const int n = valid ? 16 : 0;  // 0: zero-fill, nothing read
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
@@ -64,15 +77,16 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 }
 
 template <int BN>
-__global__ void __launch_bounds__(TC_THREADS) gemm_tc_kernel(int M, int N, int K, const __nv_bfloat16 *__restrict__ A,
-                                                             int lda, const __nv_bfloat16 *__restrict__ B, int ldb,
-                                                             const float *__restrict__ bias, int gelu_on,
+__global__ void __launch_bounds__(TC_THREADS) gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA,
+                                                             const __grid_constant__ CUtensorMap mapB, int M, int N,
+                                                             int K, const float *__restrict__ bias, int gelu_on,
                                                              float *__restrict__ Cf, __nv_bfloat16 *__restrict__ Cb,
                                                              int ldc) {
     constexpr int A_BYTES = TC_M * TC_KB * 2, B_BYTES = BN * TC_KB * 2, STAGE = A_BYTES + B_BYTES;
-    extern __shared__ __align__(128) char smem[];
-    __shared__ __align__(8) unsigned long long bars[TC_STAGES];
+    extern __shared__ __align__(1024) char smem[];
+    __shared__ __align__(8) unsigned long long full[TC_STAGES], empty[TC_STAGES];
     __shared__ uint32_t tmem_slot;
+    __shared__ int s_fail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.y * TC_M, n0 = blockIdx.x * BN;
     const int nkb = K / TC_KB;
@@ -83,67 +97,47 @@ __global__ void __launch_bounds__(TC_THREADS) gemm_tc_kernel(int M, int N, int K
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (tid == 0) {
-        for (int s = 0; s < TC_STAGES; s++)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bars[s])));
+        for (int s = 0; s < TC_STAGES; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&empty[s])));
+        }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        // TMA writes need 128-byte aligned destinations (the stage offsets are multiples of 2 KB)
+        s_fail = (smem_u32(smem) & 1023u) ? 1 : 0;
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = tmem_slot;
 
-    // copies of k-block kb into its stage: A rows (128 x 4 chunks) then B rows (BN x 4 chunks)
-    auto load_stage = [&](int kb) {
-        const int s = kb % TC_STAGES;
-        const uint32_t base = smem_u32(smem + s * STAGE);
-        const int k0 = kb * TC_KB;
-        for (int c = tid; c < (TC_M + BN) * 4; c += TC_THREADS) {
-            const int row = c >> 2, kc = c & 3;
-            if (row < TC_M) {
-                const int gr = m0 + row;
-                const bool ok = gr < M;
-                cp_async16(base + (uint32_t)(((row & 7) * 16) + (kc * 128) + ((row >> 3) * 512)),
-                           A + (size_t)(ok ? gr : 0) * lda + k0 + kc * 8, ok);
-            } else {
-                const int br = row - TC_M, gn = n0 + br;
-                const bool ok = gn < N;
-                cp_async16(base + A_BYTES + (uint32_t)(((br & 7) * 16) + (kc * 128) + ((br >> 3) * 512)),
-                           B + (size_t)(ok ? gn : 0) * ldb + k0 + kc * 8, ok);
-            }
-        }
-    };
-
-    // copies run TC_AHEAD k-blocks ahead of the MMAs; a refilled stage was last read by the
-    // MMAs of k-block next - STAGES, two blocks before the one being issued, so one block of
-    // MMAs stays in flight while the next is issued
-    constexpr int TC_AHEAD = 2;
-    int failed = 0;
-    for (int kb = 0; kb < TC_AHEAD; kb++) {
-        if (kb < nkb) load_stage(kb);
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    }
-    for (int kb = 0; kb < nkb; kb++) {
-        const int next = kb + TC_AHEAD;
-        bool to = false;
-        if (next < nkb) {
-            // use number next / STAGES of the stage: wait for the completion of use - 1
-            if (next >= TC_STAGES) to = !mbar_wait(smem_u32(&bars[next % TC_STAGES]), ((next / TC_STAGES) - 1) & 1);
-            if (!to) load_stage(next);
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-        asm volatile("cp.async.wait_group %0;\n" ::"n"(TC_AHEAD) : "memory");
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        if (__syncthreads_or(to)) {
-            failed = 1;
-            break;
-        }
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (tid == 0 && !s_fail) {
+        auto issue = [&](int kb) {
             const int s = kb % TC_STAGES;
+            const uint32_t a0 = smem_u32(smem + s * STAGE), b0 = a0 + A_BYTES, bar = smem_u32(&full[s]);
+            mbar_expect(bar, STAGE);
+#pragma unroll
+            for (int kc = 0; kc < TC_KB / 8; kc++) {
+                const int x = kb * TC_KB + kc * 8;  // 8 bf16 = 16 bytes: TMA x stays 16-byte aligned
+                tma_load_2d(a0 + kc * (TC_M * 16), &mapA, x, m0, bar);
+                tma_load_2d(b0 + kc * (BN * 16), &mapB, x, n0, bar);
+            }
+        };
+        int fail = 0;
+        for (int kb = 0; kb < nkb && kb < TC_STAGES; kb++) issue(kb);
+        for (int kb = 0; kb < nkb && !fail; kb++) {
+            const int s = kb % TC_STAGES;
+            if (!mbar_wait(smem_u32(&full[s]), (kb / TC_STAGES) & 1)) {
+                fail = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const uint32_t a0 = smem_u32(smem + s * STAGE), b0 = a0 + A_BYTES;
 #pragma unroll
             for (int j = 0; j < TC_KB / 16; j++) {
-                const uint64_t ad = smem_desc(a0 + j * 256, 128, 512), bd = smem_desc(b0 + j * 256, 128, 512);
+                // K slice 16j..16j+15 = boxes 2j, 2j+1: core matrices along K one box apart (LBO),
+                // 8-row groups 128 bytes apart (SBO)
+                const uint64_t ad = smem_desc(a0 + 2 * j * (TC_M * 16), TC_M * 16, 128);
+                const uint64_t bd = smem_desc(b0 + 2 * j * (BN * 16), BN * 16, 128);
                 const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -152,19 +146,40 @@ __global__ void __launch_bounds__(TC_THREADS) gemm_tc_kernel(int M, int N, int K
                     : "memory");
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                             smem_u32(&bars[s]))
+                             smem_u32(&empty[s]))
                          : "memory");
+            // refill the stage of the previous k-block once its MMAs have read it
+            if (kb >= 1) {
+                const int prev = kb - 1, next = prev + TC_STAGES;
+                if (next < nkb) {
+                    if (!mbar_wait(smem_u32(&empty[prev % TC_STAGES]), (prev / TC_STAGES) & 1)) {
+                        fail = 1;
+                        break;
+                    }
+                    issue(next);
+                }
+            }
         }
+        s_fail = fail;
     }
+    __syncthreads();
+    int failed = s_fail;
     if (!failed && nkb > 0) {
         const int last = nkb - 1;
-        const bool to = !mbar_wait(smem_u32(&bars[last % TC_STAGES]), (last / TC_STAGES) & 1);
+        const bool to = !mbar_wait(smem_u32(&empty[last % TC_STAGES]), (last / TC_STAGES) & 1);
         if (__syncthreads_or(to)) failed = 1;
     }
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
     if (!failed) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        const int row = m0 + warp * 32 + lane;
+        // Epilogue, two passes through the (now idle) stage memory: each thread finishes its
+        // TMEM row into a padded shared tile (row stride an odd number of 16-byte units, so
+        // the 16-byte writes of a quarter-warp hit distinct banks), then each warp writes
+        // whole rows to global memory, contiguous 16-byte pieces across its lanes.
+        const int r_loc = warp * 32 + lane;
+        constexpr int LDB = BN + 8;  // bf16 tile row stride (elements)
+        constexpr int LDF = BN + 4;  // fp32 tile row stride (elements)
+        __nv_bfloat16 *tb = reinterpret_cast<__nv_bfloat16 *>(smem);
+        float *tf = reinterpret_cast<float *>(smem);
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 16) {
             uint32_t v[16];
@@ -178,47 +193,61 @@ __global__ void __launch_bounds__(TC_THREADS) gemm_tc_kernel(int M, int N, int K
                 : "r"(addr));
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             const int col = n0 + c0;
-            if (row < M && col < N) {
-                float o[16];
-                if (bias && col + 16 <= N) {
+            float o[16];
+            if (bias && col + 16 <= N) {
 #pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        const float4 bv = __ldg(reinterpret_cast<const float4 *>(bias + col) + j);
-                        o[4 * j] = __uint_as_float(v[4 * j]) + bv.x;
-                        o[4 * j + 1] = __uint_as_float(v[4 * j + 1]) + bv.y;
-                        o[4 * j + 2] = __uint_as_float(v[4 * j + 2]) + bv.z;
-                        o[4 * j + 3] = __uint_as_float(v[4 * j + 3]) + bv.w;
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 16; j++)
-                        o[j] = __uint_as_float(v[j]) + (bias && col + j < N ? bias[col + j] : 0.0f);
+                for (int j = 0; j < 4; j++) {
+                    const float4 bv = __ldg(reinterpret_cast<const float4 *>(bias + col) + j);
+                    o[4 * j] = __uint_as_float(v[4 * j]) + bv.x;
+                    o[4 * j + 1] = __uint_as_float(v[4 * j + 1]) + bv.y;
+                    o[4 * j + 2] = __uint_as_float(v[4 * j + 2]) + bv.z;
+                    o[4 * j + 3] = __uint_as_float(v[4 * j + 3]) + bv.w;
                 }
-                if (gelu_on)
+            } else {
 #pragma unroll
-                    for (int j = 0; j < 16; j++) o[j] = gelu(o[j]);
-                if (Cb) {
-                    __nv_bfloat16 *dst = Cb + (size_t)row * ldc + col;
-                    if (col + 16 <= N) {
-                        uint4 w[2];
-                        __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(w);
+                for (int j = 0; j < 16; j++)
+                    o[j] = __uint_as_float(v[j]) + (bias && col + j < N ? bias[col + j] : 0.0f);
+            }
+            if (gelu_on)
 #pragma unroll
-                        for (int j = 0; j < 8; j++) h[j] = __floats2bfloat162_rn(o[2 * j], o[2 * j + 1]);
-                        reinterpret_cast<uint4 *>(dst)[0] = w[0];
-                        reinterpret_cast<uint4 *>(dst)[1] = w[1];
-                    } else {
-                        for (int j = 0; j < 16 && col + j < N; j++) dst[j] = __float2bfloat16_rn(o[j]);
-                    }
-                } else {
-                    float *dst = Cf + (size_t)row * ldc + col;
-                    if (col + 16 <= N) {
+                for (int j = 0; j < 16; j++) o[j] = gelu(o[j]);
+            if (Cb) {
+                uint4 w[2];
+                __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(w);
 #pragma unroll
-                        for (int j = 0; j < 4; j++)
-                            reinterpret_cast<float4 *>(dst)[j] =
-                                make_float4(o[4 * j], o[4 * j + 1], o[4 * j + 2], o[4 * j + 3]);
-                    } else {
-                        for (int j = 0; j < 16 && col + j < N; j++) dst[j] = o[j];
-                    }
+                for (int j = 0; j < 8; j++) h[j] = __floats2bfloat162_rn(o[2 * j], o[2 * j + 1]);
+                uint4 *dst = reinterpret_cast<uint4 *>(tb + r_loc * LDB + c0);
+                dst[0] = w[0];
+                dst[1] = w[1];
+            } else {
+                float4 *dst = reinterpret_cast<float4 *>(tf + r_loc * LDF + c0);
+#pragma unroll
+                for (int j = 0; j < 4; j++) dst[j] = make_float4(o[4 * j], o[4 * j + 1], o[4 * j + 2], o[4 * j + 3]);
+            }
+        }
+        __syncthreads();
+        const int ncol = min(BN, N - n0);
+#pragma unroll 1
+        for (int r = warp; r < TC_M; r += TC_THREADS / 32) {
+            const int grow = m0 + r;
+            if (grow >= M) break;
+            if (Cb) {
+                __nv_bfloat16 *g = Cb + (size_t)grow * ldc + n0;
+                const __nv_bfloat16 *t = tb + r * LDB;
+                for (int u = lane; u < BN / 8; u += 32) {
+                    if (u * 8 + 8 <= ncol)
+                        reinterpret_cast<uint4 *>(g)[u] = reinterpret_cast<const uint4 *>(t)[u];
+                    else
+                        for (int j = u * 8; j < ncol; j++) g[j] = t[j];
+                }
+            } else {
+                float *g = Cf + (size_t)grow * ldc + n0;
+                const float *t = tf + r * LDF;
+                for (int u = lane; u < BN / 4; u += 32) {
+                    if (u * 4 + 4 <= ncol)
+                        reinterpret_cast<float4 *>(g)[u] = reinterpret_cast<const float4 *>(t)[u];
+                    else
+                        for (int j = u * 4; j < ncol; j++) g[j] = t[j];
                 }
             }
         }
@@ -230,14 +259,49 @@ __global__ void __launch_bounds__(TC_THREADS) gemm_tc_kernel(int M, int N, int K
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN));
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder(rbf_ctx *ctx) {
+    static void *fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            fn = nullptr;
+    }
+    if (!fn) rbf_fail(ctx, RBF_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+}
+
+// 2-D bf16 tensor map over a row-major [rows x cols] matrix with row stride ld, boxes of
+// 8 columns (16 bytes) x box_rows rows, no swizzle, zero fill outside
+int make_map(rbf_ctx *ctx, CUtensorMap *map, const void *base, int rows, int cols, int ld, int box_rows) {
+    auto enc = tensor_map_encoder(ctx);
+    if (!enc) return RBF_ERR_CUDA;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {8, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return rbf_fail(ctx, RBF_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return RBF_OK;
+}
+
 template <int BN>
 int launch_tc(rbf_ctx *ctx, int M, int N, int K, const void *A, int lda, const void *B, int ldb, const float *bias,
               int gelu_on, float *Cf, void *Cb, int ldc) {
-    constexpr size_t smem = (size_t)TC_STAGES * (TC_M * TC_KB * 2 + BN * TC_KB * 2);
+    // the stage ring, and afterwards the output tile of the epilogue (row strides BN + 8
+    // bf16 or BN + 4 FP32): the larger of the two
+    constexpr size_t ring = (size_t)TC_STAGES * (TC_M * TC_KB * 2 + BN * TC_KB * 2);
+    const size_t tile = Cb ? (size_t)TC_M * (BN + 8) * 2 : (size_t)TC_M * (BN + 4) * 4;
+    const size_t smem = std::max(ring, tile);
+    CUtensorMap ma, mb;
+    RBF_TRY(make_map(ctx, &ma, A, M, K, lda, TC_M));
+    RBF_TRY(make_map(ctx, &mb, B, N, K, ldb, BN));
     RBF_CUDA(ctx, cudaFuncSetAttribute(gemm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((N + BN - 1) / BN, (M + TC_M - 1) / TC_M);
-    gemm_tc_kernel<BN><<<grid, TC_THREADS, smem, ctx->stream>>>(M, N, K, (const __nv_bfloat16 *)A, lda,
-                                                                (const __nv_bfloat16 *)B, ldb, bias, gelu_on, Cf,
+    gemm_tc_kernel<BN><<<grid, TC_THREADS, smem, ctx->stream>>>(ma, mb, M, N, K, bias, gelu_on, Cf,
                                                                 (__nv_bfloat16 *)Cb, ldc);
     RBF_CHECK_LAUNCH(ctx);
     return RBF_OK;
