@@ -359,7 +359,7 @@ def main():
         tf = fl * n / (ms_mlp * 1e-3) / 1e12
         mlp = {"ms_features": ms_feat, "ms_forward": ms_mlp, "flops_per_stencil": fl, "tflops": tf,
                "bf16_peak_tflops": peaks_bf16(), "frac_of_bf16_peak": tf / peaks_bf16(),
-               "kernel": "gemm_bf16_kernel (mma.sync m16n8k16, 64x64 tiles)"}
+               "kernel": "gemm_tc_kernel (tcgen05.mma, TMEM accumulators, TMA-fed, 128xBN tiles)"}
         del feats
     def kernel_ms(fn, reps=10):
         """Median device time of the library work inside fn (CUDA events recorded by the

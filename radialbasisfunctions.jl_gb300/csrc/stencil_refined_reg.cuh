@@ -253,6 +253,14 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
     __syncthreads();
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
     for (int64_t e = (int64_t)blockIdx.x * wpb + wib; e < P.ne; e += nwarps) {
+        // a learned seed is read here, at the top of the stencil, so that its latency hides
+        // behind the load and assembly (lane t holds entry t and t + 32; one operator)
+        float seed_reg[ROWS];
+#pragma unroll
+        for (int s = 0; s < ROWS; s++) {
+            const int i = lane + 32 * s;
+            seed_reg[s] = (R == 1 && P.seed && i < P.k) ? __ldg(&P.seed[e * P.k + i]) : 0.0f;
+        }
         int es = 0, eval_local = -2;
         int st = load_stencil(P, e, w, lane, &es, &eval_local);
         if (st != 0) {
@@ -275,11 +283,22 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
         // and rhs = b - A32 x0, formed here from the FP32 rows while they are still unfactored
         float rhs[ROWS][R];
         if (P.seed) {
-            for (int t = lane; t < N * R; t += 32) {
-                const int i = t / R;
-                const float sv = i < P.k ? __ldg(&P.seed[e * P.k + i]) : 0.0f;
-                xs[t] = sv;
-                u.x[t] = widen(sv);
+            if constexpr (R == 1) {
+#pragma unroll
+                for (int s = 0; s < ROWS; s++) {
+                    const int t = lane + 32 * s;
+                    if (t < N) {
+                        xs[t] = seed_reg[s];
+                        u.x[t] = widen(seed_reg[s]);
+                    }
+                }
+            } else {
+                for (int t = lane; t < N * R; t += 32) {
+                    const int i = t / R;
+                    const float sv = i < P.k ? __ldg(&P.seed[e * P.k + i]) : 0.0f;
+                    xs[t] = sv;
+                    u.x[t] = widen(sv);
+                }
             }
             __syncwarp();
 #pragma unroll
