@@ -268,7 +268,11 @@ __device__ __forceinline__ float trunc_to_float(double d) {
 // the bf16 result (the FP64 pipe of this part is ~70x slower than FP32).
 __global__ void features_kernel(const double *__restrict__ data, const double *__restrict__ eval, int dim,
                                 const int32_t *__restrict__ adjl, int64_t ne, int k, __nv_bfloat16 *__restrict__ out,
-                                int ldo) {
+                                int ldo, int ldo_pad, int vec) {
+    // each warp assembles its stencil's row in shared memory and writes it with 16-byte
+    // stores (the per-lane offsets are 2-6 bytes wide and would scatter into many pieces)
+    extern __shared__ __align__(16) __nv_bfloat16 fbuf[];
+    __nv_bfloat16 *buf = fbuf + (size_t)(threadIdx.x >> 5) * ldo_pad;
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; e < ne; e += nw) {
@@ -296,15 +300,23 @@ __global__ void features_kernel(const double *__restrict__ data, const double *_
         // 2^-es as an exact float (es within the normal range; otherwise ldexpf)
         const bool pow_ok = es > -126 && es < 127;
         const float sc = pow_ok ? __int_as_float((127 - es) << 23) : 1.0f;
-        __nv_bfloat16 *row = out + (size_t)e * ldo;
 #pragma unroll
         for (int s = 0; s < 2; s++) {
             const int i = lane + 32 * s;
             if (i < k)
                 for (int d = 0; d < dim; d++)
-                    row[i * dim + d] = __float2bfloat16_rn(pow_ok ? dv[s][d] * sc : ldexpf(dv[s][d], -es));
+                    buf[i * dim + d] = __float2bfloat16_rn(pow_ok ? dv[s][d] * sc : ldexpf(dv[s][d], -es));
         }
-        for (int c = k * dim + lane; c < ldo; c += 32) row[c] = __float2bfloat16_rn(0.0f);
+        for (int c = k * dim + lane; c < ldo; c += 32) buf[c] = __float2bfloat16_rn(0.0f);
+        __syncwarp();
+        __nv_bfloat16 *row = out + (size_t)e * ldo;
+        if (vec) {
+            for (int u = lane; u < ldo / 8; u += 32)
+                reinterpret_cast<uint4 *>(row)[u] = reinterpret_cast<const uint4 *>(buf)[u];
+        } else {
+            for (int c = lane; c < ldo; c += 32) row[c] = buf[c];
+        }
+        __syncwarp();
     }
 }
 }  // namespace
@@ -312,14 +324,21 @@ __global__ void features_kernel(const double *__restrict__ data, const double *_
 extern "C" int rbf_mlp_features(rbf_ctx *ctx, const double *data, int64_t n_data, const double *eval, int32_t dim,
                                 const int32_t *adjl, int64_t ne, int32_t k, void *out, int32_t ldo) {
     if (!ctx) return RBF_ERR_ARGUMENT;
-    if (dim < 1 || dim > 3 || k < 1 || k > 64 || ldo < k * dim || ne < 0 || n_data < 1 || n_data > INT32_MAX)
-        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "features: need 1 <= dim <= 3, 1 <= k <= 64, ldo >= k*dim, n_data >= 1");
+    if (dim < 1 || dim > 3 || k < 1 || k > 64 || ldo < k * dim || ldo > 4096 || ne < 0 || n_data < 1 ||
+        n_data > INT32_MAX)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT,
+                        "features: need 1 <= dim <= 3, 1 <= k <= 64, k*dim <= ldo <= 4096, n_data >= 1");
     if (ne == 0) return RBF_OK;
     bool idx_ok = false;
     RBF_TRY(rbf_check_indices(ctx, adjl, ne * (int64_t)k, (int32_t)n_data, &idx_ok));
     if (!idx_ok) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "features: a neighbour index is outside [0, n_data)");
     const int64_t blocks = std::min<int64_t>((ne + 7) / 8, (int64_t)ctx->num_sms * 32);
-    features_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(data, eval, dim, adjl, ne, k, (__nv_bfloat16 *)out, ldo);
+    const int ldo_pad = (ldo + 7) & ~7;
+    const int vec = (ldo % 8 == 0 && ((uintptr_t)out & 15) == 0) ? 1 : 0;
+    const size_t smem = sizeof(__nv_bfloat16) * 8 * (size_t)ldo_pad;
+    if (smem > 48 * 1024) RBF_CUDA(ctx, cudaFuncSetAttribute(features_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    features_kernel<<<(unsigned)blocks, 256, smem, ctx->stream>>>(data, eval, dim, adjl, ne, k, (__nv_bfloat16 *)out, ldo,
+                                                                  ldo_pad, vec);
     RBF_CHECK_LAUNCH(ctx);
     return RBF_OK;
 }
