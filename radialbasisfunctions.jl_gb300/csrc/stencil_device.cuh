@@ -349,11 +349,17 @@ __device__ __forceinline__ dfl df_sqr(dfl a) {
     e = fmaf(2.0f * a.hi, a.lo, e);
     return qts(p, e);
 }
+// Heron/Newton from the hardware reciprocal square root: one FP32 step brings s to about
+// one ulp of sqrt(hi), the double-float step to ~2^-46 relative; 1/(2s) enters only the
+// correction terms, where the approximate reciprocal's error is second order.
 __device__ __forceinline__ dfl df_sqrt(dfl a) {
-    if (!(a.hi > 0.0f)) return {0.0f, 0.0f};
-    float s = sqrtf(a.hi);
-    float e = fmaf(-s, s, a.hi) + a.lo;
-    return qts(s, e * (0.5f / s));
+    const float rs = rsqrtf(a.hi);
+    const float h = 0.5f * rs;
+    float s = a.hi * rs;
+    s = fmaf(fmaf(-s, s, a.hi), h, s);
+    const float e = fmaf(-s, s, a.hi) + a.lo;
+    const dfl r = qts(s, e * h);
+    return a.hi > 0.0f ? r : dfl{0.0f, 0.0f};
 }
 // float -> double by rebuilding the bit pattern on the integer pipe (normal floats and
 // zero; subnormal floats, far below any entry scale here, map to zero)

@@ -65,14 +65,14 @@ __device__ inline RegSmem carve_reg(char *base, int n, int k, int nops) {
 }
 
 // double -> float on the integer pipe, mantissa truncated (the FP32 factor only needs
-// FP32 accuracy); magnitudes below FLT_MIN map to zero
+// FP32 accuracy): the exponent is rebased and the top 23 mantissa bits taken in one funnel
+// shift; magnitudes below FLT_MIN map to a signed zero (the entries here are bounded, so
+// there is no overflow case)
 __device__ __forceinline__ float narrow(double d) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-    const unsigned sign = (unsigned)(b >> 63) << 31;
-    const int e = (int)((b >> 52) & 0x7ffu) - 1023 + 127;
-    if (e <= 0) return __uint_as_float(sign);
-    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
-    return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned mag = __funnelshift_l(lo, hi - 0x38000000u, 3);
+    return __uint_as_float((hi & 0x7fffffffu) < 0x38100000u ? sign : (sign | mag));
 }
 
 template <int N, int R>
@@ -82,15 +82,6 @@ struct RegLU {
     float a[ROWS][W];
     int step[ROWS];  // elimination step at which the row was the pivot; N+1: not yet; -1: padding
 };
-
-template <int N, int R>
-__device__ __forceinline__ float pick(const RegLU<N, R> &L, int s, int cc) {
-    float v = L.a[0][cc];
-#pragma unroll
-    for (int t = 1; t < RegLU<N, R>::ROWS; t++)
-        if (s == t) v = L.a[t][cc];
-    return v;
-}
 
 // Compile-time loop: f(std::integral_constant<int, I>) for I = B, B+S, ... while I != E.
 template <int I, int E, int S, class F>
@@ -120,18 +111,21 @@ __device__ bool reglu_factor(RegLU<N, R> &L, float *rowbuf, int *piv, float *rcp
         key = __reduce_max_sync(0xffffffffu, key);
         const int brow = 63 - (int)(key & 63u);
         const int pl = brow & 31, ps = brow >> 5;
-        if (lane == pl) {
+        // the slot ps is the same in every lane: one branch per slot publishes the row
+        // straight from its registers
 #pragma unroll
-            for (int s = 0; s < ROWS; s++)
-                if (s == ps) L.step[s] = c;
+        for (int s = 0; s < ROWS; s++) {
+            if (s == ps && lane == pl) {
+                L.step[s] = c;
 #pragma unroll
-            for (int q4 = c / 4; q4 < (W + 3) / 4; q4++) {
-                float4 v;
-                v.x = (4 * q4 + 0 < W) ? pick(L, ps, (4 * q4 + 0 < W) ? 4 * q4 + 0 : 0) : 0.0f;
-                v.y = (4 * q4 + 1 < W) ? pick(L, ps, (4 * q4 + 1 < W) ? 4 * q4 + 1 : 0) : 0.0f;
-                v.z = (4 * q4 + 2 < W) ? pick(L, ps, (4 * q4 + 2 < W) ? 4 * q4 + 2 : 0) : 0.0f;
-                v.w = (4 * q4 + 3 < W) ? pick(L, ps, (4 * q4 + 3 < W) ? 4 * q4 + 3 : 0) : 0.0f;
-                reinterpret_cast<float4 *>(rowbuf)[q4] = v;
+                for (int q4 = c / 4; q4 < (W + 3) / 4; q4++) {
+                    float4 v;
+                    v.x = (4 * q4 + 0 < W) ? L.a[s][(4 * q4 + 0 < W) ? 4 * q4 + 0 : 0] : 0.0f;
+                    v.y = (4 * q4 + 1 < W) ? L.a[s][(4 * q4 + 1 < W) ? 4 * q4 + 1 : 0] : 0.0f;
+                    v.z = (4 * q4 + 2 < W) ? L.a[s][(4 * q4 + 2 < W) ? 4 * q4 + 2 : 0] : 0.0f;
+                    v.w = (4 * q4 + 3 < W) ? L.a[s][(4 * q4 + 3 < W) ? 4 * q4 + 3 : 0] : 0.0f;
+                    reinterpret_cast<float4 *>(rowbuf)[q4] = v;
+                }
             }
         }
         __syncwarp();
