@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
               "-Xptxas", "-warn-spills"]
 
 SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "stencil_build.cu", "stencil_refined_a.cu",
-           "stencil_refined_b.cu", "batched.cu", "plan.cu", "reorder.cu", "diag.cu", "mlp.cu",
+           "stencil_refined_b.cu", "stencil_refined_c.cu", "batched.cu", "plan.cu", "reorder.cu", "diag.cu", "mlp.cu",
            "mlp_tc.cu"]
 
 

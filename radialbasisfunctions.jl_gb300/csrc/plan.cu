@@ -21,6 +21,7 @@ struct rbf_plan {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     void *counters = nullptr;  // the build's counters (device), reset inside the graph
+    void *defer = nullptr;     // room for the stencils the FP32 path hands to its second kernel
     cudaStream_t capture = nullptr;
 };
 
@@ -99,7 +100,9 @@ int rbf_plan_create(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, 
     pl->ctx = ctx;
     cudaError_t e = cudaStreamCreateWithFlags(&pl->capture, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&pl->counters, sizeof(unsigned long long) * 8 + sizeof(double));
+    if (e == cudaSuccess && cfg->precision != RBF_PREC_FP64) e = cudaMalloc(&pl->defer, sizeof(int32_t) * (size_t)ne);
     if (e != cudaSuccess) {
+        if (pl->counters) cudaFree(pl->counters);
         if (pl->capture) cudaStreamDestroy(pl->capture);
         delete pl;
         return rbf_fail(ctx, RBF_ERR_CUDA, "plan allocation failed: %s", cudaGetErrorString(e));
@@ -115,6 +118,7 @@ int rbf_plan_create(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, 
     P.val = val;
     P.counters = static_cast<unsigned long long *>(pl->counters);
     P.max_resid = reinterpret_cast<double *>(static_cast<unsigned long long *>(pl->counters) + 8);
+    P.defer = static_cast<int32_t *>(pl->defer);
     const int st = plan_capture(pl, P, cfg->precision, row_ptr, col, val + (size_t)op_index * nnz, ne, ns, x, y);
     if (st != RBF_OK) {
         rbf_plan_destroy(pl);
@@ -150,6 +154,7 @@ int rbf_plan_destroy(rbf_plan *pl) {
     if (pl->exec) cudaGraphExecDestroy(pl->exec);
     if (pl->graph) cudaGraphDestroy(pl->graph);
     if (pl->counters) cudaFree(pl->counters);
+    if (pl->defer) cudaFree(pl->defer);
     if (pl->capture) cudaStreamDestroy(pl->capture);
     delete pl;
     return RBF_OK;

@@ -407,6 +407,11 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
     P.tol = cfg->tol > 0 ? cfg->tol : 1e-9;
     P.flags = cfg->flags;
     P.seed = cfg->seed;
+    DevBuf defer;
+    if (cfg->precision != RBF_PREC_FP64) {
+        RBF_TRY(defer.alloc(ctx, sizeof(int32_t) * (size_t)ne));
+        P.defer = defer.as<int32_t>();
+    }
     if (cfg->precision == RBF_PREC_LEARNED) {
         if (!cfg->seed || !rbf_is_device_ptr(cfg->seed))
             return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the learned build needs a device pointer to the predicted weights");

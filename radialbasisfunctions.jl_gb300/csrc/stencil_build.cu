@@ -26,6 +26,7 @@
 #define RBF_LAUNCH_NO_VARIANT 1000
 int rbf_launch_refined_reg_a(rbf_ctx *ctx, const StencilParams &P);
 int rbf_launch_refined_reg_b(rbf_ctx *ctx, const StencilParams &P);
+int rbf_launch_refined_split(rbf_ctx *ctx, const StencilParams &P);
 
 namespace {
 
@@ -45,6 +46,34 @@ __global__ void build_fp32r_kernel(StencilParams P, int wpb, size_t warp_bytes) 
     Warp32 u = carve32(base, P.n, P.k, P.nops);
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
     for (int64_t e = (int64_t)blockIdx.x * wpb + wib; e < P.ne; e += nwarps) solve_fp32r_warp(P, e, w, u, lane);
+}
+
+// Stencils the split-row kernel handed over (boundary stencils, failed refinements): the
+// general refined solve with its FP64 fallback.  The count is read on the device, so the
+// launch needs no host synchronisation (and can be captured in a graph).
+__global__ void build_deferred_kernel(StencilParams P, int wpb, size_t warp_bytes) {
+    extern __shared__ __align__(16) char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    char *base = smem + wib * warp_bytes;
+    WarpSmem w = carve(base, P.n, P.k, P.nops);
+    Warp32 u = carve32(base, P.n, P.k, P.nops);
+    const int64_t count = (int64_t)*reinterpret_cast<volatile unsigned long long *>(&P.counters[7]);
+    const int64_t nwarps = (int64_t)gridDim.x * wpb;
+    for (int64_t t = (int64_t)blockIdx.x * wpb + wib; t < count; t += nwarps) solve_fp32r_warp(P, P.defer[t], w, u, lane);
+}
+
+int launch_deferred(rbf_ctx *ctx, const StencilParams &P) {
+    const size_t wb = warp_smem_bytes32(P.n, P.k, P.nops);
+    int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (100 * 1024) / wb));
+    size_t smem = wb * wpb;
+    RBF_CUDA(ctx, cudaFuncSetAttribute(build_deferred_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    RBF_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, build_deferred_kernel, wpb * 32, smem));
+    if (per_sm < 1) per_sm = 1;
+    int64_t blocks = std::min<int64_t>((P.ne + wpb - 1) / wpb, (int64_t)ctx->num_sms * per_sm);
+    build_deferred_kernel<<<(unsigned)blocks, wpb * 32, smem, ctx->stream>>>(P, wpb, wb);
+    RBF_CHECK_LAUNCH(ctx);
+    return RBF_OK;
 }
 
 }  // namespace
@@ -68,6 +97,15 @@ int rbf_build_fp64_launch(rbf_ctx *ctx, const StencilParams &P) {
 
 int rbf_build_fp32_launch(rbf_ctx *ctx, const StencilParams &P) {
     if (P.ne == 0) return RBF_OK;
+    // 33..40-row single-operator systems: the split-row kernel on the interior stencils,
+    // then the general kernel on the ones it deferred
+    if (P.defer) {
+        const int st = rbf_launch_refined_split(ctx, P);
+        if (st != RBF_LAUNCH_NO_VARIANT) {
+            if (st != RBF_OK) return st;
+            return launch_deferred(ctx, P);
+        }
+    }
     // register-resident kernels for the standard system sizes (they need 3k >= n for the
     // reciprocal-pivot buffer that reuses the split-coordinate space)
     if (3 * P.k >= P.n) {

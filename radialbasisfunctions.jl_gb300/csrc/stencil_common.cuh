@@ -45,13 +45,15 @@ struct StencilParams {
     unsigned long long *counters;  // [0] singular [1] eval-not-found [2] fallback [3] identity rows
                                    // [4] FP64 residual evaluations (FP32 paths)
                                    // [5] sum of 1e6 * min(1, |x1 - seed| / |x1|) over seeded
-                                   //     stencils, [6] their number
+                                   //     stencils, [6] their number, [7] deferred stencils
     double *max_resid;             // largest accepted relative residual (FP32 paths)
     int refine_steps;
     double tol;
     int flags;          // RBF_FLAG_*
     const float *seed;  // learned seed (ne x k, stencil order, local units) or nullptr
     const int64_t *adj_ptr;  // ragged adjacency: neighbours of e at adjl[adj_ptr[e] ..], or nullptr
+    int32_t *defer;          // FP32 paths: room for ne stencil indices that the split-row kernel
+                             // hands to the general kernel (count in counters[7]), or nullptr
 };
 
 // One size class (stencil size k, polynomial degree) of a batched build of uneven stencils.

@@ -1,0 +1,448 @@
+// Split-row register refined build for systems of 33..40 rows with one operator (the
+// k = 30, degree-2 stencils of the 3D workloads: 40 x 40 systems).
+//
+// The register kernel of stencil_refined_reg.cuh gives every lane two full rows, so for
+// n = 40 the second row slot holds real rows in 8 lanes only: 80 registers of matrix per
+// lane, a third of the elimination FMAs on padding, and (with the full FP64 system of
+// 13 KB per warp in shared memory) 12 resident warps per SM.  Here
+//   * rows 0..31 ("main" rows) stay one per lane, in registers;
+//   * rows 32..n-1 ("extra" rows) are cut into 4 pieces of ceil(n/4) columns, and lane
+//     l holds piece l & 3 of extra row 32 + (l >> 2): 50 registers of matrix for n = 40,
+//     every lane doing useful work in the extra-row updates;
+//   * the FP64 system in shared memory is the packed lower triangle (A is symmetric) and
+//     the right-hand side: 6.9 KB instead of 13.1 KB per warp;
+//   * interior stencils only.  Stencils with a boundary point (Hermite rows) and the rare
+//     stencil whose refinement fails go to a list that the general refined kernel
+//     (FP32 factor, FP64 refinement, FP64 fallback) finishes in a second launch.
+// Together: 16 resident warps per SM.  The elimination, the substitutions and the
+// acceptance rule are those of the register kernel (pivot choice by magnitude, ties to
+// the lower row); multipliers of an extra row reach the lanes that need them by shuffle
+// within the row's group of four lanes.
+#pragma once
+#include "stencil_refined_reg.cuh"
+
+namespace {
+
+// lower triangle by rows: A(i, j), j <= i, at tri(i) + j
+__host__ __device__ constexpr int tri(int i) { return (i * (i + 1)) >> 1; }
+
+template <int N>
+struct SplitLU {
+    static constexpr int NX = N - 32;        // extra rows
+    static constexpr int PW = (N + 3) / 4;   // columns per piece
+    float a[N];                              // main row: lane
+    float b[PW];                             // piece (lane & 3) of extra row 32 + (lane >> 2)
+    int mstep, xstep;  // step at which the row was the pivot; N + 1: not yet; -1: padding
+};
+
+// Shared memory of one warp: packed FP64 system and right-hand side, local coordinates and
+// column indices, FP64 solution, FP32 increments, split coordinates, pivots, reciprocal
+// pivots and the pivot-row buffer (16-byte aligned, 4 * ceil(n/4) floats).
+struct SplitSmem {
+    double *Mp, *bv, *X, *x;
+    int *cols, *piv;
+    float *xs, *XH, *XL, *rcp, *rowbuf;
+};
+
+__host__ __device__ inline size_t split_smem_bytes(int n, int k) {
+    size_t b = sizeof(double) * ((size_t)tri(n) + 2 * (size_t)n + 3 * (size_t)k);
+    b += sizeof(int) * ((size_t)k + n) + sizeof(float) * ((size_t)n + 6 * (size_t)k + n);
+    b = (b + 15) & ~(size_t)15;
+    b += sizeof(float) * 4 * (((size_t)n + 3) / 4);
+    return (b + 15) & ~(size_t)15;
+}
+
+__device__ inline SplitSmem carve_split(char *base, int n, int k) {
+    SplitSmem s;
+    double *d = reinterpret_cast<double *>(base);
+    s.Mp = d;
+    s.bv = s.Mp + tri(n);
+    s.X = s.bv + n;
+    s.x = s.X + 3 * k;
+    s.cols = reinterpret_cast<int *>(s.x + n);
+    s.piv = s.cols + k;
+    s.xs = reinterpret_cast<float *>(s.piv + n);
+    s.XH = s.xs + n;
+    s.XL = s.XH + 3 * k;
+    s.rcp = s.XL + 3 * k;
+    size_t o = (size_t)(reinterpret_cast<char *>(s.rcp + n) - base);
+    s.rowbuf = reinterpret_cast<float *>(base + ((o + 15) & ~(size_t)15));
+    return s;
+}
+
+// Column indices and local coordinates (scaled by 2^-es, as load_stencil) of stencil e.
+// Returns 1 without scaling when a boundary point is in the stencil: such stencils are
+// deferred to the general kernel.
+__device__ int load_interior(const StencilParams &P, int64_t e, const SplitSmem &s, int lane, int *es_out) {
+    const int k = P.k, dim = P.dim;
+    double x0[3] = {0, 0, 0};
+    for (int d = 0; d < dim; d++) x0[d] = P.eval[e * dim + d];
+    double r2max = 0.0;
+    bool anyb = false;
+    const int32_t *nbr = P.adj_ptr ? P.adjl + P.adj_ptr[e] : P.adjl + e * k;
+    for (int i = lane; i < k; i += 32) {
+        const int g = nbr[i];
+        s.cols[i] = g;
+        double r2 = 0.0;
+        for (int d = 0; d < 3; d++) {
+            const double dd = d < dim ? P.data[(int64_t)g * dim + d] - x0[d] : 0.0;
+            s.X[i * 3 + d] = dd;
+            r2 += dd * dd;
+        }
+        r2max = fmax(r2max, r2);
+        if (P.isb) anyb |= (P.isb[g] != 0);
+    }
+    if (__any_sync(0xffffffffu, anyb)) return 1;
+    for (int o = 16; o > 0; o >>= 1) r2max = fmax(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
+    int es = 0;
+    if (r2max > 0.0) frexp(sqrt(r2max), &es);
+    *es_out = es;
+    __syncwarp();
+    for (int i = lane; i < k; i += 32)
+        for (int d = 0; d < dim; d++) s.X[i * 3 + d] = ldexp(s.X[i * 3 + d], -es);
+    __syncwarp();
+    return 0;
+}
+
+// [Phi P; P^T 0] of an interior stencil in double-float (the arithmetic of
+// assemble_refined), stored as the packed lower triangle, and the right-hand side.
+__device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int lane, int es, const uint16_t *pairs) {
+    const int k = P.k, n = P.n, dim = P.dim, nmon = P.nmon;
+    for (int i = lane; i < k; i += 32)
+        for (int d = 0; d < 3; d++) {
+            const double xv = d < dim ? s.X[i * 3 + d] : 0.0;
+            const float hi = __double2float_rn(xv);
+            s.XH[i * 3 + d] = hi;
+            s.XL[i * 3 + d] = __double2float_rn(xv - widen(hi));
+        }
+    for (int t = lane; t < tri(n) - tri(k); t += 32) s.Mp[tri(k) + t] = 0.0;  // rows k..n-1; the
+    __syncwarp();                                                           // P^T part is set below
+    const int npairs = k * (k + 1) / 2;
+    for (int p = lane; p < npairs; p += 32) {
+        const unsigned pk = pairs[p];
+        const int i = (int)(pk & 0xffu), j = (int)(pk >> 8);  // i <= j
+        dfl r2 = {0.0f, 0.0f};
+        for (int d = 0; d < dim; d++) {
+            dfl dd = ts(s.XH[i * 3 + d], -s.XH[j * 3 + d]);
+            dd = qts(dd.hi, dd.lo + (s.XL[i * 3 + d] - s.XL[j * 3 + d]));
+            r2 = df_add(r2, df_sqr(dd));
+        }
+        const dfl r = df_sqrt(r2);
+        dfl phi;
+        switch (P.phs) {
+        case 1: phi = r; break;
+        case 3: phi = df_mul(r2, r); break;
+        case 5: phi = df_mul(df_sqr(r2), r); break;
+        default: phi = df_mul(df_mul(df_sqr(r2), r2), r); break;
+        }
+        s.Mp[tri(j) + i] = df_to_double(phi);
+    }
+    const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
+    for (int i = lane; i < k; i += 32) {
+        dfl xd[3];
+        for (int d = 0; d < 3; d++) xd[d] = {s.XH[i * 3 + d], s.XL[i * 3 + d]};
+        for (int m = 0; m < nmon; m++) {
+            dfl v = {1.0f, 0.0f};
+            for (int d = 0; d < dim; d++)
+                for (int t = 0; t < P.exps[m][d]; t++) v = df_mul(v, xd[d]);
+            s.Mp[tri(k + m) + i] = df_to_double(v);
+        }
+        double D[3];
+        for (int d = 0; d < dim; d++) D[d] = -s.X[i * 3 + d];
+        s.bv[i] = phs_op<double>(P.phs, P.op_code[0], P.op_dim[0], D, dim, AI);
+    }
+    for (int m = lane; m < nmon; m += 32) s.bv[k + m] = mono_op_at_origin(P, m, P.op_code[0], P.op_dim[0]);
+    __syncwarp();
+}
+
+// A(i, j) of the packed symmetric system
+__device__ __forceinline__ double pk_at(const double *Mp, int i, int j) {
+    return Mp[i >= j ? tri(i) + j : tri(j) + i];
+}
+
+template <int N>
+__device__ __forceinline__ void split_defer(const StencilParams &P, int64_t e, int lane) {
+    if (lane == 0) {
+        const unsigned long long t = atomicAdd(&P.counters[7], 1ull);
+        P.defer[t] = (int32_t)e;
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilParams P, int wpb, size_t warp_bytes) {
+    using LU = SplitLU<N>;
+    constexpr int NX = LU::NX, PW = LU::PW;
+    static_assert(NX >= 1 && NX <= 8, "split layout: 33..40 rows");
+    static_assert(PW % 2 == 0, "pieces are published as float2");
+    extern __shared__ __align__(16) char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const SplitSmem s = carve_split(smem + wib * warp_bytes, N, P.k);
+    uint16_t *pairs = reinterpret_cast<uint16_t *>(smem + wpb * warp_bytes);
+    for (int p = threadIdx.x; p < P.k * (P.k + 1) / 2; p += blockDim.x) {
+        int j = 0;
+        while ((j + 1) * (j + 2) / 2 <= p) j++;
+        pairs[p] = (uint16_t)((p - j * (j + 1) / 2) | (j << 8));
+    }
+    __syncthreads();
+    const int g = lane >> 2, q = lane & 3;
+    const bool xvalid = g < NX;
+    const int gx = 32 + (xvalid ? g : 0);  // extra row of this lane's group
+    const int64_t nwarps = (int64_t)gridDim.x * wpb;
+    for (int64_t e = (int64_t)blockIdx.x * wpb + wib; e < P.ne; e += nwarps) {
+        // a learned seed is read first so that its latency hides behind the load and assembly
+        const float seed_main = (P.seed && lane < P.k) ? __ldg(&P.seed[e * P.k + lane]) : 0.0f;
+        const float seed_x = (P.seed && lane < NX && 32 + lane < P.k) ? __ldg(&P.seed[e * P.k + 32 + lane]) : 0.0f;
+        int es = 0;
+        if (load_interior(P, e, s, lane, &es) != 0) {
+            split_defer<N>(P, e, lane);
+            __syncwarp();
+            continue;
+        }
+        assemble_packed(P, s, lane, es, pairs);
+        LU L;
+        const int ti = tri(lane);
+#pragma unroll
+        for (int cc = 0; cc < N; cc++) L.a[cc] = narrow(s.Mp[cc > lane ? tri(cc) + lane : ti + cc]);
+#pragma unroll
+        for (int t = 0; t < PW; t++) {
+            const int col = q * PW + t;
+            L.b[t] = (xvalid && col < N) ? narrow(pk_at(s.Mp, gx, col < N ? col : 0)) : 0.0f;
+        }
+        L.mstep = N + 1;
+        L.xstep = xvalid ? N + 1 : -1;
+        // start of the refinement: x0 = 0 and rhs = b, or with a learned seed x0 = [w_pred; 0]
+        // and rhs = b - A32 x0, formed from the FP32 rows before they are factorised
+        float rm = narrow(s.bv[lane]);
+        float rx = xvalid ? narrow(s.bv[gx]) : 0.0f;
+        if (P.seed) {
+            s.xs[lane] = seed_main;
+            s.x[lane] = widen(seed_main);
+            if (lane < NX) {
+                s.xs[32 + lane] = seed_x;
+                s.x[32 + lane] = widen(seed_x);
+            }
+            __syncwarp();
+            float am = 0.0f, ax = 0.0f;
+#pragma unroll
+            for (int j = 0; j < N; j++) am = fmaf(L.a[j], s.xs[j], am);
+#pragma unroll
+            for (int t = 0; t < PW; t++) ax = fmaf(L.b[t], s.xs[q * PW + t < N ? q * PW + t : 0], ax);  // b = 0 past N
+            ax += __shfl_xor_sync(0xffffffffu, ax, 1);
+            ax += __shfl_xor_sync(0xffffffffu, ax, 2);
+            rm -= am;
+            rx = xvalid ? rx - ax : 0.0f;
+        } else {
+            s.x[lane] = 0.0;
+            if (lane < NX) s.x[32 + lane] = 0.0;
+        }
+        __syncwarp();
+
+        // ---- FP32 LU with partial pivoting, rows in place
+        bool ok = true;
+        static_for<0, N, 1>([&](auto cI) {
+            constexpr int c = decltype(cI)::value;
+            constexpr int qc = c / PW, tc = c % PW;
+            const unsigned km = L.mstep == N + 1
+                                    ? (__float_as_uint(fabsf(L.a[c])) & ~63u) | (unsigned)(63 - lane) : 0u;
+            const unsigned kx = (L.xstep == N + 1 && q == qc)
+                                    ? (__float_as_uint(fabsf(L.b[tc])) & ~63u) | (unsigned)(63 - gx) : 0u;
+            const unsigned key = __reduce_max_sync(0xffffffffu, max(km, kx));
+            const int brow = 63 - (int)(key & 63u);
+            if (brow < 32) {  // the same in every lane
+                if (lane == brow) {
+                    L.mstep = c;
+#pragma unroll
+                    for (int q4 = c / 4; q4 < (N + 3) / 4; q4++) {
+                        float4 v;
+                        v.x = L.a[4 * q4 + 0 < N ? 4 * q4 + 0 : 0];
+                        v.y = 4 * q4 + 1 < N ? L.a[4 * q4 + 1 < N ? 4 * q4 + 1 : 0] : 0.0f;
+                        v.z = 4 * q4 + 2 < N ? L.a[4 * q4 + 2 < N ? 4 * q4 + 2 : 0] : 0.0f;
+                        v.w = 4 * q4 + 3 < N ? L.a[4 * q4 + 3 < N ? 4 * q4 + 3 : 0] : 0.0f;
+                        reinterpret_cast<float4 *>(s.rowbuf)[q4] = v;
+                    }
+                }
+            } else if (gx == brow && xvalid) {  // the four lanes of the pivot's group
+                L.xstep = c;
+#pragma unroll
+                for (int t = 0; t < PW; t += 2)
+                    reinterpret_cast<float2 *>(s.rowbuf)[(q * PW + t) >> 1] =
+                        make_float2(L.b[t], t + 1 < PW ? L.b[t + 1 < PW ? t + 1 : 0] : 0.0f);
+            }
+            __syncwarp();
+            const float pvt = s.rowbuf[c];
+            ok &= (pvt != 0.0f) && isfinite(pvt);
+            const float inv = __frcp_rn(pvt);
+            if (lane == 0) {
+                s.piv[c] = brow;
+                s.rcp[c] = inv;
+            }
+            // main rows: multiplier into column c, update of columns c+1..N-1 (rows already
+            // used as pivots get a zero multiplier)
+            {
+                const bool act = L.mstep == N + 1;
+                const float l = act ? L.a[c] * inv : 0.0f;
+                L.a[c] = act ? l : L.a[c];
+#pragma unroll
+                for (int q4 = (c + 1) / 4; q4 < (N + 3) / 4; q4++) {
+                    const float4 v = reinterpret_cast<const float4 *>(s.rowbuf)[q4];
+                    const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int t = 0; t < 4; t++) {
+                        const int cc = 4 * q4 + t;
+                        if (cc > c && cc < N) L.a[cc < N ? cc : 0] = fmaf(-l, vv[t], L.a[cc < N ? cc : 0]);
+                    }
+                }
+            }
+            // extra rows: the lane holding column c computes the multiplier, its group gets
+            // it by shuffle; columns of the piece right of c are updated
+            {
+                const bool xact = L.xstep == N + 1;
+                float lx = __shfl_sync(0xffffffffu, L.b[tc] * inv, (lane & ~3) | qc);
+                lx = xact ? lx : 0.0f;
+                const bool right_hi = q >= qc, right_lo = q > qc;  // column q*PW+t > c
+#pragma unroll
+                for (int t = 0; t < PW; t += 2) {
+                    const float2 v = reinterpret_cast<const float2 *>(s.rowbuf)[(q * PW + t) >> 1];
+                    if (t > tc ? right_hi : right_lo) L.b[t] = fmaf(-lx, v.x, L.b[t]);
+                    if (t + 1 < PW && (t + 1 > tc ? right_hi : right_lo))
+                        L.b[t + 1 < PW ? t + 1 : 0] = fmaf(-lx, v.y, L.b[t + 1 < PW ? t + 1 : 0]);
+                }
+                if (q == qc && xact) L.b[tc] = lx;
+            }
+            __syncwarp();
+        });
+
+        // ---- refinement: solves with the register factors, FP64 residuals
+        bool accepted = false;
+        double est_final = 0.0;
+        int nres = 0;
+        if (ok) {
+            auto forward = [&]() {
+                static_for<0, N, 1>([&](auto cI) {
+                    constexpr int c = decltype(cI)::value;
+                    constexpr int qc = c / PW, tc = c % PW;
+                    const int p = s.piv[c];
+                    const float y = __shfl_sync(0xffffffffu, p < 32 ? rm : rx, p < 32 ? p : 4 * (p - 32));
+                    const float mx = __shfl_sync(0xffffffffu, L.b[tc], (lane & ~3) | qc);
+                    if (L.mstep > c) rm = fmaf(-L.a[c], y, rm);
+                    if (L.xstep > c) rx = fmaf(-mx, y, rx);
+                });
+            };
+            auto back = [&]() {
+                static_for<N - 1, -1, -1>([&](auto cI) {
+                    constexpr int c = decltype(cI)::value;
+                    constexpr int qc = c / PW, tc = c % PW;
+                    const int p = s.piv[c];
+                    const float xq =
+                        __shfl_sync(0xffffffffu, p < 32 ? rm : rx, p < 32 ? p : 4 * (p - 32)) * s.rcp[c];
+                    const float ux = __shfl_sync(0xffffffffu, L.b[tc], (lane & ~3) | qc);
+                    if (lane == 0) s.xs[c] = xq;
+                    if (L.mstep >= 0 && L.mstep < c) rm = fmaf(-L.a[c], xq, rm);
+                    if (L.xstep >= 0 && L.xstep < c) rx = fmaf(-ux, xq, rx);
+                });
+                __syncwarp();
+            };
+            // FP64 residual r = b - A x: rows 0..31 one per lane, rows 32..N-1 as (row, quarter
+            // of the columns) over the four lanes of the row's group, summed by shuffles
+            auto residual = [&]() {
+                nres++;
+                double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+#pragma unroll 1
+                for (int j = 0; j < (N & ~3); j += 4) {
+                    c0 = fma(-s.Mp[j + 0 > lane ? tri(j + 0) + lane : ti + j + 0], s.x[j + 0], c0);
+                    c1 = fma(-s.Mp[j + 1 > lane ? tri(j + 1) + lane : ti + j + 1], s.x[j + 1], c1);
+                    c2 = fma(-s.Mp[j + 2 > lane ? tri(j + 2) + lane : ti + j + 2], s.x[j + 2], c2);
+                    c3 = fma(-s.Mp[j + 3 > lane ? tri(j + 3) + lane : ti + j + 3], s.x[j + 3], c3);
+                }
+#pragma unroll
+                for (int j = N & ~3; j < N; j++) c0 = fma(-s.Mp[j > lane ? tri(j) + lane : ti + j], s.x[j], c0);
+                double ex = 0.0;
+                const int tg = tri(gx);
+#pragma unroll
+                for (int t = 0; t < PW; t++) {
+                    const int j = q * PW + t;
+                    if (j < N) ex = fma(-s.Mp[j <= gx ? tg + j : tri(j) + gx], s.x[j], ex);
+                }
+                ex += __shfl_xor_sync(0xffffffffu, ex, 1);
+                ex += __shfl_xor_sync(0xffffffffu, ex, 2);
+                rm = narrow(s.bv[lane] + ((c0 + c1) + (c2 + c3)));
+                rx = xvalid ? narrow(s.bv[gx] + ex) : 0.0f;
+            };
+            const float tolf = (float)P.tol;
+            float dprev = 0.0f;
+            for (int step = 0;; step++) {
+                forward();
+                back();
+                float dmaxf = 0.0f, xmaxf = 0.0f;
+                for (int t = lane; t < N; t += 32) {
+                    const float d = s.xs[t];
+                    s.x[t] += widen(d);
+                    if (t < P.k) {
+                        dmaxf = fmaxf(dmaxf, fabsf(d));
+                        xmaxf = fmaxf(xmaxf, fabsf(narrow(s.x[t])));
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    dmaxf = fmaxf(dmaxf, __shfl_xor_sync(0xffffffffu, dmaxf, o));
+                    xmaxf = fmaxf(xmaxf, __shfl_xor_sync(0xffffffffu, xmaxf, o));
+                }
+                __syncwarp();
+                if (step == 0) {
+                    // the first solve reaches the FP32 floor from any start; with a seed,
+                    // |d0| / |x| is the surrogate's error as judged by the solve
+                    if (P.seed && lane == 0 && xmaxf > 0.0f) {
+                        atomicAdd(&P.counters[5], (unsigned long long)(1e6f * fminf(1.0f, dmaxf / xmaxf)));
+                        atomicAdd(&P.counters[6], 1ull);
+                    }
+                    dprev = xmaxf;
+                } else {
+                    // contraction |d1| / |d0| past 1e-3: the stencil takes the general path;
+                    // accept once |d_s| is below tol relative to x and shrinking
+                    if (step == 1 && !(dmaxf <= 1e-3f * dprev)) break;
+                    if (dmaxf <= tolf * xmaxf && dmaxf <= 0.5f * dprev) {
+                        accepted = true;
+                        est_final = xmaxf > 0.0f ? (double)(dmaxf / xmaxf) : 0.0;
+                        break;
+                    }
+                    dprev = dmaxf;
+                }
+                if (step >= P.refine_steps || !isfinite(dmaxf)) break;
+                residual();
+            }
+        }
+        if (lane == 0 && ok) atomicAdd(&P.counters[4], (unsigned long long)nres);
+        if (accepted) {
+            WarpSmem w;
+            w.cols = s.cols;
+            scatter_row(P, e, w, lane, es, s.x, 1, 1);
+            if (lane == 0) {
+                if (P.status) P.status[e] = 0;
+                atomicMax(reinterpret_cast<unsigned long long *>(P.max_resid),
+                          (unsigned long long)__double_as_longlong(est_final));
+            }
+        } else {
+            split_defer<N>(P, e, lane);
+        }
+        __syncwarp();
+    }
+}
+
+template <int N>
+int launch_refined_split(rbf_ctx *ctx, const StencilParams &P) {
+    const size_t wb = split_smem_bytes(N, P.k);
+    const int wpb = 4;
+    const size_t smem = wb * wpb + sizeof(uint16_t) * (size_t)(P.k * (P.k + 1) / 2);
+    RBF_CUDA(ctx, cudaFuncSetAttribute(build_refined_split_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    int per_sm = 0;
+    RBF_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, build_refined_split_kernel<N>, wpb * 32,
+                                                                smem));
+    if (per_sm < 1) per_sm = 1;
+    const int64_t blocks = std::min<int64_t>((P.ne + wpb - 1) / wpb, (int64_t)ctx->num_sms * per_sm);
+    build_refined_split_kernel<N><<<(unsigned)blocks, wpb * 32, smem, ctx->stream>>>(P, wpb, wb);
+    RBF_CHECK_LAUNCH(ctx);
+    return RBF_OK;
+}
+
+}  // namespace
