@@ -55,7 +55,7 @@ PEAKS = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.ex
 
 # DRAM bytes (read + write) per stencil of the headline build kernel, from one ncu capture of
 # that kernel at N = 1,000,000 (3D Laplacian, k = 30); traffic grows with the stencil count.
-KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": 481.4}
+KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": 481.4, "learned": 611.9}
 
 
 def peaks_bf16():
@@ -403,7 +403,8 @@ def main():
     flops_stencil = nsys ** 3 / 3 + 2 * nsys ** 2 * R + 10 * (k * (k + 1) / 2 + R * k)
     ms_kernel = float(st_h.ms_build)
     ach = flops_stencil * n / (ms_kernel * 1e-3) / 1e12
-    kname = f"build_refined_reg_kernel<{nsys},{R}>" + (" (learned seed)" if learned_on else "")
+    kbase = f"build_refined_split_kernel<{nsys}>" if (33 <= nsys <= 40 and R == 1) else f"build_refined_reg_kernel<{nsys},{R}>"
+    kname = kbase + (" (learned seed)" if learned_on else "")
     roof = {"kernel": kname, "bound": "fp64 pipe", "achieved": ach, "peak": fp64_peak.value, "unit": "TFLOP/s",
             "frac": ach / fp64_peak.value, "traffic": KERNEL_TRAFFIC_PER_STENCIL.get(headline, 0) * n or None,
             "flops": f"reference FP64 algorithm count per stencil ({flops_stencil:.0f}: n^3/3 + 2n^2R + assembly)",

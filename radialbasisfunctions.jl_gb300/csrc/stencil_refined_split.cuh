@@ -37,7 +37,7 @@ struct SplitLU {
 
 // Shared memory of one warp: packed FP64 system and right-hand side, local coordinates and
 // column indices, FP64 solution, FP32 increments, split coordinates, pivots, reciprocal
-// pivots and the pivot-row buffer (16-byte aligned, 4 * ceil(n/4) floats).
+// pivots and two pivot-row buffers (16-byte aligned, 4 * ceil(n/4) floats each).
 struct SplitSmem {
     double *Mp, *bv, *X, *x;
     int *cols, *piv;
@@ -48,7 +48,7 @@ __host__ __device__ inline size_t split_smem_bytes(int n, int k) {
     size_t b = sizeof(double) * ((size_t)tri(n) + 2 * (size_t)n + 3 * (size_t)k);
     b += sizeof(int) * ((size_t)k + n) + sizeof(float) * ((size_t)n + 6 * (size_t)k + n);
     b = (b + 15) & ~(size_t)15;
-    b += sizeof(float) * 4 * (((size_t)n + 3) / 4);
+    b += sizeof(float) * 8 * (((size_t)n + 3) / 4);  // two buffers, alternating by step
     return (b + 15) & ~(size_t)15;
 }
 
@@ -242,6 +242,9 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
         static_for<0, N, 1>([&](auto cI) {
             constexpr int c = decltype(cI)::value;
             constexpr int qc = c / PW, tc = c % PW;
+            // pivot-row buffers alternate by step: the publish of step c + 1 cannot overwrite
+            // the row that step c is still reading, so one warp barrier per step suffices
+            float *const rowbuf = s.rowbuf + (c & 1) * 4 * ((N + 3) / 4);
             const unsigned km = L.mstep == N + 1
                                     ? (__float_as_uint(fabsf(L.a[c])) & ~63u) | (unsigned)(63 - lane) : 0u;
             const unsigned kx = (L.xstep == N + 1 && q == qc)
@@ -258,20 +261,23 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
                         v.y = 4 * q4 + 1 < N ? L.a[4 * q4 + 1 < N ? 4 * q4 + 1 : 0] : 0.0f;
                         v.z = 4 * q4 + 2 < N ? L.a[4 * q4 + 2 < N ? 4 * q4 + 2 : 0] : 0.0f;
                         v.w = 4 * q4 + 3 < N ? L.a[4 * q4 + 3 < N ? 4 * q4 + 3 : 0] : 0.0f;
-                        reinterpret_cast<float4 *>(s.rowbuf)[q4] = v;
+                        reinterpret_cast<float4 *>(rowbuf)[q4] = v;
                     }
                 }
             } else if (gx == brow && xvalid) {  // the four lanes of the pivot's group
                 L.xstep = c;
 #pragma unroll
                 for (int t = 0; t < PW; t += 2)
-                    reinterpret_cast<float2 *>(s.rowbuf)[(q * PW + t) >> 1] =
+                    reinterpret_cast<float2 *>(rowbuf)[(q * PW + t) >> 1] =
                         make_float2(L.b[t], t + 1 < PW ? L.b[t + 1 < PW ? t + 1 : 0] : 0.0f);
             }
             __syncwarp();
-            const float pvt = s.rowbuf[c];
-            ok &= (pvt != 0.0f) && isfinite(pvt);
-            const float inv = __frcp_rn(pvt);
+            const float pvt = rowbuf[c];
+            // approximate reciprocal (the FP32 factor only preconditions the refinement); a
+            // zero, subnormal or non-finite pivot fails the factorisation
+            float inv;
+            asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(pvt));
+            ok &= (pvt != 0.0f) && isfinite(pvt) && isfinite(inv);
             if (lane == 0) {
                 s.piv[c] = brow;
                 s.rcp[c] = inv;
@@ -284,7 +290,7 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
                 L.a[c] = act ? l : L.a[c];
 #pragma unroll
                 for (int q4 = (c + 1) / 4; q4 < (N + 3) / 4; q4++) {
-                    const float4 v = reinterpret_cast<const float4 *>(s.rowbuf)[q4];
+                    const float4 v = reinterpret_cast<const float4 *>(rowbuf)[q4];
                     const float vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
                     for (int t = 0; t < 4; t++) {
@@ -302,15 +308,15 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
                 const bool right_hi = q >= qc, right_lo = q > qc;  // column q*PW+t > c
 #pragma unroll
                 for (int t = 0; t < PW; t += 2) {
-                    const float2 v = reinterpret_cast<const float2 *>(s.rowbuf)[(q * PW + t) >> 1];
+                    const float2 v = reinterpret_cast<const float2 *>(rowbuf)[(q * PW + t) >> 1];
                     if (t > tc ? right_hi : right_lo) L.b[t] = fmaf(-lx, v.x, L.b[t]);
                     if (t + 1 < PW && (t + 1 > tc ? right_hi : right_lo))
                         L.b[t + 1 < PW ? t + 1 : 0] = fmaf(-lx, v.y, L.b[t + 1 < PW ? t + 1 : 0]);
                 }
                 if (q == qc && xact) L.b[tc] = lx;
             }
-            __syncwarp();
         });
+        __syncwarp();  // pivots and reciprocal pivots (lane 0) before the solves
 
         // ---- refinement: solves with the register factors, FP64 residuals
         bool accepted = false;
