@@ -233,10 +233,12 @@ def main():
         from importlib import import_module
         L = import_module(pkg.__name__ + ".learned")
 
-    def build(precision, X, adjl, stats=None):
+    def build(precision, X, adjl, stats=None, sell=True):
+        # the build writes the sliced-ELL copy next to the CSR; single-field applies use it
         if precision == "learned":
-            return L.build_learned(model, cfg["ops"], X, adjl, basis, ctx=ctx, stats=stats)
-        return pkg.build_weights(cfg["ops"], X, None, adjl, basis, precision=precision, ctx=ctx, stats=stats)
+            return L.build_learned(model, cfg["ops"], X, adjl, basis, ctx=ctx, stats=stats, sell=sell)
+        return pkg.build_weights(cfg["ops"], X, None, adjl, basis, precision=precision, ctx=ctx, stats=stats,
+                                 sell=sell)
 
     def step(precision, X=Xd, f=fd):
         adjl = pkg.find_neighbors(X, k=k, ctx=ctx)
@@ -382,14 +384,21 @@ def main():
 
     W = build(headline, Xd, adjl)[-1]
     ms_spmv_api = timed(lambda: W.apply(fd), 10, 3)
-    ms_spmv = kernel_ms(lambda: W.apply(fd))
+    ms_spmv = kernel_ms(lambda: W.apply(fd))  # sliced-ELL apply
+    W_sell, W.sell = W.sell, None
+    ms_spmv_csr = kernel_ms(lambda: W.apply(fd))  # the CSR apply of the same operator
+    W.sell = W_sell
     ms_knn_kernel = kernel_ms(lambda: pkg.find_neighbors(Xd, k=k, ctx=ctx), 3)
     nnz = W.nnz
-    # algorithmic bytes of one apply: val (8 B) + col (4 B) per entry, row_ptr (8 B) per row,
-    # the field read once and the result written once
-    apply_bytes = nnz * 12 + (n + 1) * 8 + 2 * n * 8
+    sell_nnz = int(W.sell.col.shape[0])
+    # algorithmic bytes of one apply: val (8 B) + col (4 B) per entry, the row offsets (8 B
+    # per row in CSR, per 32-row slice in the sliced copy), the field read once and the
+    # result written once
+    apply_bytes = sell_nnz * 12 + ((n + 31) // 32 + 1) * 8 + 2 * n * 8
+    csr_bytes = nnz * 12 + (n + 1) * 8 + 2 * n * 8
     apply_gbs = apply_bytes / (ms_spmv * 1e-3) / 1e9
-    del W
+    csr_gbs = csr_bytes / (ms_spmv_csr * 1e-3) / 1e9
+    del W, W_sell
     hbm_peak = PEAKS.get("hbm_gbs", 6800.0)
     hbm_src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in PEAKS else "fallback"
     fp64_peak = pkg.ctypes.c_double(0.0)
@@ -420,12 +429,19 @@ def main():
     Wo = build(headline, Xo, adj_o)[-1]
     ms_spmv_o = kernel_ms(lambda: Wo.apply(fo))
     gbs_o = apply_bytes / (ms_spmv_o * 1e-3) / 1e9
+    Wo_sell, Wo.sell = Wo.sell, None
+    ms_spmv_o_csr = kernel_ms(lambda: Wo.apply(fo))
+    Wo.sell = Wo_sell
+    gbs_o_csr = csr_bytes / (ms_spmv_o_csr * 1e-3) / 1e9
     ms_step_o = timed(lambda: step(headline, Xo, fo), max(1, args.steps // 2), 1)
     ms_reorder = timed(lambda: pkg.reorder_points(Xd, k, ctx=ctx), 3, 1)
     reordered = {"ms_reorder_points": ms_reorder, "ms_per_step": ms_step_o,
                  "stencils_per_s": n * world / (ms_step_o * 1e-3),
-                 "apply": {"value": gbs_o, "unit": "GB/s", "ms": ms_spmv_o, "frac_of_hbm": gbs_o / hbm_peak}}
-    del Wo, adj_o, Xo, fo
+                 "apply": {"value": gbs_o, "unit": "GB/s", "ms": ms_spmv_o, "frac_of_hbm": gbs_o / hbm_peak,
+                           "kernel": "spmv_sell_kernel (sliced-ELL copy)"},
+                 "apply_csr": {"value": gbs_o_csr, "unit": "GB/s", "ms": ms_spmv_o_csr,
+                               "frac_of_hbm": gbs_o_csr / hbm_peak, "kernel": "spmv_pair_kernel (CSR)"}}
+    del Wo, Wo_sell, adj_o, Xo, fo
 
     # ---- e2e through the public API: host points in, host Laplacian of a host field out
     X_pin = torch.from_numpy(X_h).pin_memory()
@@ -459,7 +475,8 @@ def main():
             "dtype": ("bf16 surrogate seed + " if learned_on else "") + "f32 factor + f64 refinement",
             "data": "synthetic (seeded)",
             "config": {"workload": cfg["desc"], "n": n, "k": k, "headline": headline,
-                       "step": "kNN + " + ("features + MLP + " if learned_on else "") + "build (CSR) + one apply",
+                       "step": "kNN + " + ("features + MLP + " if learned_on else "")
+                               + "build (CSR + sliced-ELL copy) + one apply (sliced)",
                        "l2": "inputs larger than L2 (CSR 12 B/nnz x nnz, adjacency 4 B x N x k)",
                        "parallelism": f"replicas x{world}"},
             "plain_fp64": {"value": n * world / (ms_fp64 * 1e-3), "unit": "stencils/s", "ms_per_step": ms_fp64},
@@ -482,7 +499,10 @@ def main():
             "surrogate": training, "mlp": mlp,
             "apply": {"value": apply_gbs, "unit": "GB/s", "ms": ms_spmv, "ms_per_call_api": ms_spmv_api,
                       "nnz": nnz, "frac_of_hbm": apply_gbs / hbm_peak, "peak_source": hbm_src,
-                      "bytes": "nnz*12 + (ne+1)*8 + 2*n*8 per apply; ms = kernel time (library CUDA events)"},
+                      "kernel": "spmv_sell_kernel (sliced-ELL copy written by the build)",
+                      "bytes": "sell_nnz*12 + (ne/32+1)*8 + 2*n*8 per apply; ms = kernel time (library CUDA events)",
+                      "csr": {"value": csr_gbs, "unit": "GB/s", "ms": ms_spmv_csr, "frac_of_hbm": csr_gbs / hbm_peak,
+                              "kernel": "spmv_pair_kernel", "bytes": "nnz*12 + (ne+1)*8 + 2*n*8"}},
             "reordered": reordered,
             "kernels_ms": {"knn": ms_knn_kernel, "knn_per_call_api": ms_knn, "build_headline": ms_kernel,
                            "build_fp64": float(st64.ms_build), "spmv": ms_spmv},

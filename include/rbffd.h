@@ -75,6 +75,14 @@ typedef struct rbf_build_cfg {
                                      kernels serve the system size (3k >= n), otherwise
                                      unused (the first FP32 solve reaches the same error
                                      floor from any start)                            */
+    /* Optional sliced-ELL copy written by the build next to the CSR (device pointers;
+       all of them or none): sell_slice_off from rbf_sell_offsets on this build's row_ptr,
+       room for sell_nnz columns and nops * sell_nnz values (operator q's at
+       sell_val + q * sell_nnz).  rbf_spmv_sell applies it.                          */
+    const int64_t *sell_slice_off;
+    int32_t *sell_col;
+    double *sell_val;
+    int64_t sell_nnz;
 } rbf_build_cfg;
 
 /* flags */
@@ -176,6 +184,25 @@ int rbf_spmm(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const
 int rbf_csr_to_csc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr,
                    const int32_t *col, const double *val, int64_t *col_ptr_out,
                    int32_t *row_out, double *val_out);
+
+/* Sliced-ELL copy of one operator, for operators applied many times (the time-stepping
+ * use of _eval_op / mul!, src/operators/operators.jl:217-218, 529-542; same product, a
+ * different memory layout).  Slices of 32 rows; inside slice s, entry j of row r sits at
+ * slice_off[s] + 32 j + (r - 32 s) for j below the slice's longest row (shorter rows are
+ * padded with column 0, value 0).  On GB300 the CSR apply of a locality-ordered operator
+ * is bound by the FP64 pipe (cross-lane reductions, padding); the sliced apply does one
+ * FMA per entry with fully coalesced loads.  Device pointers only.
+ *   rbf_sell_offsets: slice_off[ceil(ne/32) + 1] from a CSR row_ptr; *sell_nnz = the
+ *                     sliced entry count (slice_off[last]; = nnz for equal row lengths).
+ *   rbf_sell_from_csr: fill sell_col[sell_nnz], sell_val[sell_nnz] from the CSR.
+ *   rbf_spmv_sell: y = alpha * W x + beta * y (beta == 0 ignores y). */
+int rbf_sell_offsets(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, int64_t *slice_off,
+                     int64_t *sell_nnz);
+int rbf_sell_from_csr(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, const int32_t *col,
+                      const double *val, const int64_t *slice_off, int32_t *sell_col,
+                      double *sell_val);
+int rbf_spmv_sell(rbf_ctx *ctx, int64_t ne, const int64_t *slice_off, const int32_t *sell_col,
+                  const double *sell_val, const double *x, double alpha, double beta, double *y);
 
 /* ---- learned stencil surrogate (no counterpart in the reference) ------------ */
 /* Kernels of the MLP that predicts stencil weights (training and inference run on

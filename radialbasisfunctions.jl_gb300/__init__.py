@@ -34,7 +34,7 @@ from . import _native
 __all__ = [
     "PHS", "PHS1", "PHS3", "PHS5", "PHS7", "BoundaryCondition", "Dirichlet", "Neumann", "Robin", "Internal",
     "find_neighbors", "autoselect_k", "Laplacian", "Partial", "Jacobian", "Regrid", "Operators",
-    "laplacian", "partial", "gradient", "jacobian", "regrid", "RadialBasisOperator", "WeightsCSR",
+    "laplacian", "partial", "gradient", "jacobian", "regrid", "RadialBasisOperator", "WeightsCSR", "WeightsSELL",
     "weights", "update_weights", "mul", "DimensionMismatch", "SingularException", "Context", "build_library",
     "build_weights", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph", "reorder_points",
 ]
@@ -382,8 +382,9 @@ class WeightsCSR:
     The reference returns SparseMatrixCSC (src/solve/execution.jl:105-115); the same
     matrix in CSR is the CSC of its transpose, and to_csc() produces the CSC arrays."""
 
-    def __init__(self, row_ptr, col, val, shape, ctx: Context):
+    def __init__(self, row_ptr, col, val, shape, ctx: Context, sell=None):
         self.row_ptr, self.col, self.val, self.shape, self.ctx = row_ptr, col, val, shape, ctx
+        self.sell = sell  # optional WeightsSELL copy of the same operator
 
     @property
     def nnz(self):
@@ -406,7 +407,51 @@ class WeightsCSR:
         return cp, rw, vv
 
     def apply(self, x, y=None, alpha=1.0, beta=0.0, layout="colmajor"):
+        if (self.sell is not None and _is_torch(x) and x.is_cuda and x.ndim == 1 and x.dtype == _torch().float64
+                and (y is None or (_is_torch(y) and y.is_cuda and y.is_contiguous() and y.dtype == x.dtype))):
+            return self.sell.apply(x, y, alpha, beta)
         return _spmm(self, x, y, alpha, beta, layout)
+
+    def to_sell(self):
+        """The same operator in sliced-ELL form (rbf_sell_offsets + rbf_sell_from_csr), for
+        repeated single-field applies."""
+        torch = _torch()
+        ne, ns = self.shape
+        dev = self.col.device
+        off = torch.empty((ne + 31) // 32 + 1, dtype=torch.int64, device=dev)
+        tot = ctypes.c_int64(0)
+        self.ctx.check(self.ctx.lib.rbf_sell_offsets(self.ctx.h, ne, _ptr(self.row_ptr), _ptr(off), ctypes.byref(tot)))
+        c = torch.empty(tot.value, dtype=torch.int32, device=dev)
+        v = torch.empty(tot.value, dtype=torch.float64, device=dev)
+        self.ctx.check(self.ctx.lib.rbf_sell_from_csr(self.ctx.h, ne, _ptr(self.row_ptr), _ptr(self.col),
+                                                      _ptr(self.val), _ptr(off), _ptr(c), _ptr(v)))
+        return WeightsSELL(off, c, v, self.shape, self.ctx)
+
+    def __matmul__(self, x):
+        return self.apply(x)
+
+
+class WeightsSELL:
+    """An operator in sliced-ELL form (slices of 32 rows, entry j of a slice's rows
+    contiguous): y = alpha W x + beta y for one field on the GPU (rbf_spmv_sell), the
+    product of the CSR it was made from."""
+
+    def __init__(self, slice_off, col, val, shape, ctx: Context):
+        self.slice_off, self.col, self.val, self.shape, self.ctx = slice_off, col, val, shape, ctx
+
+    def apply(self, x, y=None, alpha=1.0, beta=0.0):
+        torch = _torch()
+        ne, ns = self.shape
+        xt = torch.as_tensor(x, dtype=torch.float64).to(self.col.device).contiguous()
+        if xt.ndim != 1 or xt.shape[0] != ns:
+            raise DimensionMismatch(f"the sliced apply takes one field of {ns} values")
+        out = y if y is not None else torch.zeros(ne, dtype=torch.float64, device=self.col.device)
+        if out.dtype != torch.float64 or not out.is_cuda or not out.is_contiguous() or out.shape != (ne,):
+            raise DimensionMismatch("y must be a contiguous float64 CUDA vector of the operator's row count")
+        self.ctx.check(self.ctx.lib.rbf_spmv_sell(self.ctx.h, ne, _ptr(self.slice_off), _ptr(self.col),
+                                                  _ptr(self.val), _ptr(xt), float(alpha),
+                                                  float(beta) if y is not None else 0.0, _ptr(out)))
+        return out
 
     def __matmul__(self, x):
         return self.apply(x)
@@ -479,10 +524,11 @@ def _hermite_arrays(hermite, ns, dim):
 
 
 def build_weights(ops, data, eval_points, adjl, basis, hermite=None, precision="fp64", *, ctx=None,
-                  refine_steps=0, tol=0.0, return_status=False, stats=None, flags=0, seed=None):
+                  refine_steps=0, tol=0.0, return_status=False, stats=None, flags=0, seed=None, sell=False):
     """Weights of `ops` (list of (op_code, op_dim)) on stencils adjl; returns a list of WeightsCSR.
 
-    The drop-in for _build_weights (src/solve/api.jl:26-35, 167-196)."""
+    The drop-in for _build_weights (src/solve/api.jl:26-35, 167-196).  sell=True has the
+    build also write a sliced-ELL copy (WeightsCSR.sell), which single-field applies use."""
     torch = _torch()
     d = _points(data)
     q = d if eval_points is None else _points(eval_points, "eval_points")
@@ -523,11 +569,20 @@ def build_weights(ops, data, eval_points, adjl, basis, hermite=None, precision="
     col = torch.empty(nnz.value, dtype=torch.int32, device=dev)
     val = torch.empty((len(ops), nnz.value), dtype=torch.float64, device=dev)
     status = torch.empty(ne, dtype=torch.int8, device=dev) if return_status else None
+    sells = [None] * len(ops)
+    if sell:
+        off = torch.empty((ne + 31) // 32 + 1, dtype=torch.int64, device=dev)
+        tot = ctypes.c_int64(0)
+        ctx.check(ctx.lib.rbf_sell_offsets(ctx.h, ne, _ptr(row_ptr), _ptr(off), ctypes.byref(tot)))
+        scol = torch.empty(tot.value, dtype=torch.int32, device=dev)
+        sval = torch.empty((len(ops), tot.value), dtype=torch.float64, device=dev)
+        cfg.sell_slice_off, cfg.sell_col, cfg.sell_val, cfg.sell_nnz = _ptr(off), _ptr(scol), _ptr(sval), tot.value
+        sells = [WeightsSELL(off, scol, sval[i], (ne, ns), ctx) for i in range(len(ops))]
     st = _native.BuildStats() if stats is None else stats
     ctx.check(ctx.lib.rbf_build(ctx.h, ctypes.byref(cfg), _ptr(d), ns, _ptr(q), ne, _ptr(a), k,
                                 ctypes.byref(hs) if hs else None, _ptr(row_ptr), _ptr(col), _ptr(val),
                                 _ptr(status), ctypes.byref(st)))
-    Ws = [WeightsCSR(row_ptr, col, val[i], (ne, ns), ctx) for i in range(len(ops))]
+    Ws = [WeightsCSR(row_ptr, col, val[i], (ne, ns), ctx, sell=sells[i]) for i in range(len(ops))]
     if return_status:
         return Ws, status
     return Ws

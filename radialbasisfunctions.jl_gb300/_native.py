@@ -23,7 +23,7 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
 
-SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "stencil_build.cu", "stencil_refined_a.cu",
+SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "sell.cu", "stencil_build.cu", "stencil_refined_a.cu",
            "stencil_refined_b.cu", "stencil_refined_c.cu", "batched.cu", "plan.cu", "reorder.cu", "diag.cu", "mlp.cu",
            "mlp_tc.cu"]
 
@@ -83,7 +83,8 @@ class BuildCfg(ctypes.Structure):
                 ("nops", ctypes.c_int32), ("op_code", ctypes.c_int32 * RBF_MAX_OPS),
                 ("op_dim", ctypes.c_int32 * RBF_MAX_OPS), ("precision", ctypes.c_int32),
                 ("refine_steps", ctypes.c_int32), ("tol", ctypes.c_double), ("flags", ctypes.c_int32),
-                ("seed", ctypes.c_void_p)]
+                ("seed", ctypes.c_void_p), ("sell_slice_off", ctypes.c_void_p), ("sell_col", ctypes.c_void_p),
+                ("sell_val", ctypes.c_void_p), ("sell_nnz", ctypes.c_int64)]
 
 
 class Hermite(ctypes.Structure):
@@ -116,6 +117,9 @@ SIGNATURES = {
     "rbf_build": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _I32, _P, _P, _P, _P, _P, _P]),
     "rbf_spmm": (_I, [_P, _I64, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _D, _D, _P, _I64]),
     "rbf_csr_to_csc": (_I, [_P, _I64, _I64, _P, _P, _P, _P, _P, _P]),
+    "rbf_sell_offsets": (_I, [_P, _I64, _P, _P, _P]),
+    "rbf_sell_from_csr": (_I, [_P, _I64, _P, _P, _P, _P, _P, _P]),
+    "rbf_spmv_sell": (_I, [_P, _I64, _P, _P, _P, _P, _D, _D, _P]),
     "rbf_spmm_noalloc": (_I, [_P, _I64, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _D, _D, _P, _I64]),
     "rbf_diag_fma_peak": (_I, [_P, _I32, ctypes.POINTER(_D)]),
     "rbf_ctx_kernel_launches": (_I64, [_P]),

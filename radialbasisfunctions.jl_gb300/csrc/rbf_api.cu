@@ -407,6 +407,20 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
     P.tol = cfg->tol > 0 ? cfg->tol : 1e-9;
     P.flags = cfg->flags;
     P.seed = cfg->seed;
+    if (cfg->sell_col || cfg->sell_val || cfg->sell_slice_off) {
+        if (!cfg->sell_col || !cfg->sell_val || !cfg->sell_slice_off || !rbf_is_device_ptr(cfg->sell_col) ||
+            !rbf_is_device_ptr(cfg->sell_val) || !rbf_is_device_ptr(cfg->sell_slice_off))
+            return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the sliced copy needs device pointers for offsets, columns and values");
+        if (cfg->sell_nnz < nnz) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "sell_nnz is below the CSR entry count");
+        if (cfg->sell_nnz > nnz) {  // uneven rows: padding entries are column 0, value 0
+            RBF_CUDA(ctx, cudaMemsetAsync(cfg->sell_col, 0, sizeof(int32_t) * cfg->sell_nnz, ctx->stream));
+            RBF_CUDA(ctx, cudaMemsetAsync(cfg->sell_val, 0, sizeof(double) * cfg->sell_nnz * cfg->nops, ctx->stream));
+        }
+        P.sell_off = cfg->sell_slice_off;
+        P.sell_col = cfg->sell_col;
+        P.sell_val = cfg->sell_val;
+        P.sell_nnz = cfg->sell_nnz;
+    }
     DevBuf defer;
     if (cfg->precision != RBF_PREC_FP64) {
         RBF_TRY(defer.alloc(ctx, sizeof(int32_t) * (size_t)ne));
@@ -534,6 +548,51 @@ int rbf_csr_to_csc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr,
     RBF_TRY(vo.finish(ctx));
     RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RBF_OK;
+}
+
+int rbf_sell_offsets(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, int64_t *slice_off, int64_t *sell_nnz) {
+    RBF_TRY(check_ctx(ctx));
+    if (ne < 0 || ne >= INT32_MAX) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid row count");
+    if (!rbf_is_device_ptr(row_ptr) || !rbf_is_device_ptr(slice_off))
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the sliced layout takes device pointers only");
+    int64_t total = 0;
+    RBF_TRY(rbf_sell_offsets_device(ctx, ne, row_ptr, slice_off, &total));
+    if (sell_nnz) *sell_nnz = total;
+    return RBF_OK;
+}
+
+int rbf_sell_from_csr(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, const int32_t *col, const double *val,
+                      const int64_t *slice_off, int32_t *sell_col, double *sell_val) {
+    RBF_TRY(check_ctx(ctx));
+    if (ne < 0 || ne >= INT32_MAX) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid row count");
+    const void *ptrs[] = {row_ptr, col, val, slice_off, sell_col, sell_val};
+    for (const void *p : ptrs)
+        if (!rbf_is_device_ptr(p)) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the sliced layout takes device pointers only");
+    return rbf_sell_fill_device(ctx, ne, row_ptr, col, val, slice_off, sell_col, sell_val);
+}
+
+int rbf_spmv_sell(rbf_ctx *ctx, int64_t ne, const int64_t *slice_off, const int32_t *sell_col,
+                  const double *sell_val, const double *x, double alpha, double beta, double *y) {
+    RBF_TRY(check_ctx(ctx));
+    if (ne < 0 || ne >= INT32_MAX) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid row count");
+    const void *ptrs[] = {slice_off, sell_col, sell_val, x, y};
+    for (const void *p : ptrs)
+        if (!rbf_is_device_ptr(p)) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the sliced apply takes device pointers only");
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (ctx->timing) {
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, ctx->stream);
+    }
+    const int st = rbf_spmv_sell_device(ctx, ne, slice_off, sell_col, sell_val, x, alpha, beta, y);
+    if (ctx->timing) {
+        cudaEventRecord(t1, ctx->stream);
+        cudaEventSynchronize(t1);
+        cudaEventElapsedTime(&ctx->last_ms, t0, t1);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
+    return st;
 }
 
 int rbf_build_count_ragged(rbf_ctx *ctx, int64_t ns, int64_t ne, const int64_t *adj_ptr, const rbf_hermite *herm,

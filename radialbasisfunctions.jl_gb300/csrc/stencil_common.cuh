@@ -54,7 +54,20 @@ struct StencilParams {
     const int64_t *adj_ptr;  // ragged adjacency: neighbours of e at adjl[adj_ptr[e] ..], or nullptr
     int32_t *defer;          // FP32 paths: room for ne stencil indices that the split-row kernel
                              // hands to the general kernel (count in counters[7]), or nullptr
+    // optional sliced-ELL copy of the rows (slices of 32 rows, entry j of row r at
+    // sell_off[r / 32] + 32 j + r % 32; operator q's values at sell_val + q * sell_nnz)
+    const int64_t *sell_off;
+    int32_t *sell_col;
+    double *sell_val;
+    int64_t sell_nnz;
 };
+
+// Entry `rank` of row e into the sliced-ELL copy, when there is one.
+__device__ __forceinline__ void sell_put(const StencilParams &P, int64_t e, int rank, int32_t c, int q, double v) {
+    const int64_t p = P.sell_off[e >> 5] + 32 * (int64_t)rank + (e & 31);
+    if (q == 0) P.sell_col[p] = c;
+    P.sell_val[q * P.sell_nnz + p] = v;
+}
 
 // One size class (stencil size k, polynomial degree) of a batched build of uneven stencils.
 struct BinDesc {

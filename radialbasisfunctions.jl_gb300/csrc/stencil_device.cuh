@@ -79,6 +79,8 @@ __device__ int load_stencil(const StencilParams &P, int64_t e, const WarpSmem &w
                     int64_t p = P.row_ptr[e];
                     P.col[p] = (int32_t)e;
                     for (int r = 0; r < P.nops; r++) P.val[r * P.nnz + p] = 1.0;
+                    if (P.sell_col)
+                        for (int r = 0; r < P.nops; r++) sell_put(P, e, 0, (int32_t)e, r, 1.0);
                     if (P.status) P.status[e] = 2;
                     atomicAdd(&P.counters[3], 1ull);
                 }
@@ -280,7 +282,9 @@ __device__ void scatter_row(const StencilParams &P, int64_t e, const WarpSmem &w
         P.col[base + rank] = ci;
         for (int r = 0; r < P.nops; r++) {
             const double v = sol[i * sol_ld + r * sol_stride];
-            P.val[r * P.nnz + base + rank] = local ? v : ldexp(v, -es * P.op_order[r]);
+            const double vo = local ? v : ldexp(v, -es * P.op_order[r]);
+            P.val[r * P.nnz + base + rank] = vo;
+            if (P.sell_col) sell_put(P, e, rank, ci, r, vo);
         }
     }
 }

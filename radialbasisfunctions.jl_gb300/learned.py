@@ -286,10 +286,10 @@ def surrogate_error(model, Xb, T):
     return float(err.max()), float(err.median())
 
 
-def build_learned(model, ops, data, adjl, basis, ctx=None, stats=None, return_status=False):
+def build_learned(model, ops, data, adjl, basis, ctx=None, stats=None, return_status=False, sell=False):
     """Learned + FP32-refined build: the surrogate's prediction seeds the refinement."""
     from . import build_weights
     feats = model.features(data, None, adjl)
     seed = model.predict(feats)
     return build_weights(ops, data, None, adjl, basis, precision="learned", ctx=ctx or model.ctx, stats=stats,
-                         seed=seed, return_status=return_status)
+                         seed=seed, return_status=return_status, sell=sell)
