@@ -17,7 +17,10 @@
 //   dimension order without FMA contraction, exactly as the reference's Euclidean
 //   reduction does, and exact ties go to the smaller index.  The running top-k list is a
 //   sorted array spread over the warp (slot j at lane j%32, register j/32) and candidates
-//   that beat the current k-th key are inserted with warp shuffles.
+//   that beat the current k-th key are inserted with warp shuffles.  In the first block of
+//   cells (up to 256 candidates) the keys are held in registers first and a bisection finds
+//   a key bound with at least k + 8 keys below it; only those are offered to the list, which
+//   cuts the insertions (74 % of the search time before) from ~2.8 (k + 8) to ~(k + 8).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -349,11 +352,13 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                 int32_t *__restrict__ out, int32_t *__restrict__ fb_list, int32_t *__restrict__ fb_count) {
     __shared__ int32_t s_start[KNN_WARPS][KNN_RANGES];
     __shared__ int32_t s_off[KNN_WARPS][KNN_RANGES + 1];
+    __shared__ int32_t s_cid[KNN_WARPS][256];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t warp0 = (int64_t)blockIdx.x * KNN_WARPS + wib;
     const int64_t nwarps = (int64_t)gridDim.x * KNN_WARPS;
     int32_t *my_start = s_start[wib];
     int32_t *my_off = s_off[wib];
+    int32_t *my_cid = s_cid[wib];
     const float u8 = 8.0f * 5.9604645e-08f;
     const int tl = (kp - 1) & 31, ts = (kp - 1) >> 5;
 
@@ -441,32 +446,30 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                 my_off[2 * lane + 1] = excl + l0;
                 const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
                 __syncwarp();
-                for (int32_t f0 = 0; f0 < total; f0 += 32) {
-                    int32_t f = f0 + lane;
-                    float dd = INFINITY;
-                    int32_t id = 0x7fffffff;
-                    if (f < total) {
-                        int lo = 0, hi = KNN_RANGES - 1;
-                        while (lo < hi) {
-                            int mid = (lo + hi + 1) >> 1;
-                            if (my_off[mid] <= f) lo = mid;
-                            else hi = mid - 1;
-                        }
-                        int32_t p = my_start[lo] + (f - my_off[lo]);
-                        float4 c4 = __ldg(&sp32[p]);
-                        float dx = c4.x - qf[0];
-                        dd = dx * dx;
-                        if (DIM > 1) {
-                            float dy = c4.y - qf[1];
-                            dd = fmaf(dy, dy, dd);
-                        }
-                        if (DIM > 2) {
-                            float dz = c4.z - qf[2];
-                            dd = fmaf(dz, dz, dd);
-                        }
-                        id = __ldg(&sidx[p]);
+                // FP32 key and point index of flattened candidate f < total
+                auto cand = [&](int32_t f, float &dd, int32_t &id) {
+                    int lo = 0, hi = KNN_RANGES - 1;
+                    while (lo < hi) {
+                        int mid = (lo + hi + 1) >> 1;
+                        if (my_off[mid] <= f) lo = mid;
+                        else hi = mid - 1;
                     }
-                    bool pass = (f < total) && fkey_less(dd, id, kth, kth_id);
+                    int32_t p = my_start[lo] + (f - my_off[lo]);
+                    float4 c4 = __ldg(&sp32[p]);
+                    float dx = c4.x - qf[0];
+                    dd = dx * dx;
+                    if (DIM > 1) {
+                        float dy = c4.y - qf[1];
+                        dd = fmaf(dy, dy, dd);
+                    }
+                    if (DIM > 2) {
+                        float dz = c4.z - qf[2];
+                        dd = fmaf(dz, dz, dd);
+                    }
+                    id = __ldg(&sidx[p]);
+                };
+                // the passing candidates of the warp, one at a time, into the sorted list
+                auto insert_passing = [&](float dd, int32_t id, bool pass) {
                     unsigned m = __ballot_sync(0xffffffffu, pass);
                     while (m) {
                         const int src = __ffs(m) - 1;
@@ -514,6 +517,58 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                         kth = __shfl_sync(0xffffffffu, kv, tl);
                         kth_id = __shfl_sync(0xffffffffu, ki, tl);
                     }
+                };
+                if (r_in < 0 && nrows <= 32 && total <= 256 && total > kp) {
+                    // first block: keys in registers, indices in shared memory, and a key
+                    // threshold t with at least kp keys <= t (found by bisection, aiming at
+                    // kp .. 1.25 kp): only keys <= t can be among the kp best, so only they
+                    // are offered to the list (about kp insertions instead of ~2.8 kp)
+                    float bk[8];
+                    float kmax = 0.0f;
+#pragma unroll
+                    for (int r = 0; r < 8; r++) {
+                        const int32_t f = r * 32 + lane;
+                        bk[r] = INFINITY;
+                        if (f < total) {
+                            int32_t id;
+                            cand(f, bk[r], id);
+                            my_cid[f] = id;
+                            kmax = fmaxf(kmax, bk[r]);
+                        }
+                    }
+                    kmax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(kmax)));  // keys >= 0
+                    __syncwarp();
+                    float lo_t = 0.0f, hi_t = kmax;  // all total >= kp keys are <= kmax
+                    float t = kmax * exp2f(0.6667f * log2f(1.15f * (float)kp / (float)total));
+                    for (int it = 0; it < 8; it++) {
+                        int c = 0;
+#pragma unroll
+                        for (int r = 0; r < 8; r++) c += bk[r] <= t;
+                        c = __reduce_add_sync(0xffffffffu, c);
+                        if (c >= kp) {
+                            hi_t = t;
+                            if (c <= kp + (kp >> 2)) break;
+                        } else {
+                            lo_t = t;
+                        }
+                        t = 0.5f * (lo_t + hi_t);
+                    }
+#pragma unroll
+                    for (int r = 0; r < 8; r++) {
+                        const int32_t f = r * 32 + lane;
+                        const bool offer = f < total && bk[r] <= hi_t;
+                        const int32_t id = offer ? my_cid[f] : 0x7fffffff;
+                        insert_passing(bk[r], id, offer && fkey_less(bk[r], id, kth, kth_id));
+                    }
+                    __syncwarp();
+                    continue;
+                }
+                for (int32_t f0 = 0; f0 < total; f0 += 32) {
+                    int32_t f = f0 + lane;
+                    float dd = INFINITY;
+                    int32_t id = 0x7fffffff;
+                    if (f < total) cand(f, dd, id);
+                    insert_passing(dd, id, (f < total) && fkey_less(dd, id, kth, kth_id));
                 }
                 __syncwarp();
             }
