@@ -20,7 +20,8 @@
 //   that beat the current k-th key are inserted with warp shuffles.  In the first block of
 //   cells (up to 256 candidates) the keys are held in registers first and a bisection finds
 //   a key bound with at least k + 8 keys below it; only those are offered to the list, which
-//   cuts the insertions (74 % of the search time before) from ~2.8 (k + 8) to ~(k + 8).
+//   cuts the insertions (74 % of the search time before) from ~2.8 (k + 8) to ~(k + 8);
+//   when the offered keys fit the list they become it by one warp bitonic sort instead.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -334,6 +335,41 @@ __device__ __forceinline__ bool xkey_less(unsigned long long d1, int32_t i1, uns
     return d1 < d2 || (d1 == d2 && i1 < i2);
 }
 
+// Bitonic sort of the 32 * SLOTS (FP32 key, index) pairs of a warp, ascending (element
+// j = lane + 32 s): strides below 32 by shuffles, stride 32 between a lane's registers.
+template <int SLOTS>
+__device__ __forceinline__ void warp_sort_keys(float (&key)[SLOTS], int32_t (&kid)[SLOTS], int lane) {
+#pragma unroll
+    for (int size = 2; size <= 32 * SLOTS; size <<= 1) {
+#pragma unroll
+        for (int stride = size / 2; stride > 0; stride >>= 1) {
+            if (stride >= 32) {
+                if constexpr (SLOTS > 1) {
+                    if (fkey_less(key[SLOTS - 1], kid[SLOTS - 1], key[0], kid[0])) {
+                        const float tk = key[0];
+                        const int32_t ti = kid[0];
+                        key[0] = key[SLOTS - 1];
+                        kid[0] = kid[SLOTS - 1];
+                        key[SLOTS - 1] = tk;
+                        kid[SLOTS - 1] = ti;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int s = 0; s < SLOTS; s++) {
+                    const int e = lane + 32 * s;
+                    const float ok = __shfl_xor_sync(0xffffffffu, key[s], stride);
+                    const int32_t oi = __shfl_xor_sync(0xffffffffu, kid[s], stride);
+                    const bool keep_min = ((e & size) == 0) == ((e & stride) == 0);
+                    const bool take = keep_min ? fkey_less(ok, oi, key[s], kid[s]) : fkey_less(key[s], kid[s], ok, oi);
+                    key[s] = take ? ok : key[s];
+                    kid[s] = take ? oi : kid[s];
+                }
+            }
+        }
+    }
+}
+
 // FP32-key search.  Candidate keys are squared distances from the FP32 copy of the points;
 // the warp keeps the kp = k + 8 best (FP32 key, index) pairs.  The search stops once the
 // kp-th FP32 distance plus its error bound is inside the covered ball, so the kp listed
@@ -345,7 +381,7 @@ __device__ __forceinline__ bool xkey_less(unsigned long long d1, int32_t i1, uns
 // Error bound of an FP32 distance (u = 2^-24, M the largest coordinate magnitude):
 // |d32 - d| <= 8u (M + d).
 template <int DIM, int SLOTS>
-__global__ void __launch_bounds__(KNN_WARPS * 32)
+__global__ void __launch_bounds__(KNN_WARPS * 32, 3)  // 24 warps/SM: the register budget
 knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__restrict__ sidx,
                 const int32_t *__restrict__ cstart, const double *__restrict__ data, const double *__restrict__ q,
                 const int32_t *__restrict__ qorder, int64_t nq, int k, int kp, int R0, float mag, int64_t ns,
@@ -353,6 +389,8 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
     __shared__ int32_t s_start[KNN_WARPS][KNN_RANGES];
     __shared__ int32_t s_off[KNN_WARPS][KNN_RANGES + 1];
     __shared__ int32_t s_cid[KNN_WARPS][256];
+    __shared__ float s_lk[KNN_WARPS][32 * SLOTS];
+    __shared__ int32_t s_li[KNN_WARPS][32 * SLOTS];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t warp0 = (int64_t)blockIdx.x * KNN_WARPS + wib;
     const int64_t nwarps = (int64_t)gridDim.x * KNN_WARPS;
@@ -553,12 +591,48 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                         }
                         t = 0.5f * (lo_t + hi_t);
                     }
+                    // the offered keys, compacted; when they fit the list (the usual case) they
+                    // become the list by one bitonic sort, else they are inserted one by one
+                    int32_t nof = 0;
 #pragma unroll
                     for (int r = 0; r < 8; r++) {
                         const int32_t f = r * 32 + lane;
                         const bool offer = f < total && bk[r] <= hi_t;
-                        const int32_t id = offer ? my_cid[f] : 0x7fffffff;
-                        insert_passing(bk[r], id, offer && fkey_less(bk[r], id, kth, kth_id));
+                        const unsigned m = __ballot_sync(0xffffffffu, offer);
+                        const int32_t pos = nof + __popc(m & ((1u << lane) - 1u));
+                        if (offer && pos < 32 * SLOTS) {
+                            s_lk[wib][pos] = bk[r];
+                            s_li[wib][pos] = my_cid[f];
+                        }
+                        nof += __popc(m);
+                    }
+                    __syncwarp();
+                    if (nof <= 32 * SLOTS) {
+#pragma unroll
+                        for (int s = 0; s < SLOTS; s++) {
+                            const int j = lane + 32 * s;
+                            key[s] = j < nof ? s_lk[wib][j] : INFINITY;
+                            kid[s] = j < nof ? s_li[wib][j] : 0x7fffffff;
+                        }
+                        warp_sort_keys<SLOTS>(key, kid, lane);
+                        float kv = key[0];
+                        int32_t ki = kid[0];
+#pragma unroll
+                        for (int s = 1; s < SLOTS; s++)
+                            if (s == ts) {
+                                kv = key[s];
+                                ki = kid[s];
+                            }
+                        kth = __shfl_sync(0xffffffffu, kv, tl);
+                        kth_id = __shfl_sync(0xffffffffu, ki, tl);
+                    } else {
+#pragma unroll
+                        for (int r = 0; r < 8; r++) {
+                            const int32_t f = r * 32 + lane;
+                            const bool offer = f < total && bk[r] <= hi_t;
+                            const int32_t id = offer ? my_cid[f] : 0x7fffffff;
+                            insert_passing(bk[r], id, offer && fkey_less(bk[r], id, kth, kth_id));
+                        }
                     }
                     __syncwarp();
                     continue;
