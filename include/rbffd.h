@@ -185,6 +185,23 @@ int rbf_csr_to_csc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr,
                    const int32_t *col, const double *val, int64_t *col_ptr_out,
                    int32_t *row_out, double *val_out);
 
+/* Operator algebra on built weights (operators of the same data and stencils share
+ * row_ptr / col; every array a device pointer):
+ *   rbf_weights_axpby: out = alpha * a + beta * b entry-wise over nnz values (b may be
+ *     NULL: out = alpha * a) -- op1 + op2, op1 - op2, alpha * op, op / alpha, -op on
+ *     RadialBasisOperator (src/operators/operator_algebra.jl:245-295, _combine_weights /
+ *     _scale_weights, :307-309 and :288-289).
+ *   rbf_weights_directional: out = sum_i v_i * W_i over the nd gradient value arrays of one
+ *     Jacobian build (operator i at val + i * nnz); v: nd doubles (constant direction,
+ *     per_row = 0) or ne * nd (one direction per row, per_row = 1) --
+ *     _combine_directional_weights (src/operators/directional.jl:69-82).
+ * Products and sums are rounded separately, in the reference's evaluation order. */
+int rbf_weights_axpby(rbf_ctx *ctx, int64_t nnz, double alpha, const double *a, double beta,
+                      const double *b, double *out);
+int rbf_weights_directional(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, int32_t nd,
+                            const double *val, int64_t nnz, const double *v, int32_t per_row,
+                            double *out);
+
 /* Sliced-ELL copy of one operator, for operators applied many times (the time-stepping
  * use of _eval_op / mul!, src/operators/operators.jl:217-218, 529-542; same product, a
  * different memory layout).  Slices of 32 rows; inside slice s, entry j of row r sits at

@@ -34,7 +34,8 @@ from . import _native
 __all__ = [
     "PHS", "PHS1", "PHS3", "PHS5", "PHS7", "BoundaryCondition", "Dirichlet", "Neumann", "Robin", "Internal",
     "find_neighbors", "autoselect_k", "Laplacian", "Partial", "Jacobian", "Regrid", "Operators",
-    "laplacian", "partial", "gradient", "jacobian", "regrid", "RadialBasisOperator", "WeightsCSR", "WeightsSELL",
+    "laplacian", "partial", "gradient", "jacobian", "regrid", "directional", "Directional", "RadialBasisOperator",
+    "WeightsCSR", "WeightsSELL",
     "weights", "update_weights", "mul", "DimensionMismatch", "SingularException", "Context", "build_library",
     "build_weights", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph", "reorder_points",
 ]
@@ -320,6 +321,30 @@ class Regrid(_Op):
 
     def __repr__(self):
         return "regrid"
+
+
+class Directional(_Op):
+    """∇f⋅v: the gradient weights combined with a direction (src/operators/directional.jl:6-10,
+    69-95); v is one direction of length dim or one direction per evaluation point."""
+
+    def __init__(self, v):
+        self.v = v
+
+    def ops(self, dim):
+        return [(OP_PARTIAL1, d) for d in range(dim)]
+
+    def __repr__(self):
+        return "Directional Derivative (∇f⋅v)"
+
+
+class _Combined(_Op):
+    """A sum / difference / scaling of built operators (operator_algebra.jl:245-295)."""
+
+    def __init__(self, desc: str, rank: int):
+        self.desc, self.rank = desc, rank
+
+    def __repr__(self):
+        return self.desc
 
 
 class Operators(_Op):
@@ -789,7 +814,59 @@ class RadialBasisOperator:
         ops = self.L.ops(self.dim)
         Ws = build_weights(ops, self.data, self.eval_points, self.adjl, self.basis, self.hermite, self.precision,
                            ctx=self.ctx)
+        if isinstance(self.L, Directional):
+            return _directional_weights(Ws, self.L.v, self.dim)
         return Ws[0] if (len(Ws) == 1 and self.L.rank == 0) else tuple(Ws)
+
+    # ---- operator algebra (src/operators/operator_algebra.jl:245-295): the weights of the
+    # result are combined on the device; the result rebuilds its parts when updated
+    def _check_compatible(self, other):
+        torch = _torch()
+        if not isinstance(other, RadialBasisOperator):
+            return NotImplemented
+        if self.L.rank != other.L.rank:
+            raise ValueError(f"Cannot combine operators with different output ranks: {self.L!r} (rank "
+                             f"{self.L.rank}) and {other.L!r} (rank {other.L.rank})")
+        if self.data.shape != other.data.shape or not torch.allclose(self.data, other.data):
+            raise ValueError("Can not add operators that were not built with the same data.")
+        a1, a2 = torch.as_tensor(self.adjl), torch.as_tensor(other.adjl)
+        if a1.shape != a2.shape or not torch.equal(a1.to(a2.device, torch.int64), a2.to(torch.int64)):
+            raise ValueError("Can not add operators that do not have the same stencils.")
+
+    def _combined(self, other, alpha, beta, desc):
+        def combine():
+            for op in (self, other) if other is not None else (self,):
+                if not op.valid_cache:
+                    op.update_weights()
+            if other is None:
+                return _map_weights(lambda w: _axpby(w, alpha, None, 0.0), self.weights)
+            return _map_weights(lambda w1, w2: _axpby(w1, alpha, w2, beta), self.weights, other.weights)
+        return _DerivedOperator(_Combined(desc, self.L.rank), self, combine)
+
+    def __add__(self, other):
+        if self._check_compatible(other) is NotImplemented:
+            return NotImplemented
+        return self._combined(other, 1.0, 1.0, f"{self.L!r} + {other.L!r}")
+
+    def __sub__(self, other):
+        if self._check_compatible(other) is NotImplemented:
+            return NotImplemented
+        return self._combined(other, 1.0, -1.0, f"{self.L!r} - {other.L!r}")
+
+    def __mul__(self, alpha):
+        if not isinstance(alpha, (int, float, np.number)):
+            return NotImplemented
+        return self._combined(None, float(alpha), 0.0, f"{float(alpha)} * {self.L!r}")
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, alpha):
+        if not isinstance(alpha, (int, float, np.number)):
+            return NotImplemented
+        return self._combined(None, 1.0 / float(alpha), 0.0, f"{self.L!r} / {float(alpha)}")
+
+    def __neg__(self):
+        return self._combined(None, -1.0, 0.0, f"-{self.L!r}")
 
     def update_weights(self):
         """Rebuild the weights from data / eval_points (operators.jl:589-602)."""
@@ -822,6 +899,66 @@ class RadialBasisOperator:
         return f"RadialBasisOperator\n├─Operator: {self.L!r}\n├─Data type: float64\n├─Number of weights: " \
                f"{self.weights.nnz if isinstance(self.weights, WeightsCSR) else self.weights[0].nnz}\n" \
                f"└─Basis: {self.basis!r}"
+
+
+class _DerivedOperator(RadialBasisOperator):
+    """An operator whose weights come from other built operators (sum, difference, scaling);
+    it shares their points and stencils and rebuilds them when updated."""
+
+    def __init__(self, L, template: RadialBasisOperator, combine):
+        self.L = L
+        self._combine = combine
+        self.ctx, self.data, self.eval_points = template.ctx, template.data, template.eval_points
+        self.basis, self.k, self.adjl = template.basis, template.k, template.adjl
+        self.hermite, self.precision = template.hermite, template.precision
+        self.weights = None
+        self.valid_cache = False
+        self.update_weights()
+
+    def _build(self):
+        return self._combine()
+
+
+def _map_weights(fn, *ws):
+    if isinstance(ws[0], tuple):
+        return tuple(fn(*parts) for parts in zip(*ws))
+    return fn(*ws)
+
+
+def _axpby(W1: WeightsCSR, alpha, W2, beta):
+    """alpha * W1 + beta * W2 on the device (W2 of the same structure, or None)."""
+    torch = _torch()
+    out = torch.empty_like(W1.val)
+    ctx = W1.ctx
+    ctx.check(ctx.lib.rbf_weights_axpby(ctx.h, W1.nnz, float(alpha), _ptr(W1.val), float(beta),
+                                        _ptr(W2.val) if W2 is not None else None, _ptr(out)))
+    return WeightsCSR(W1.row_ptr, W1.col, out, W1.shape, ctx)
+
+
+def _directional_weights(Ws, v, dim):
+    """sum_i v_i W_i (directional.jl:69-82): v of length dim, or one direction per row."""
+    torch = _torch()
+    W0 = Ws[0]
+    ne = W0.shape[0]
+    vt = torch.as_tensor(v, dtype=torch.float64).to(W0.val.device)
+    if vt.ndim == 1 and vt.shape[0] == dim:
+        per_row = 0
+    elif vt.ndim == 2 and vt.shape == (ne, dim):
+        per_row = 1
+    elif vt.ndim == 1 and vt.shape[0] == ne * dim:
+        vt, per_row = vt.reshape(ne, dim), 1
+    else:
+        raise ValueError(f"Direction vector length {tuple(vt.shape)} must equal dimension {dim} or data length {ne}")
+    vt = vt.contiguous()
+    nnz = W0.nnz
+    base = W0.val
+    if not all(W.val.data_ptr() == base.data_ptr() + 8 * i * nnz for i, W in enumerate(Ws)):
+        base = torch.stack([W.val for W in Ws])
+    out = torch.empty_like(W0.val)
+    ctx = W0.ctx
+    ctx.check(ctx.lib.rbf_weights_directional(ctx.h, ne, _ptr(W0.row_ptr), dim, _ptr(base), nnz, _ptr(vt), per_row,
+                                              _ptr(out)))
+    return WeightsCSR(W0.row_ptr, W0.col, out, W0.shape, ctx)
 
 
 def weights(op: RadialBasisOperator):
@@ -863,6 +1000,12 @@ def jacobian(data, basis=None, **kw):
 def gradient(data, basis=None, **kw):
     """gradient(data; ...) = jacobian(data; ...) (gradient.jl:32)."""
     return jacobian(data, basis=basis, **kw)
+
+
+def directional(data, v, basis=None, **kw):
+    """directional(data, v; basis, eval_points, k, adjl, hermite) (directional.jl:37-40): the
+    directional derivative ∇f⋅v with a constant direction or one direction per point."""
+    return RadialBasisOperator(Directional(v), data, basis=basis, **kw)
 
 
 def regrid(data, eval_points, basis=None, **kw):

@@ -23,7 +23,7 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
 
-SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "sell.cu", "stencil_build.cu", "stencil_refined_a.cu",
+SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "sell.cu", "algebra.cu", "stencil_build.cu", "stencil_refined_a.cu",
            "stencil_refined_b.cu", "stencil_refined_c.cu", "batched.cu", "plan.cu", "reorder.cu", "diag.cu", "mlp.cu",
            "mlp_tc.cu"]
 
@@ -117,6 +117,8 @@ SIGNATURES = {
     "rbf_build": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _I32, _P, _P, _P, _P, _P, _P]),
     "rbf_spmm": (_I, [_P, _I64, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _D, _D, _P, _I64]),
     "rbf_csr_to_csc": (_I, [_P, _I64, _I64, _P, _P, _P, _P, _P, _P]),
+    "rbf_weights_axpby": (_I, [_P, _I64, _D, _P, _D, _P, _P]),
+    "rbf_weights_directional": (_I, [_P, _I64, _P, _I32, _P, _I64, _P, _I32, _P]),
     "rbf_sell_offsets": (_I, [_P, _I64, _P, _P, _P]),
     "rbf_sell_from_csr": (_I, [_P, _I64, _P, _P, _P, _P, _P, _P]),
     "rbf_spmv_sell": (_I, [_P, _I64, _P, _P, _P, _P, _D, _D, _P]),

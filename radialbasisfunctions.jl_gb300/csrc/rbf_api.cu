@@ -550,6 +550,25 @@ int rbf_csr_to_csc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr,
     return RBF_OK;
 }
 
+int rbf_weights_axpby(rbf_ctx *ctx, int64_t nnz, double alpha, const double *a, double beta, const double *b,
+                      double *out) {
+    RBF_TRY(check_ctx(ctx));
+    if (nnz < 0) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid entry count");
+    if (!rbf_is_device_ptr(a) || !rbf_is_device_ptr(out) || (b && !rbf_is_device_ptr(b)))
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "operator algebra takes device pointers only");
+    return rbf_weights_axpby_device(ctx, nnz, alpha, a, beta, b, out);
+}
+
+int rbf_weights_directional(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, int32_t nd, const double *val,
+                            int64_t nnz, const double *v, int32_t per_row, double *out) {
+    RBF_TRY(check_ctx(ctx));
+    if (ne < 0 || nnz < 0 || nd < 1 || nd > RBF_MAX_OPS) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid sizes");
+    const void *ptrs[] = {row_ptr, val, v, out};
+    for (const void *p : ptrs)
+        if (!rbf_is_device_ptr(p)) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "operator algebra takes device pointers only");
+    return rbf_weights_directional_device(ctx, ne, row_ptr, nd, val, nnz, v, per_row != 0, out);
+}
+
 int rbf_sell_offsets(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, int64_t *slice_off, int64_t *sell_nnz) {
     RBF_TRY(check_ctx(ctx));
     if (ne < 0 || ne >= INT32_MAX) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid row count");

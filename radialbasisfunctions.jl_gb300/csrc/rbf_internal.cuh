@@ -120,6 +120,11 @@ int rbf_boundary_map_device(rbf_ctx *ctx, int64_t n, const uint8_t *d_isb, int32
 int rbf_check_indices(rbf_ctx *ctx, const int32_t *d_idx, int64_t n, int32_t hi, bool *ok);
 int rbf_exclusive_scan_i64(rbf_ctx *ctx, const int64_t *d_in, int64_t *d_out, int64_t n,
                            int64_t *total);
+// operator algebra on built weights (algebra.cu)
+int rbf_weights_axpby_device(rbf_ctx *ctx, int64_t nnz, double alpha, const double *a, double beta, const double *b,
+                             double *out);
+int rbf_weights_directional_device(rbf_ctx *ctx, int64_t ne, const int64_t *rp, int nd, const double *val,
+                                   int64_t nnz, const double *v, int per_row, double *out);
 // sliced-ELL copy of an operator (sell.cu)
 int rbf_sell_offsets_device(rbf_ctx *ctx, int64_t ne, const int64_t *d_rp, int64_t *d_off, int64_t *sell_nnz);
 int rbf_sell_fill_device(rbf_ctx *ctx, int64_t ne, const int64_t *d_rp, const int32_t *d_col, const double *d_val,
