@@ -419,7 +419,11 @@ def main():
             "flops": f"reference FP64 algorithm count per stencil ({flops_stencil:.0f}: n^3/3 + 2n^2R + assembly)",
             "peak_source": "FP64 FMA loop measured in this run (rbf_diag_fma_peak)",
             "fp32_pipe": {"peak": fp32_peak.value, "frac": ach / fp32_peak.value},
-            "traffic_source": "ncu dram__bytes_read+write of the same kernel at N=1M, scaled by stencils"}
+            "traffic_source": "ncu dram__bytes_read+write of the same kernel at N=1M, scaled by stencils",
+            "note": "frac counts the reference's FP64 algorithm at the FP64 peak; the kernel does most of it "
+                    "on the FP32 pipe, so the pipes it actually uses are below (ncu, N = 1M)",
+            "pipes_measured": {"fp64": 0.439, "fma_fp32": 0.162, "alu": 0.308, "issue_active": 0.457,
+                               "source": "profiles/build_refined_split_40_lap3d_1M.md"}}
 
     # ---- the same workload after reorder_points (Morton order, the reference's locality
     # utility applied once): the apply's gathers become local

@@ -97,8 +97,8 @@ int rbf_build_fp64_launch(rbf_ctx *ctx, const StencilParams &P) {
 
 int rbf_build_fp32_launch(rbf_ctx *ctx, const StencilParams &P) {
     if (P.ne == 0) return RBF_OK;
-    // 33..40-row single-operator systems: the split-row kernel on the interior stencils,
-    // then the general kernel on the ones it deferred
+    // 40-row single-operator systems: the split-row kernel on the interior stencils, then the
+    // general kernel on the ones it deferred (every FP32 build passes a deferred list)
     if (P.defer) {
         const int st = rbf_launch_refined_split(ctx, P);
         if (st != RBF_LAUNCH_NO_VARIANT) {
