@@ -125,12 +125,13 @@ def test_learned_build_equals_fp64(pkg):
         assert set(np.unique(status.cpu().numpy())) <= {0, 3}
 
 
-@pytest.mark.parametrize("M,N,K", [(300, 256, 96), (128, 32, 256), (1000, 96, 32), (257, 64, 64)])
+@pytest.mark.parametrize("M,N,K", [(300, 256, 96), (128, 32, 256), (1000, 96, 32), (257, 64, 64), (100003, 256, 256)])
 @pytest.mark.parametrize("gelu,bf16_out", [(False, False), (True, True)])
 def test_tc_gemm_equals_mma_sync(pkg, M, N, K, gelu, bf16_out):
     """The tcgen05 GEMM (TMEM accumulators) equals the mma.sync GEMM bit for bit on operands
     whose products and sums are exact (small integers), incl. row/column tails, the bias and
-    the GELU epilogue, and it reports no pipeline timeout."""
+    the GELU epilogue, several tiles per CTA (the persistent kernel's alternating
+    accumulators and ring wrap-around), and it reports no pipeline timeout."""
     L = pkg.learned
     model = L.StencilMLP(k=30, dim=3, hidden=(64,), seed=0)
     rng = np.random.default_rng(M + N + K)
