@@ -169,6 +169,20 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
               const rbf_hermite *herm, const int64_t *row_ptr, int32_t *col, double *val,
               int8_t *status_out, rbf_build_stats *stats);
 
+/* Reverse-mode sensitivities of a build with respect to the point positions: given the
+ * cotangent dW of the built values (val layout: dW[op * nnz + p], the row_ptr / column
+ * order of the forward rbf_build with the same cfg->flags), writes ddata (ns x dim) and
+ * deval (ne x dim) = the gradients of L = sum(dW .* val).  With eval == NULL the eval
+ * points are the data points and the full gradient is ddata + deval.  Replaces the
+ * pullback of _build_weights (src/solve/ad_shared.jl:63-157 with the stencil rules of
+ * src/solve/backward.jl:31-222: backward_linear_solve!, backward_collocation!,
+ * backward_rhs!).  Supports PHS 1/3/5/7, the identity, first partials and the Laplacian,
+ * interior stencils (no Hermite rows; every row holds k entries).  Each stencil system
+ * is re-assembled and factorised once in FP64 for the weights and the adjoint. */
+int rbf_build_backward(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns,
+                       const double *eval, int64_t ne, const int32_t *adjl, int32_t k,
+                       const int64_t *row_ptr, const double *dW, double *ddata, double *deval);
+
 /* ---- apply ------------------------------------------------------------------ */
 /* Y = alpha * W X + beta * Y for nf fields, W the op_index-th operator of a built
  * CSR (ne x ns).  Replaces _eval_op / mul! (src/operators/operators.jl:217-218,

@@ -37,7 +37,7 @@ __all__ = [
     "laplacian", "partial", "gradient", "jacobian", "regrid", "directional", "Directional", "RadialBasisOperator",
     "WeightsCSR", "WeightsSELL",
     "weights", "update_weights", "mul", "DimensionMismatch", "SingularException", "Context", "build_library",
-    "build_weights", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph", "reorder_points",
+    "build_weights", "build_weights_backward", "build_weights_differentiable", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph", "reorder_points",
 ]
 
 build_library = _native.build_library
@@ -611,6 +611,75 @@ def build_weights(ops, data, eval_points, adjl, basis, hermite=None, precision="
     if return_status:
         return Ws, status
     return Ws
+
+
+def build_weights_backward(ops, data, eval_points, adjl, basis, row_ptr, dW, *, ctx=None, flags=0):
+    """Gradients (ddata, deval) of L = sum(dW * val) for the build
+    build_weights(ops, data, eval_points, adjl, basis, flags=flags) whose CSR row_ptr is
+    given, dW shaped like its values (len(ops), nnz).  The pullback of _build_weights
+    (src/solve/ad_shared.jl:63-157, src/solve/backward.jl:31-222); eval_points None means
+    the data points, whose full gradient is then ddata + deval.  PHS 3/5/7; the identity,
+    first partials and the Laplacian; interior stencils."""
+    torch = _torch()
+    d = _points(data)
+    q = None if eval_points is None else _points(eval_points, "eval_points")
+    ns, dim = d.shape
+    ne = ns if q is None else q.shape[0]
+    ctx = ctx or Context.default(_device_of(d, adjl, dW))
+    dev = torch.device("cuda", ctx.device)
+    a = adjl.to(torch.int32).contiguous() if _is_torch(adjl) else \
+        np.ascontiguousarray(np.asarray(adjl, dtype=np.int32))
+    if a.ndim != 2 or a.shape[0] != ne:
+        raise DimensionMismatch("adjl must be an (N_eval, k) array of 0-based data indices")
+    k = int(a.shape[1])
+    g = dW.to(torch.float64).contiguous() if _is_torch(dW) else np.ascontiguousarray(np.asarray(dW, np.float64))
+    if g.ndim == 1:
+        g = g.reshape(1, -1)
+    if g.shape[0] != len(ops) or g.shape[1] != ne * k:
+        raise DimensionMismatch("dW must be shaped (number of operators, nnz) with nnz = N_eval * k")
+    cfg = _native.BuildCfg()
+    cfg.dim, cfg.phs, cfg.poly_deg, cfg.nops = dim, basis.order, basis.poly_deg, len(ops)
+    for i, (c, od) in enumerate(ops):
+        cfg.op_code[i] = c
+        cfg.op_dim[i] = od
+    cfg.flags = flags
+    ddata = torch.empty((ns, dim), dtype=torch.float64, device=dev)
+    deval = torch.empty((ne, dim), dtype=torch.float64, device=dev)
+    ctx.check(ctx.lib.rbf_build_backward(ctx.h, ctypes.byref(cfg), _ptr(d), ns, _ptr(q), ne, _ptr(a), k,
+                                         _ptr(row_ptr), _ptr(g), _ptr(ddata), _ptr(deval)))
+    return ddata, deval
+
+
+def build_weights_differentiable(ops, data, eval_points, adjl, basis, *, ctx=None, flags=0):
+    """build_weights as a torch autograd function of the point positions (the rrule of
+    _build_weights, src/solve/ad_shared.jl:130-157): returns (row_ptr, col, val) with
+    val (len(ops), nnz) differentiable with respect to data and eval_points (CUDA float64
+    tensors).  eval_points None evaluates at the data points."""
+    torch = _torch()
+
+    class _BuildFn(torch.autograd.Function):
+        @staticmethod
+        def forward(fctx, x, y):
+            Ws = build_weights(ops, x.detach(), None if y is None else y.detach(), adjl, basis, ctx=ctx,
+                               flags=flags)
+            val = torch.stack([W.val for W in Ws])
+            fctx.save_for_backward(x, y if y is not None else x)
+            fctx.row_ptr = Ws[0].row_ptr
+            fctx.same = y is None
+            fctx.mark_non_differentiable(Ws[0].row_ptr, Ws[0].col)
+            return Ws[0].row_ptr, Ws[0].col, val
+
+        @staticmethod
+        def backward(fctx, _g_rp, _g_col, g_val):
+            x, y = fctx.saved_tensors
+            gd, ge = build_weights_backward(ops, x.detach(), None if fctx.same else y.detach(), adjl, basis,
+                                            fctx.row_ptr, g_val.contiguous(), ctx=ctx, flags=flags)
+            if fctx.same:
+                return gd + ge, None
+            return gd, ge
+
+    x = data if _is_torch(data) else torch.as_tensor(np.asarray(data, np.float64))
+    return _BuildFn.apply(x, eval_points)
 
 
 def reorder_points(data, k=None, ctx=None):

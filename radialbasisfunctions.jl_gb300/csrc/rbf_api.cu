@@ -550,6 +550,70 @@ int rbf_csr_to_csc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr,
     return RBF_OK;
 }
 
+int rbf_build_backward(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns, const double *eval,
+                       int64_t ne, const int32_t *adjl, int32_t k, const int64_t *row_ptr, const double *dW,
+                       double *ddata, double *deval) {
+    RBF_TRY(check_ctx(ctx));
+    if (!cfg) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null configuration");
+    if (k < 1 || k > RBF_MAX_STENCIL) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "k must be in 1..%d", RBF_MAX_STENCIL);
+    if (k > ns) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "k exceeds the number of data points");
+    if (ns >= INT32_MAX || ne >= INT32_MAX || ne < 0) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "point counts must be < 2^31");
+    if (!data || !adjl || !row_ptr || !dW || !ddata || (ne > 0 && !deval))
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null array");
+    StencilParams P;
+    memset(&P, 0, sizeof P);
+    P.k = k;
+    RBF_TRY(rbf_plan_params(ctx, cfg, P));
+    for (int r = 0; r < P.nops; r++)
+        if (P.op_code[r] == RBF_OP_PARTIAL2)
+            return rbf_fail(ctx, RBF_ERR_UNSUPPORTED, "the weight adjoint supports the identity, first partials and "
+                                                      "the Laplacian");
+    const int dim = P.dim;
+    if (!eval) {
+        eval = data;
+        if (ne != ns) return rbf_fail(ctx, RBF_ERR_DIMENSION, "without eval points ne must equal ns");
+    }
+    InArray d, q, a, rp, gw;
+    RBF_TRY(d.bind(ctx, data, sizeof(double) * ns * dim));
+    RBF_TRY(q.bind(ctx, eval, sizeof(double) * ne * dim));
+    RBF_TRY(a.bind(ctx, adjl, sizeof(int32_t) * ne * k));
+    RBF_TRY(rp.bind(ctx, row_ptr, sizeof(int64_t) * (ne + 1)));
+    bool idx_ok = true;
+    RBF_TRY(rbf_check_indices(ctx, a.as<int32_t>(), ne * (int64_t)k, (int32_t)ns, &idx_ok));
+    if (!idx_ok) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "adjl holds indices outside [0, %lld)", (long long)ns);
+    int64_t nnz = 0;
+    RBF_CUDA(ctx, cudaMemcpyAsync(&nnz, rp.as<int64_t>() + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (nnz != ne * (int64_t)k)
+        return rbf_fail(ctx, RBF_ERR_UNSUPPORTED, "the weight adjoint takes interior builds (k entries per row)");
+    RBF_TRY(gw.bind(ctx, dW, sizeof(double) * nnz * P.nops));
+    OutArray od, oe;
+    RBF_TRY(od.bind(ctx, ddata, sizeof(double) * ns * dim));
+    RBF_TRY(oe.bind(ctx, deval, sizeof(double) * ne * dim));
+    RBF_CUDA(ctx, cudaMemsetAsync(od.as<double>(), 0, sizeof(double) * ns * dim, ctx->stream));
+    if (ne > 0) RBF_CUDA(ctx, cudaMemsetAsync(oe.as<double>(), 0, sizeof(double) * ne * dim, ctx->stream));
+    DevBuf counters;
+    RBF_TRY(counters.alloc(ctx, sizeof(unsigned long long) * 8 + sizeof(double)));
+    RBF_CUDA(ctx, cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long) * 8 + sizeof(double), ctx->stream));
+    P.ne = ne;
+    P.ns = ns;
+    P.nnz = nnz;
+    P.data = d.as<double>();
+    P.eval = q.as<double>();
+    P.adjl = a.as<int32_t>();
+    P.row_ptr = rp.as<int64_t>();
+    P.counters = counters.as<unsigned long long>();
+    P.max_resid = reinterpret_cast<double *>(counters.as<unsigned long long>() + 8);
+    RBF_TRY(rbf_backward_launch(ctx, P, gw.as<double>(), od.as<double>(), oe.as<double>()));
+    unsigned long long nsing = 0;
+    RBF_CUDA(ctx, cudaMemcpyAsync(&nsing, counters.ptr, sizeof nsing, cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_TRY(od.finish(ctx));
+    RBF_TRY(oe.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (nsing) return rbf_fail(ctx, RBF_ERR_SINGULAR, "%llu stencil system(s) are singular", nsing);
+    return RBF_OK;
+}
+
 int rbf_weights_axpby(rbf_ctx *ctx, int64_t nnz, double alpha, const double *a, double beta, const double *b,
                       double *out) {
     RBF_TRY(check_ctx(ctx));

@@ -118,6 +118,7 @@ int rbf_boundary_map_device(rbf_ctx *ctx, int64_t n, const uint8_t *d_isb, int32
                             int64_t *n_boundary);
 
 int rbf_check_indices(rbf_ctx *ctx, const int32_t *d_idx, int64_t n, int32_t hi, bool *ok);
+int rbf_backward_launch(rbf_ctx *ctx, const StencilParams &P, const double *dW, double *ddata, double *deval);
 int rbf_exclusive_scan_i64(rbf_ctx *ctx, const int64_t *d_in, int64_t *d_out, int64_t n,
                            int64_t *total);
 // operator algebra on built weights (algebra.cu)
