@@ -425,6 +425,21 @@ def main():
             "pipes_measured": {"fp64": 0.439, "fma_fp32": 0.162, "alu": 0.308, "issue_active": 0.457,
                                "source": "profiles/build_refined_split_40_lap3d_1M.md"}}
 
+    # ---- the adjoint of the build: gradients of <dW, W> with respect to the points (the
+    # pullback of _build_weights), for a random cotangent of the headline operator
+    adjoint = None
+    if all(c in (0, 1, 3) for c, _ in cfg["ops"]):
+        adj_b = pkg.find_neighbors(Xd, k=k, ctx=ctx)
+        rp = build(headline, Xd, adj_b, sell=False)[0].row_ptr
+        gen = torch.Generator(device=dev).manual_seed(7)
+        dW = torch.rand((len(cfg["ops"]), n * k), generator=gen, device=dev, dtype=torch.float64) - 0.5
+        ms_adj = timed(lambda: pkg.build_weights_backward(cfg["ops"], Xd, None, adj_b, basis, rp, dW, ctx=ctx),
+                       2, 1)
+        adjoint = {"ms": ms_adj, "stencils_per_s": n / (ms_adj * 1e-3), "ms_fp64_build": ms_b_64,
+                   "kernel": "build_backward_kernel (FP64, one warp per stencil: assembly, LU with the weights' "
+                             "and the adjoint's right-hand sides, pair gradients, atomic scatter)"}
+        del dW, rp, adj_b
+
     # ---- the same workload after reorder_points (Morton order, the reference's locality
     # utility applied once): the apply's gathers become local
     perm, Xo = pkg.reorder_points(Xd, k, ctx=ctx)
@@ -508,6 +523,7 @@ def main():
                       "csr": {"value": csr_gbs, "unit": "GB/s", "ms": ms_spmv_csr, "frac_of_hbm": csr_gbs / hbm_peak,
                               "kernel": "spmv_pair_kernel", "bytes": "nnz*12 + (ne+1)*8 + 2*n*8"}},
             "reordered": reordered,
+            "adjoint": adjoint,
             "kernels_ms": {"knn": ms_knn_kernel, "knn_per_call_api": ms_knn, "build_headline": ms_kernel,
                            "build_fp64": float(st64.ms_build), "spmv": ms_spmv},
             "peaks": {"fp64_tflops_measured": fp64_peak.value, "fp32_tflops_measured": fp32_peak.value,
