@@ -71,6 +71,7 @@ def parse():
     p.add_argument("--config", default="lap3d_4M", choices=sorted(CONFIGS))
     p.add_argument("--n", type=int, default=0, help="override the point count (development runs)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--interp-n", type=int, default=10_000, help="points of the Interpolator leg (0: skip)")
     p.add_argument("--cpu-sample", type=int, default=0, help="stencils in the CPU baseline sample")
     p.add_argument("--train-stencils", type=int, default=2_000_000, help="solver stencils the surrogate trains on")
     p.add_argument("--train-epochs", type=int, default=12)
@@ -164,6 +165,81 @@ def cpu_baseline(cfg, n, sample, steps=1):
     t2 = time.perf_counter()
     return {"stencils_per_s": sample / (t2 - t0), "knn_s": t1 - t0, "build_s": t2 - t1,
             "cores": O.num_threads(), "sample": sample}
+
+
+def halton(n, base):
+    """Radical-inverse sequence of base `base`, indices 1..n."""
+    out = np.zeros(n)
+    idx = np.arange(1, n + 1)
+    f = 1.0
+    while idx.any():
+        f /= base
+        out += f * (idx % base)
+        idx //= base
+    return out
+
+
+def franke(p):
+    x, y = p[:, 0], p[:, 1]
+    return (0.75 * np.exp(-(9 * x - 2) ** 2 / 4 - (9 * y - 2) ** 2 / 4)
+            + 0.75 * np.exp(-(9 * x + 1) ** 2 / 49 - (9 * y + 1) / 10)
+            + 0.5 * np.exp(-(9 * x - 7) ** 2 / 4 - (9 * y - 3) ** 2 / 4)
+            - 0.2 * np.exp(-(9 * x - 4) ** 2 - (9 * y - 7) ** 2))
+
+
+def interp_bench(pkg, torch, stream, n_points, cpu):
+    """Interpolator on Franke's function at Halton points (the reference's interpolation
+    test, PHS3 degree 2) at n_points: fit (assembly + rook Bunch-Kaufman + solve) and the
+    evaluation at 1M points, on the GPU; LAPACK's dsytrf_rook (all host cores) and the oracle's
+    evaluation beside it."""
+    x = np.stack([halton(n_points, 2), halton(n_points, 3)], 1)
+    y = franke(x)
+    xd, yd = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    basis = pkg.PHS(3, poly_deg=2)
+    I = pkg.Interpolator(xd, yd, basis)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    reps = 2
+    for _ in range(reps):
+        I = pkg.Interpolator(xd, yd, basis)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_fit = e0.elapsed_time(e1) / reps
+    m = 1_000_000
+    xe = torch.rand((m, 2), dtype=torch.float64, device=xd.device, generator=torch.Generator(device=xd.device).manual_seed(3))
+    I(xe)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    v = I(xe)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_eval = e0.elapsed_time(e1)
+    err = float(np.abs(v.cpu().numpy() - franke(xe.cpu().numpy())).max())
+    nt = n_points + 6
+    fl = nt ** 3 / 3.0  # symmetric indefinite factorisation
+    by = 16.0 * nt ** 3 / 6.0  # unblocked updates: each leading-triangle entry read and written per step
+    out = {"workload": f"Franke's function on {n_points} Halton points, PHS3 degree 2 (n = {nt}); eval at {m} points",
+           "fit_ms": ms_fit, "eval_ms": ms_eval, "eval_points_per_s": m / (ms_eval * 1e-3),
+           "eval_pairs_per_s": m * n_points / (ms_eval * 1e-3), "max_abs_err_vs_franke": err,
+           "factor_fp64_tflops": fl / (ms_fit * 1e-3) / 1e12,
+           "factor_update_gbs": by / (ms_fit * 1e-3) / 1e9,
+           "kernels": "interp_assemble_kernel, rook_pivot_kernel + rook_update_kernel per column (unblocked "
+                      "dsytf2_rook order), blocked solve, interp_eval_kernel"}
+    if cpu:
+        from oracle import oracle as O
+        solver = O.lapack_rook_solver()
+        if solver is not None:
+            t0 = time.perf_counter()
+            w = O.interp_fit(x, y, 3, 2, solver=solver)
+            t1 = time.perf_counter()
+            me = 20_000
+            O.interp_eval(x, w, xe[:me].cpu().numpy(), 3, 2)
+            t2 = time.perf_counter()
+            out["cpu"] = {"fit_ms": (t1 - t0) * 1e3, "kind": "reference LAPACK (OpenBLAS dsytrf_rook, the routine "
+                          "bunchkaufman! calls) + oracle assembly", "cores": O.num_threads(),
+                          "eval_points_per_s": me / (t2 - t1), "eval_sample": me}
+    return out
 
 
 def run_reference(args, cfg, n):
@@ -478,6 +554,10 @@ def main():
     e2e = {"value": n * world / (ms_e2e * 1e-3), "unit": "stencils/s", "h2d_bytes_per_step": n * cfg["dim"] * 8 + n * 8,
            "d2h_bytes_per_step": n * 8}
 
+    interp = None
+    if rank == 0 and args.interp_n > 0:
+        interp = interp_bench(pkg, torch, stream, args.interp_n, world == 1 and not args.no_cpu_baseline)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sample = args.cpu_sample or (200_000 if n >= 1_000_000 else n)
@@ -524,6 +604,7 @@ def main():
                               "kernel": "spmv_pair_kernel", "bytes": "nnz*12 + (ne+1)*8 + 2*n*8"}},
             "reordered": reordered,
             "adjoint": adjoint,
+            "interpolator": interp,
             "kernels_ms": {"knn": ms_knn_kernel, "knn_per_call_api": ms_knn, "build_headline": ms_kernel,
                            "build_fp64": float(st64.ms_build), "spmv": ms_spmv},
             "peaks": {"fp64_tflops_measured": fp64_peak.value, "fp32_tflops_measured": fp32_peak.value,

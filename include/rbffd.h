@@ -183,6 +183,36 @@ int rbf_build_backward(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *dat
                        const double *eval, int64_t ne, const int32_t *adjl, int32_t k,
                        const int64_t *row_ptr, const double *dW, double *ddata, double *deval);
 
+/* ---- global interpolation ------------------------------------------------------ */
+/* Interpolator(x, y, basis) (src/interpolation.jl:22-37): the weights of the global RBF
+ * interpolant of the n points x (AoS, dim doubles each) with values y.  The collocation
+ * matrix of all points, [Phi P; P^T 0] of order nt = n + nmon (nmon = C(dim + poly_deg,
+ * dim)), is assembled on the device (8 nt^2 bytes of device memory), factorised by rook
+ * Bunch-Kaufman and solved; coef (nt doubles) receives the RBF weights then the monomial
+ * weights (rbf_weights, monomial_weights).  RBF_ERR_SINGULAR if a pivot is exactly zero
+ * (bunchkaufman!(A, true) raises). */
+int rbf_interp_fit(rbf_ctx *ctx, int32_t dim, int32_t phs, int32_t poly_deg, const double *x,
+                   int64_t n, const double *y, double *coef);
+
+/* (rbfi::Interpolator)(x) for m points xe (src/interpolation.jl:39-52): out[t] =
+ * sum_i coef[i] phi(xe_t, x_i) + sum_q coef[n + q] p_q(xe_t). */
+int rbf_interp_eval(rbf_ctx *ctx, int32_t dim, int32_t phs, int32_t poly_deg, const double *x,
+                    int64_t n, const double *coef, const double *xe, int64_t m, double *out);
+
+/* The dense symmetric-indefinite factorisation the interpolator uses, for any symmetric
+ * matrix: bunchkaufman!(Symmetric(A, :U), true) -> LAPACK dsytrf_rook (UPLO = 'U'), the
+ * same pivots and the same per-entry arithmetic as the unblocked dsytf2_rook.  On return A
+ * holds U and D as dsytrf_rook leaves them, except that each step's interchanges are also
+ * applied to the factor columns computed before it (the form LAPACK's dsyconvf_rook
+ * produces with WAY = 'C'; the 2x2 blocks of D stay in place); ipiv is LAPACK's rook ipiv
+ * (1-based, negative for 2x2 blocks).  info > 0: D(info, info) is exactly zero. */
+int rbf_sytrf_rook(rbf_ctx *ctx, int64_t n, double *A, int64_t lda, int32_t *ipiv, int64_t *info);
+
+/* Solve A X = B (nrhs columns, leading dimension ldb, overwritten) with the factors of
+ * rbf_sytrf_rook (ldiv! of the BunchKaufman object, LAPACK dsytrs_rook's result). */
+int rbf_sytrs_rook(rbf_ctx *ctx, int64_t n, int32_t nrhs, const double *A, int64_t lda,
+                   const int32_t *ipiv, double *B, int64_t ldb);
+
 /* ---- apply ------------------------------------------------------------------ */
 /* Y = alpha * W X + beta * Y for nf fields, W the op_index-th operator of a built
  * CSR (ne x ns).  Replaces _eval_op / mul! (src/operators/operators.jl:217-218,

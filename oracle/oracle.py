@@ -82,6 +82,9 @@ def lib():
         L.orc_knn_grid.restype = ctypes.c_int
         L.orc_knn_grid.argtypes = [P, i64, P, i64, ctypes.c_int, ctypes.c_int, P, ctypes.c_int]
         L.orc_num_threads.restype = ctypes.c_int
+        L.orc_interp_matrix.restype = ctypes.c_int
+        L.orc_interp_matrix.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, i64, P]
+        L.orc_interp_eval.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, i64, P, P, i64, P, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -287,3 +290,129 @@ def spmm(csr: CSR, x, op_index=0, alpha=1.0, beta=0.0, y=None, nthreads=0):
 
 def num_threads():
     return lib().orc_num_threads()
+
+
+# ---------------------------------------------------------------- global interpolation
+def interp_matrix(x, phs, poly_deg):
+    """Upper triangle of the Interpolator's collocation matrix (src/interpolation.jl:27-31),
+    column-major (Fortran order) numpy array of order n + nmon."""
+    x = _f64(x)
+    n, dim = x.shape
+    nmon = len(monomial_exponents(dim, poly_deg)) if poly_deg >= 0 else 0
+    A = np.zeros((n + nmon) * (n + nmon))
+    lib().orc_interp_matrix(dim, phs, poly_deg, _p(x), n, _p(A))
+    return A.reshape(n + nmon, n + nmon).T  # view: A[i, j] = element (i, j)
+
+
+def sytrf_rook_restated(A):
+    """The restated unblocked dsytf2_rook (UPLO = 'U') on a Fortran-ordered copy of A."""
+    n = A.shape[0]
+    F = np.asfortranarray(np.array(A, dtype=np.float64))
+    ipiv = np.zeros(n, dtype=np.int32)
+    info = lib().orc_sytrf_rook_u(n, _p(F), n, _p(ipiv))
+    return F, ipiv, info
+
+
+def rook_steps(ipiv):
+    """The pivot steps of a UPLO = 'U' rook factorisation in factorisation order: (k, kstep,
+    interchanges), k 1-based, interchanges the (row, row) swaps the step applied in order."""
+    n = len(ipiv)
+    k = n
+    steps = []
+    while k >= 1:
+        if ipiv[k - 1] > 0:
+            kp = int(ipiv[k - 1])
+            steps.append((k, 1, [(k, kp)] if kp != k else []))
+            k -= 1
+        else:
+            p, kp = -int(ipiv[k - 1]), -int(ipiv[k - 2])
+            sw = []
+            if p != k:
+                sw.append((k, p))
+            if kp != k - 1:
+                sw.append((k - 1, kp))
+            steps.append((k, 2, sw))
+            k -= 2
+    return steps
+
+
+def convert_rook_factor(F, ipiv):
+    """Apply each step's interchanges to the factor columns computed before it (columns > k),
+    in factorisation order: the factor with one row permutation, as LAPACK's dsyconvf_rook
+    (UPLO = 'U', WAY = 'C') leaves it (the D blocks are not moved).  Returns a copy."""
+    G = np.array(F, order="F", copy=True)
+    n = G.shape[0]
+    for k, _, sw in rook_steps(ipiv):
+        for a, b in sw:
+            if k < n:
+                ra, rb = G[a - 1, k:].copy(), G[b - 1, k:].copy()
+                G[a - 1, k:], G[b - 1, k:] = rb, ra
+    return G
+
+
+def interp_fit(x, y, phs, poly_deg, solver="restated"):
+    """Interpolator(x, y, basis) weights [rbf weights; monomial weights]: the collocation
+    matrix factorised by rook Bunch-Kaufman and solved (src/interpolation.jl:27-36).
+    solver "restated": this oracle's dsytf2_rook / dsytrs_rook; a callable (A, b) -> w
+    substitutes another implementation of the same LAPACK routines."""
+    x = _f64(x)
+    n = x.shape[0]
+    A = interp_matrix(x, phs, poly_deg)
+    b = np.zeros(A.shape[0])
+    b[:n] = np.asarray(y, np.float64)
+    if callable(solver):
+        return solver(A, b)
+    F, ipiv, info = sytrf_rook_restated(A)
+    if info != 0:
+        raise np.linalg.LinAlgError("singular collocation matrix")
+    return sytrs_rook(F, ipiv, b)[:, 0]
+
+
+def interp_eval(x, coef, xe, phs, poly_deg, nthreads=0):
+    """(rbfi::Interpolator)(xe) for every row of xe (src/interpolation.jl:39-52)."""
+    x, xe, coef = _f64(x), _f64(xe), _f64(coef)
+    n, dim = x.shape
+    m = xe.shape[0]
+    out = np.zeros(m)
+    lib().orc_interp_eval(dim, phs, poly_deg, _p(x), n, _p(coef), _p(xe), m, _p(out), nthreads)
+    return out
+
+
+def lapack_rook_solver():
+    """(A, b) -> x through LAPACK's dsytrf_rook / dsytrs_rook (UPLO = 'U') from scipy's bundled
+    OpenBLAS -- the routines bunchkaufman!(A, true) and its ldiv! call; None if not found."""
+    import glob
+    import os as _os
+    try:
+        import scipy
+    except ImportError:
+        return None
+    L = None
+    for p in glob.glob(_os.path.join(_os.path.dirname(scipy.__file__), "..", "scipy.libs", "libscipy_openblas*.so")):
+        cand = ctypes.CDLL(p)
+        if hasattr(cand, "scipy_dsytrf_rook_") and hasattr(cand, "scipy_dsytrs_rook_"):
+            L = cand
+            break
+    if L is None:
+        return None
+
+    def solve(A, b):
+        n = A.shape[0]
+        F = np.asfortranarray(A)
+        ip = np.zeros(n, dtype=np.int32)
+        lw = 64 * n
+        w = np.zeros(lw)
+        info = ctypes.c_int(0)
+        N, LW, R = ctypes.c_int(n), ctypes.c_int(lw), ctypes.c_int(1)
+        V = ctypes.c_void_p
+        L.scipy_dsytrf_rook_(ctypes.c_char_p(b"U"), ctypes.byref(N), F.ctypes.data_as(V), ctypes.byref(N),
+                             ip.ctypes.data_as(V), w.ctypes.data_as(V), ctypes.byref(LW), ctypes.byref(info),
+                             ctypes.c_size_t(1))
+        if info.value != 0:
+            raise np.linalg.LinAlgError("singular collocation matrix")
+        B = np.asfortranarray(np.array(b, dtype=np.float64).reshape(n, 1))
+        L.scipy_dsytrs_rook_(ctypes.c_char_p(b"U"), ctypes.byref(N), ctypes.byref(R), F.ctypes.data_as(V),
+                             ctypes.byref(N), ip.ctypes.data_as(V), B.ctypes.data_as(V), ctypes.byref(N),
+                             ctypes.byref(info), ctypes.c_size_t(1))
+        return B[:, 0]
+    return solve

@@ -897,3 +897,48 @@ int orc_num_threads(void) {
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------ */
+/* global interpolation: Interpolator(x, y, basis) (src/interpolation.jl:22-37) */
+/* ------------------------------------------------------------------------ */
+/* Upper triangle of the collocation matrix of all n points (column-major, order
+   nt = n + nmon, leading dimension nt), as _build_collocation_matrix!
+   (src/solve/assembly.jl:95-115) fills it: phi(x_i, x_j) for i <= j < n, P(x_i) in the
+   polynomial columns, zeros in the polynomial block. */
+int orc_interp_matrix(int dim, int phs, int poly_deg, const double *x, int64_t n, double *A) {
+    int exps[64 * MAXDIM];
+    int nmon = orc_monomial_exponents(dim, poly_deg, exps);
+    int64_t nt = n + nmon;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t j = 0; j < n; j++)
+        for (int64_t i = 0; i <= j; i++) A[j * nt + i] = orc_phs_phi(phs, x + i * dim, x + j * dim, dim);
+    for (int m = 0; m < nmon; m++) {
+        double *col = A + (n + m) * nt;
+        for (int64_t i = 0; i < n; i++) col[i] = mono_prod(exps + m * dim, x + i * dim, dim);
+        for (int64_t i = n; i <= n + m; i++) col[i] = 0.0;
+    }
+    return nmon;
+}
+
+/* (rbfi::Interpolator)(x) (src/interpolation.jl:39-50) at m points: the RBF sum over the
+   n centres in order, then the dot product of the monomial weights with P(x) in order,
+   then their sum.  coef = [rbf weights (n); monomial weights (nmon)]. */
+void orc_interp_eval(int dim, int phs, int poly_deg, const double *x, int64_t n, const double *coef,
+                     const double *xe, int64_t m, double *out, int nthreads) {
+    int exps[64 * MAXDIM];
+    int nmon = orc_monomial_exponents(dim, poly_deg, exps);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t t = 0; t < m; t++) {
+        const double *p = xe + t * dim;
+        double rbf = 0.0;
+        for (int64_t i = 0; i < n; i++) rbf = rbf + coef[i] * orc_phs_phi(phs, p, x + i * dim, dim);
+        double poly = 0.0;
+        for (int q = 0; q < nmon; q++) poly = poly + coef[n + q] * mono_prod(exps + q * dim, p, dim);
+        out[t] = rbf + poly;
+    }
+}

@@ -37,7 +37,7 @@ __all__ = [
     "laplacian", "partial", "gradient", "jacobian", "regrid", "directional", "Directional", "RadialBasisOperator",
     "WeightsCSR", "WeightsSELL",
     "weights", "update_weights", "mul", "DimensionMismatch", "SingularException", "Context", "build_library",
-    "build_weights", "build_weights_backward", "build_weights_differentiable", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph", "reorder_points",
+    "Interpolator", "sytrf_rook", "sytrs_rook", "build_weights", "build_weights_backward", "build_weights_differentiable", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph", "reorder_points",
 ]
 
 build_library = _native.build_library
@@ -680,6 +680,99 @@ def build_weights_differentiable(ops, data, eval_points, adjl, basis, *, ctx=Non
 
     x = data if _is_torch(data) else torch.as_tensor(np.asarray(data, np.float64))
     return _BuildFn.apply(x, eval_points)
+
+
+class Interpolator:
+    """Global RBF interpolant, Interpolator(x, y, basis=PHS()) (src/interpolation.jl:22-37):
+    the collocation matrix of all points is assembled, factorised (rook Bunch-Kaufman) and
+    solved on the GPU.  Calling it evaluates at one point (a length-dim vector: a float) or
+    at many (an (m, dim) array: an array of m values) (src/interpolation.jl:39-52)."""
+
+    def __init__(self, x, y, basis=None, *, ctx: Context | None = None):
+        torch = _torch()
+        basis = basis if basis is not None else PHS()
+        d = _points(x, "x")
+        n, dim = d.shape
+        yy = y.to(torch.float64).contiguous() if _is_torch(y) else np.ascontiguousarray(np.asarray(y, np.float64))
+        if yy.ndim != 1 or yy.shape[0] != n:
+            raise DimensionMismatch("y must hold one value per point")
+        self.ctx = ctx or Context.default(_device_of(d, yy))
+        dev = torch.device("cuda", self.ctx.device)
+        self.x = _to_device(d, self.ctx)
+        self.y = y
+        self.rbf_basis = basis
+        self.dim = dim
+        nmon = math.comb(dim + basis.poly_deg, dim) if basis.poly_deg >= 0 else 0
+        coef = torch.empty(n + nmon, dtype=torch.float64, device=dev)
+        self.ctx.check(self.ctx.lib.rbf_interp_fit(self.ctx.h, dim, basis.order, basis.poly_deg, _ptr(self.x), n,
+                                                   _ptr(_to_device(yy, self.ctx)), _ptr(coef)))
+        self.coef = coef
+        self.rbf_weights = coef[:n]
+        self.monomial_weights = coef[n:]
+        self._in_type = "torch.Tensor" if _is_torch(x) else "numpy.ndarray"
+        self._out_type = "torch.float64" if _is_torch(y) else "float64"
+
+    def __call__(self, xe):
+        torch = _torch()
+        single = False
+        if _is_torch(xe):
+            q = xe.to(torch.float64)
+        else:
+            q = np.asarray(xe, np.float64)
+        if q.ndim == 1:
+            if q.shape[0] != self.dim:
+                raise DimensionMismatch("point dimension differs from the interpolator's")
+            q = q.reshape(1, -1)
+            single = True
+        if q.ndim != 2 or q.shape[1] != self.dim:
+            raise DimensionMismatch("points must be (m, dim)")
+        qd = _to_device(q, self.ctx)
+        m = qd.shape[0]
+        out = torch.empty(m, dtype=torch.float64, device=qd.device)
+        self.ctx.check(self.ctx.lib.rbf_interp_eval(self.ctx.h, self.dim, self.rbf_basis.order,
+                                                    self.rbf_basis.poly_deg, _ptr(self.x), self.x.shape[0],
+                                                    _ptr(self.coef), _ptr(qd), m, _ptr(out)))
+        if single:
+            return float(out[0])
+        if _is_torch(xe):
+            return out if xe.is_cuda else out.cpu()
+        return out.cpu().numpy()
+
+    def __repr__(self):
+        sup = {1: "¹", 3: "³", 5: "⁵", 7: "⁷"}[self.rbf_basis.order]
+        return ("Interpolator\n"
+                f"├─Input type: {self._in_type} (dim {self.dim})\n"
+                f"├─Output type: {self._out_type}\n"
+                f"├─Number of points: {self.x.shape[0]}\n"
+                f"└─Basis: Polyharmonic spline (r{sup}) with degree {self.rbf_basis.poly_deg} Monomial")
+
+
+def sytrf_rook(A, *, ctx: Context | None = None):
+    """bunchkaufman!(Symmetric(A, :U), true) on the GPU: (factors, ipiv, info) of the dense
+    symmetric matrix A (its upper triangle is read), LAPACK dsytrf_rook's pivots and
+    arithmetic; the factor columns carry the later interchanges (dsyconvf_rook form)."""
+    torch = _torch()
+    ctx = ctx or Context.default(_device_of(A))
+    F = _to_device(A, ctx).t().contiguous()  # column-major storage of A
+    n = F.shape[0]
+    ipiv = torch.empty(n, dtype=torch.int32, device=F.device)
+    info = ctypes.c_int64(0)
+    ctx.check(ctx.lib.rbf_sytrf_rook(ctx.h, n, _ptr(F), n, _ptr(ipiv), ctypes.byref(info)))
+    return F.t(), ipiv, int(info.value)
+
+
+def sytrs_rook(F, ipiv, b, *, ctx: Context | None = None):
+    """Solve A x = b with the factors of sytrf_rook (b: n or (n, nrhs))."""
+    torch = _torch()
+    ctx = ctx or Context.default(_device_of(F))
+    Fc = F.t().contiguous()
+    B = _to_device(b, ctx)
+    one = B.ndim == 1
+    Bc = B.reshape(B.shape[0], -1).t().contiguous()  # column-major right-hand sides
+    n = Fc.shape[0]
+    ctx.check(ctx.lib.rbf_sytrs_rook(ctx.h, n, Bc.shape[0], _ptr(Fc), n, _ptr(ipiv.to(torch.int32).contiguous()),
+                                     _ptr(Bc), n))
+    return Bc[0] if one else Bc.t()
 
 
 def reorder_points(data, k=None, ctx=None):

@@ -25,7 +25,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 
 SOURCES = ["rbf_api.cu", "knn.cu", "scan.cu", "spmm.cu", "sell.cu", "algebra.cu", "stencil_build.cu", "stencil_refined_a.cu",
            "stencil_refined_b.cu", "stencil_refined_c.cu", "batched.cu", "plan.cu", "reorder.cu", "diag.cu", "mlp.cu",
-           "mlp_tc.cu", "backward.cu"]
+           "mlp_tc.cu", "backward.cu",
+           "dense.cu"]
 
 
 def _nvcc():
@@ -116,6 +117,10 @@ SIGNATURES = {
     "rbf_build_count": (_I, [_P, _I64, _I64, _I32, _P, _P, _P]),
     "rbf_build": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _I32, _P, _P, _P, _P, _P, _P]),
     "rbf_build_backward": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _I32, _P, _P, _P, _P]),
+    "rbf_interp_fit": (_I, [_P, _I32, _I32, _I32, _P, _I64, _P, _P]),
+    "rbf_interp_eval": (_I, [_P, _I32, _I32, _I32, _P, _I64, _P, _P, _I64, _P]),
+    "rbf_sytrf_rook": (_I, [_P, _I64, _P, _I64, _P, _P]),
+    "rbf_sytrs_rook": (_I, [_P, _I64, _I32, _P, _I64, _P, _P, _I64]),
     "rbf_spmm": (_I, [_P, _I64, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _D, _D, _P, _I64]),
     "rbf_csr_to_csc": (_I, [_P, _I64, _I64, _P, _P, _P, _P, _P, _P]),
     "rbf_weights_axpby": (_I, [_P, _I64, _D, _P, _D, _P, _P]),

@@ -614,6 +614,134 @@ int rbf_build_backward(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *dat
     return RBF_OK;
 }
 
+int rbf_sytrf_rook(rbf_ctx *ctx, int64_t n, double *A, int64_t lda, int32_t *ipiv, int64_t *info) {
+    RBF_TRY(check_ctx(ctx));
+    if (n < 0 || n >= INT32_MAX || lda < std::max<int64_t>(1, n)) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "bad n / lda");
+    if ((n > 0 && (!A || !ipiv)) || !info) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null array");
+    *info = 0;
+    if (n == 0) return RBF_OK;
+    const size_t abytes = sizeof(double) * (size_t)lda * (size_t)n;
+    OutArray ao, po;
+    RBF_TRY(ao.bind(ctx, A, abytes));
+    if (ao.host) RBF_CUDA(ctx, cudaMemcpyAsync(ao.dptr, A, abytes, cudaMemcpyHostToDevice, ctx->stream));
+    RBF_TRY(po.bind(ctx, ipiv, sizeof(int32_t) * n));
+    DevBuf perm;
+    RBF_TRY(perm.alloc(ctx, sizeof(int32_t) * n));
+    RBF_TRY(rbf_sytrf_rook_device(ctx, (int)n, ao.as<double>(), lda, po.as<int32_t>(), perm.as<int32_t>(), info));
+    RBF_TRY(ao.finish(ctx));
+    RBF_TRY(po.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
+int rbf_sytrs_rook(rbf_ctx *ctx, int64_t n, int32_t nrhs, const double *A, int64_t lda, const int32_t *ipiv,
+                   double *B, int64_t ldb) {
+    RBF_TRY(check_ctx(ctx));
+    if (n < 0 || n >= INT32_MAX || nrhs < 0 || lda < std::max<int64_t>(1, n) || ldb < std::max<int64_t>(1, n))
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "bad n / nrhs / lda / ldb");
+    if (n == 0 || nrhs == 0) return RBF_OK;
+    if (!A || !ipiv || !B) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null array");
+    const size_t bbytes = sizeof(double) * (size_t)ldb * (size_t)nrhs;
+    InArray ai, pi;
+    OutArray bo;
+    RBF_TRY(ai.bind(ctx, A, sizeof(double) * (size_t)lda * (size_t)n));
+    RBF_TRY(pi.bind(ctx, ipiv, sizeof(int32_t) * n));
+    RBF_TRY(bo.bind(ctx, B, bbytes));
+    bool ok = true;
+    RBF_TRY(rbf_check_ipiv_device(ctx, (int)n, pi.as<int32_t>(), &ok));
+    if (!ok) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "ipiv holds entries outside +-[1, n]");
+    if (bo.host) RBF_CUDA(ctx, cudaMemcpyAsync(bo.dptr, B, bbytes, cudaMemcpyHostToDevice, ctx->stream));
+    DevBuf tmp;
+    RBF_TRY(tmp.alloc(ctx, sizeof(double) * n));
+    for (int r = 0; r < nrhs; r++) {
+        double *col = bo.as<double>() + (size_t)r * ldb;
+        RBF_TRY(rbf_sytrs_rook_device(ctx, (int)n, ai.as<double>(), lda, pi.as<int32_t>(), nullptr, col,
+                                      tmp.as<double>()));
+        RBF_CUDA(ctx, cudaMemcpyAsync(col, tmp.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    RBF_TRY(bo.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
+}  // extern "C"
+
+namespace {
+int interp_args(rbf_ctx *ctx, int32_t dim, int32_t phs, int32_t poly_deg, int64_t n, int8_t (*ex)[3], int *nmon) {
+    if (dim < 1 || dim > 3) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "dim must be 1, 2 or 3 (got %d)", dim);
+    if (!(phs == 1 || phs == 3 || phs == 5 || phs == 7))
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "n must be 1, 3, 5, or 7 (got n=%d)", phs);
+    if (poly_deg < -1) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "poly_deg must be >= -1 (got %d)", poly_deg);
+    if (poly_deg >= 0 && binom(dim + poly_deg, dim) > RBF_MAX_SYSTEM)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "more than %d monomials", RBF_MAX_SYSTEM);
+    *nmon = monomial_exponents(dim, poly_deg, ex);
+    if (n < 1 || n + *nmon >= 2000000000LL) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "bad number of points");
+    return RBF_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int rbf_interp_fit(rbf_ctx *ctx, int32_t dim, int32_t phs, int32_t poly_deg, const double *x, int64_t n,
+                   const double *y, double *coef) {
+    RBF_TRY(check_ctx(ctx));
+    int8_t ex[RBF_MAX_SYSTEM][3];
+    int nmon = 0;
+    RBF_TRY(interp_args(ctx, dim, phs, poly_deg, n, ex, &nmon));
+    if (!x || !y || !coef) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null array");
+    const int64_t nt = n + nmon;
+    const size_t abytes = sizeof(double) * (size_t)nt * (size_t)nt;
+    size_t free_b = 0, total_b = 0;
+    RBF_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
+    if (abytes + (size_t)nt * 64 > free_b / 10 * 9)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the %lld x %lld collocation matrix (%.1f GB) does not fit in device memory",
+                        (long long)nt, (long long)nt, abytes / 1e9);
+    InArray xi, yi;
+    OutArray co;
+    RBF_TRY(xi.bind(ctx, x, sizeof(double) * n * dim));
+    RBF_TRY(yi.bind(ctx, y, sizeof(double) * n));
+    RBF_TRY(co.bind(ctx, coef, sizeof(double) * nt));
+    DevBuf A, piv, perm, rhs;
+    RBF_TRY(A.alloc(ctx, abytes));
+    RBF_TRY(piv.alloc(ctx, sizeof(int32_t) * nt));
+    RBF_TRY(perm.alloc(ctx, sizeof(int32_t) * nt));
+    RBF_TRY(rhs.alloc(ctx, sizeof(double) * nt));
+    RBF_TRY(rbf_interp_assemble_device(ctx, dim, phs, nmon, ex, xi.as<double>(), (int)n, A.as<double>(), nt));
+    int64_t info = 0;
+    RBF_TRY(rbf_sytrf_rook_device(ctx, (int)nt, A.as<double>(), nt, piv.as<int32_t>(), perm.as<int32_t>(), &info));
+    if (info) return rbf_fail(ctx, RBF_ERR_SINGULAR, "the collocation matrix is singular (D(%lld,%lld) = 0)",
+                              (long long)info, (long long)info);
+    RBF_CUDA(ctx, cudaMemcpyAsync(rhs.ptr, yi.dptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (nmon) RBF_CUDA(ctx, cudaMemsetAsync(rhs.as<double>() + n, 0, sizeof(double) * nmon, ctx->stream));
+    RBF_TRY(rbf_sytrs_rook_device(ctx, (int)nt, A.as<double>(), nt, piv.as<int32_t>(), perm.as<int32_t>(),
+                                  rhs.as<double>(), co.as<double>()));
+    RBF_TRY(co.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
+int rbf_interp_eval(rbf_ctx *ctx, int32_t dim, int32_t phs, int32_t poly_deg, const double *x, int64_t n,
+                    const double *coef, const double *xe, int64_t m, double *out) {
+    RBF_TRY(check_ctx(ctx));
+    int8_t ex[RBF_MAX_SYSTEM][3];
+    int nmon = 0;
+    RBF_TRY(interp_args(ctx, dim, phs, poly_deg, n, ex, &nmon));
+    if (m < 0) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "m must be >= 0");
+    if (m == 0) return RBF_OK;
+    if (!x || !coef || !xe || !out) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null array");
+    InArray xi, ci, ei;
+    OutArray oo;
+    RBF_TRY(xi.bind(ctx, x, sizeof(double) * n * dim));
+    RBF_TRY(ci.bind(ctx, coef, sizeof(double) * (n + nmon)));
+    RBF_TRY(ei.bind(ctx, xe, sizeof(double) * m * dim));
+    RBF_TRY(oo.bind(ctx, out, sizeof(double) * m));
+    RBF_TRY(rbf_interp_eval_device(ctx, dim, phs, nmon, ex, xi.as<double>(), (int)n, ci.as<double>(), ei.as<double>(), m,
+                                   oo.as<double>()));
+    RBF_TRY(oo.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
 int rbf_weights_axpby(rbf_ctx *ctx, int64_t nnz, double alpha, const double *a, double beta, const double *b,
                       double *out) {
     RBF_TRY(check_ctx(ctx));

@@ -119,6 +119,15 @@ int rbf_boundary_map_device(rbf_ctx *ctx, int64_t n, const uint8_t *d_isb, int32
 
 int rbf_check_indices(rbf_ctx *ctx, const int32_t *d_idx, int64_t n, int32_t hi, bool *ok);
 int rbf_backward_launch(rbf_ctx *ctx, const StencilParams &P, const double *dW, double *ddata, double *deval);
+int rbf_sytrf_rook_device(rbf_ctx *ctx, int nt, double *dA, int64_t lda, int32_t *dipiv, int32_t *dperm,
+                          int64_t *info);
+int rbf_check_ipiv_device(rbf_ctx *ctx, int nt, const int32_t *dipiv, bool *ok);
+int rbf_sytrs_rook_device(rbf_ctx *ctx, int nt, const double *dA, int64_t lda, const int32_t *dipiv,
+                          const int32_t *dperm, const double *db, double *dx);
+int rbf_interp_assemble_device(rbf_ctx *ctx, int dim, int phs, int nmon, const int8_t (*exps)[3], const double *dx,
+                               int n, double *dA, int64_t lda);
+int rbf_interp_eval_device(rbf_ctx *ctx, int dim, int phs, int nmon, const int8_t (*exps)[3], const double *dx, int n,
+                           const double *dcoef, const double *dxe, int64_t m, double *dout);
 int rbf_exclusive_scan_i64(rbf_ctx *ctx, const int64_t *d_in, int64_t *d_out, int64_t n,
                            int64_t *total);
 // operator algebra on built weights (algebra.cu)
