@@ -201,7 +201,8 @@ int rbf_interp_eval(rbf_ctx *ctx, int32_t dim, int32_t phs, int32_t poly_deg, co
 
 /* The dense symmetric-indefinite factorisation the interpolator uses, for any symmetric
  * matrix: bunchkaufman!(Symmetric(A, :U), true) -> LAPACK dsytrf_rook (UPLO = 'U'), the
- * same pivots and the same per-entry arithmetic as the unblocked dsytf2_rook.  On return A
+ * same pivots and per-entry arithmetic as the unblocked dsytf2_rook (its rank-1 / rank-2
+ * updates as fused multiply-adds, as optimised BLAS kernels evaluate them).  On return A
  * holds U and D as dsytrf_rook leaves them, except that each step's interchanges are also
  * applied to the factor columns computed before it (the form LAPACK's dsyconvf_rook
  * produces with WAY = 'C'; the 2x2 blocks of D stay in place); ipiv is LAPACK's rook ipiv

@@ -69,6 +69,8 @@ def lib():
         L.orc_mono_normal.argtypes = [ctypes.c_int, ctypes.c_int, P, P, P, P]
         L.orc_sytrf_rook_u.restype = ctypes.c_int
         L.orc_sytrf_rook_u.argtypes = [ctypes.c_int, P, ctypes.c_int, P]
+        L.orc_sytrf_rook_u_fma.restype = ctypes.c_int
+        L.orc_sytrf_rook_u_fma.argtypes = [ctypes.c_int, P, ctypes.c_int, P]
         L.orc_sytrs_rook_u.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int, P, P, ctypes.c_int]
         L.orc_assemble.restype = ctypes.c_int
         L.orc_assemble.argtypes = [P, P, ctypes.c_int, P, P, P, P]
@@ -304,12 +306,14 @@ def interp_matrix(x, phs, poly_deg):
     return A.reshape(n + nmon, n + nmon).T  # view: A[i, j] = element (i, j)
 
 
-def sytrf_rook_restated(A):
-    """The restated unblocked dsytf2_rook (UPLO = 'U') on a Fortran-ordered copy of A."""
+def sytrf_rook_restated(A, fused=False):
+    """The restated unblocked dsytf2_rook (UPLO = 'U') on a Fortran-ordered copy of A; fused:
+    its rank-1 / rank-2 updates as fused multiply-adds (as optimised BLAS kernels do)."""
     n = A.shape[0]
     F = np.asfortranarray(np.array(A, dtype=np.float64))
     ipiv = np.zeros(n, dtype=np.int32)
-    info = lib().orc_sytrf_rook_u(n, _p(F), n, _p(ipiv))
+    f = lib().orc_sytrf_rook_u_fma if fused else lib().orc_sytrf_rook_u
+    info = f(n, _p(F), n, _p(ipiv))
     return F, ipiv, info
 
 

@@ -313,8 +313,11 @@ static int idamax_row(int n, const double *a, int lda, int i, int j0) { /* cols 
     return best;
 }
 
-/* returns INFO (0 ok, >0: D(info,info) is exactly zero) */
-int orc_sytrf_rook_u(int n, double *a, int lda, int *ipiv) {
+/* returns INFO (0 ok, >0: D(info,info) is exactly zero).  fused = 1: the rank-1 / rank-2
+   updates of the leading triangle as fused multiply-adds (the form optimised BLAS kernels
+   such as OpenBLAS's dsyr / dgemm evaluate), otherwise products and sums rounded separately
+   as the reference Fortran BLAS writes them. */
+static int sytrf_rook_u(int n, double *a, int lda, int *ipiv, int fused) {
     const double alpha = (1.0 + sqrt(17.0)) / 8.0;
     const double sfmin = 2.2250738585072014e-308;
     int info = 0;
@@ -374,7 +377,8 @@ int orc_sytrf_rook_u(int n, double *a, int lda, int *ipiv) {
                         for (int j = 1; j <= k - 1; j++) {
                             if (A_(j, k) != 0.0) {
                                 double temp = -d11 * A_(j, k);
-                                for (int i = 1; i <= j; i++) A_(i, j) = A_(i, j) + A_(i, k) * temp;
+                                for (int i = 1; i <= j; i++)
+                                    A_(i, j) = fused ? fma(A_(i, k), temp, A_(i, j)) : A_(i, j) + A_(i, k) * temp;
                             }
                         }
                         for (int i = 1; i <= k - 1; i++) A_(i, k) = d11 * A_(i, k);
@@ -384,7 +388,8 @@ int orc_sytrf_rook_u(int n, double *a, int lda, int *ipiv) {
                         for (int j = 1; j <= k - 1; j++) {
                             if (A_(j, k) != 0.0) {
                                 double temp = -d11 * A_(j, k);
-                                for (int i = 1; i <= j; i++) A_(i, j) = A_(i, j) + A_(i, k) * temp;
+                                for (int i = 1; i <= j; i++)
+                                    A_(i, j) = fused ? fma(A_(i, k), temp, A_(i, j)) : A_(i, j) + A_(i, k) * temp;
                             }
                         }
                     }
@@ -398,8 +403,12 @@ int orc_sytrf_rook_u(int n, double *a, int lda, int *ipiv) {
                     for (int j = k - 2; j >= 1; j--) {
                         double wkm1 = t * (d11 * A_(j, k - 1) - A_(j, k));
                         double wk = t * (d22 * A_(j, k) - A_(j, k - 1));
-                        for (int i = j; i >= 1; i--)
-                            A_(i, j) = A_(i, j) - (A_(i, k) / d12) * wk - (A_(i, k - 1) / d12) * wkm1;
+                        for (int i = j; i >= 1; i--) {
+                            if (fused)
+                                A_(i, j) = fma(-(A_(i, k - 1) / d12), wkm1, fma(-(A_(i, k) / d12), wk, A_(i, j)));
+                            else
+                                A_(i, j) = A_(i, j) - (A_(i, k) / d12) * wk - (A_(i, k - 1) / d12) * wkm1;
+                        }
                         A_(j, k) = wk / d12;
                         A_(j, k - 1) = wkm1 / d12;
                     }
@@ -412,6 +421,9 @@ int orc_sytrf_rook_u(int n, double *a, int lda, int *ipiv) {
     }
     return info;
 }
+
+int orc_sytrf_rook_u(int n, double *a, int lda, int *ipiv) { return sytrf_rook_u(n, a, lda, ipiv, 0); }
+int orc_sytrf_rook_u_fma(int n, double *a, int lda, int *ipiv) { return sytrf_rook_u(n, a, lda, ipiv, 1); }
 
 void orc_sytrs_rook_u(int n, int nrhs, const double *a, int lda, const int *ipiv, double *bm, int ldb) {
     int k = n;

@@ -4,24 +4,27 @@
 // Fit.  The collocation matrix of all n points, [Φ P; Pᵀ 0] of order nt = n + nmon (upper
 // triangle, column-major, as _build_collocation_matrix! fills it, src/solve/assembly.jl:95-115),
 // is factorised by rook-pivoted Bunch-Kaufman (bunchkaufman!(A, true) -> LAPACK dsytrf_rook,
-// UPLO = 'U') and solved.  The factorisation follows the unblocked dsytf2_rook step by step:
-// for k = nt down to 1 one launch decides the pivot (one block: the rook search with block
-// arg-max reductions, first index on ties as idamax, the interchanges, the pivot block) and
-// one launch applies the rank-1 or rank-2 update to the leading upper triangle (every SM;
-// the per-element arithmetic is LAPACK's, products and sums rounded separately, so the
-// factors equal the oracle's restatement bit for bit).  The steps are decided on the device:
-// the host launches a (pivot, update) pair for every k and a step whose column a 2x2 pivot
-// already consumed does nothing, so the whole factorisation is queued without a host sync.
-// Column writes that must follow the update (the 1x1 column scaling, the 2x2 multipliers)
-// run at the start of the next pivot launch.  The update launch also applies the step's
-// interchanges to the factor columns already computed (columns > k): the factor is left in
-// the converted form of LAPACK's dsyconvf_rook (one row permutation, kept in perm), which
-// the blocked solve needs.
+// UPLO = 'U') and solved.  The factorisation follows the unblocked dsytf2_rook step by step,
+// one launch per column k = nt .. 1: every SM applies the rank-1 or rank-2 update of the
+// current step to the leading upper triangle (the per-element arithmetic is LAPACK's, with
+// the update's multiply-adds fused as optimised BLAS kernels evaluate them, so the factors
+// equal the oracle's restatement in that form bit for bit) and the step's interchanges to the
+// factor columns already computed (columns > k: the converted form of LAPACK's
+// dsyconvf_rook, one row permutation kept in perm, which the blocked solve needs).  The
+// pivot decisions are made on the device, so the whole factorisation is queued without a host
+// sync: the block that owns the next pivot column updates it first and settles the common
+// case (a 1x1 pivot without interchange depends on that column alone); the last block to
+// finish (an atomic count, no waiting) writes the columns that must follow the update (the
+// 1x1 scaling, the 2x2 multipliers) and otherwise runs the full rook search (block arg-max
+// reductions, first index on ties as idamax).  A launch whose column a 2x2 pivot consumed
+// does nothing.  Step records are double-buffered: a decision never overwrites the record
+// that blocks of the running launch read.
 //
 // Roofline: each 1x1 step reads and writes the k(k-1)/2 entries of the leading triangle once
-// (16 bytes per entry, FP64 arithmetic 2 flops per entry); on GB300 the FP64 pipe and HBM
-// give similar bounds (~1 TFLOP/s vs ~7 TB/s / 16 B x 2 flops = 0.9 TFLOP/s), so the
-// unblocked order costs little against a blocked one and keeps LAPACK's rounding.
+// (16 bytes and one FP64 FMA per entry); on GB300 the FP64 pipe and HBM give similar bounds
+// (~0.5 T FMA/s vs ~7 TB/s / 16 B = 0.44 T entries/s), so the unblocked order costs little
+// against a blocked one (which would be FP64-bound at the same rate) and keeps LAPACK's
+// per-step rounding.
 //
 // Solve (converted form, A = P U D Uᵀ Pᵀ): b[perm], U⁻¹ by 64-column chunks from the bottom
 // (one block for the chunk's triangle, every SM for the rows above), D⁻¹ (1x1 / 2x2 blocks as
@@ -46,18 +49,21 @@ constexpr double BK_ALPHA_NUM = 1.0;  // alpha = (1 + sqrt(17)) / 8 (dsytf2_rook
 // blocks' writes: through L2 (never a line this SM cached earlier in the launch)
 #define AG(i, j) __ldcg(&A_(i, j))
 
-struct RookState {
-    int cur;     // the next column to factorise (1-based); pivot launches for other k do nothing
-    int info;    // first k with an exactly zero (or NaN) pivot column, 0 if none
-    int err;     // 1: rook search did not terminate within its bound
-    // the step decided by the last pivot launch, applied by the update launch of the same k
-    int k, kstep, mode, nswap;  // mode 0: 1x1 (d11 = 1/A(k,k)), 1: 1x1 tiny pivot, 2: 2x2, 3: none
-    int sw_a[2], sw_b[2];       // its interchanges, in order (1-based rows)
+// one pivot step (dsytf2_rook): mode 0: 1x1, update with d11 = 1/A(k,k), then the column is
+// scaled by d11; 1: 1x1 tiny pivot, the column already divided by d11 = A(k,k); 2: 2x2 (d11,
+// d12, d22, t as dsytf2_rook, multipliers in wk / wkm1 / u / v); 3: no update
+struct RookStep {
+    int k, kstep, mode, nswap;
+    int sw_a[2], sw_b[2];  // the step's interchanges, in order (1-based rows)
     double d11, d12, d22, t;
-    // column writes left for the next pivot launch: 1 = scale column pk by pd11, 2 = 2x2
-    // multipliers of columns pk-1, pk
-    int pend, pk;
-    double pd11, pd12;
+};
+
+struct RookState {
+    RookStep step[2];  // step[slot]: applied by the current launch; step[1 - slot]: the next one
+    int slot;
+    int spec;  // 1: the next step was decided during the current launch by its column's owner
+    int info;  // first k with an exactly zero (or NaN) pivot column, 0 if none
+    int err;   // 1: rook search did not terminate within its bound
 };
 
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
@@ -128,39 +134,25 @@ __device__ __forceinline__ void swap_el(double *A, int64_t lda, int i1, int j1, 
     A_(i2, j2) = t;
 }
 
-// the column writes that had to wait for the previous step's update
-__device__ void finish_pending(double *A, int64_t lda, RookState *st, const double *wk, const double *wkm1,
-                               int pend, int pk, double pd11, double pd12) {
-    if (pend == 1) {
-        for (int i = 1 + threadIdx.x; i <= pk - 1; i += blockDim.x) A_(i, pk) = dmul(pd11, AG(i, pk));
-    } else if (pend == 2) {
-        for (int j = 1 + threadIdx.x; j <= pk - 2; j += blockDim.x) {
-            A_(j, pk) = wk[j - 1] / pd12;
-            A_(j, pk - 1) = wkm1[j - 1] / pd12;
+// the column writes of step S that must follow its update (after every block has read the
+// pivot columns): the 1x1 column scaling, the 2x2 multipliers
+__device__ void finish_step(double *A, int64_t lda, const RookStep &S, const double *wk, const double *wkm1) {
+    const int k = S.k;
+    if (S.mode == 0) {
+        for (int i = 1 + threadIdx.x; i <= k - 1; i += blockDim.x) A_(i, k) = dmul(S.d11, AG(i, k));
+    } else if (S.mode == 2) {
+        for (int j = 1 + threadIdx.x; j <= k - 2; j += blockDim.x) {
+            A_(j, k) = wk[j - 1] / S.d12;
+            A_(j, k - 1) = wkm1[j - 1] / S.d12;
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) st->pend = 0;
 }
 
-// One block: the column writes left by the previous step, then the pivot decision of the
-// next column st->cur (dsytf2_rook), its interchanges in the leading submatrix and what the
-// update needs; the step is recorded in st for the update launch of that column.
-__device__ void rook_decide(double *A, int64_t lda, int32_t *ipiv, RookState *st, int32_t *perm, double *wk,
-                            double *wkm1, double *u, double *v, ArgMax *red) {
-    __shared__ int s_cur, s_pend, s_pk;
-    __shared__ double s_pd11, s_pd12;
-    if (threadIdx.x == 0) {
-        s_cur = __ldcg(&st->cur);
-        s_pend = __ldcg(&st->pend);
-        s_pk = __ldcg(&st->pk);
-        s_pd11 = __ldcg(&st->pd11);
-        s_pd12 = __ldcg(&st->pd12);
-    }
-    __syncthreads();
-    if (s_pend) finish_pending(A, lda, st, wk, wkm1, s_pend, s_pk, s_pd11, s_pd12);
-    if (s_cur < 1) return;
-    const int k = s_cur;
+// One block: the pivot decision of column k (dsytf2_rook), its interchanges in the leading
+// submatrix and what the update needs, recorded in *out for the update launch of column k.
+__device__ __noinline__ void rook_decide(double *A, int64_t lda, int k, int32_t *ipiv, RookState *st, RookStep *out,
+                                         int32_t *perm, double *wk, double *wkm1, double *u, double *v, ArgMax *red) {
     const double alpha = (BK_ALPHA_NUM + sqrt(17.0)) / 8.0;
     const double sfmin = 2.2250738585072014e-308;
     // ---- pivot decision (dsytf2_rook)
@@ -275,102 +267,164 @@ __device__ void rook_decide(double *A, int64_t lda, int32_t *ipiv, RookState *st
         int ns = 0;
         if (!zero_col) {
             if (kstep == 2 && p != k) {
-                st->sw_a[ns] = k;
-                st->sw_b[ns] = p;
+                out->sw_a[ns] = k;
+                out->sw_b[ns] = p;
                 ns++;
             }
             if (kp != kq) {
-                st->sw_a[ns] = kq;
-                st->sw_b[ns] = kp;
+                out->sw_a[ns] = kq;
+                out->sw_b[ns] = kp;
                 ns++;
             }
         }
         for (int s = 0; s < ns; s++) {
-            const int a = st->sw_a[s] - 1, b = st->sw_b[s] - 1;
+            const int a = out->sw_a[s] - 1, b = out->sw_b[s] - 1;
             const int32_t t = perm[a];
             perm[a] = perm[b];
             perm[b] = t;
         }
-        st->nswap = ns;
-        st->k = k;
-        st->kstep = kstep;
-        st->mode = mode;
-        st->d11 = d11;
-        st->d12 = d12;
-        st->d22 = d22;
-        st->t = tt;
+        out->nswap = ns;
+        out->k = k;
+        out->kstep = kstep;
+        out->mode = mode;
+        out->d11 = d11;
+        out->d12 = d12;
+        out->d22 = d22;
+        out->t = tt;
         if (kstep == 1) {
             ipiv[k - 1] = kp;
         } else {
             ipiv[k - 1] = -p;
             ipiv[k - 2] = -kp;
         }
-        st->cur = k - kstep;
-        st->pend = mode == 0 ? 1 : (mode == 2 ? 2 : 0);
-        st->pk = k;
-        st->pd11 = d11;
-        st->pd12 = d12;
     }
+    __syncthreads();
 }
 
-__global__ void __launch_bounds__(PIV_THREADS) rook_pivot_kernel(double *A, int64_t lda, int32_t *ipiv, RookState *st,
-                                                                 int32_t *perm, double *wk, double *wkm1, double *u,
-                                                                 double *v) {
+// The common case of the next decision, made by the block that owns column k while the other
+// blocks still update: a 1x1 pivot without interchange (|A(k,k)| >= alpha * colmax) depends
+// on column k alone.  Anything else (a zero column, the rook search) is left to the last
+// block.  Returns whether *out now holds the step.
+__device__ __noinline__ bool rook_speculate(double *A, int64_t lda, int k, int32_t *ipiv, RookStep *out, ArgMax *red) {
+    __shared__ bool s_ok;
+    const double alpha = (BK_ALPHA_NUM + sqrt(17.0)) / 8.0;
+    const double sfmin = 2.2250738585072014e-308;
+    const double absakk = fabs(AG(k, k));
+    int imax = 0;
+    double colmax = 0.0;
+    if (k > 1) {
+        imax = col_argmax(A, lda, 1, k - 1, k, red);
+        colmax = fabs(AG(imax, k));
+    }
+    if (fmax(absakk, colmax) == 0.0 || isnan(absakk) || isnan(colmax) || absakk < alpha * colmax) return false;
+    int mode = 3;
+    double d11 = 0.0;
+    if (k > 1) {
+        const double akk = AG(k, k);
+        if (fabs(akk) >= sfmin) {
+            mode = 0;
+            d11 = 1.0 / akk;
+        } else {
+            mode = 1;
+            d11 = akk;
+            for (int i = 1 + threadIdx.x; i <= k - 1; i += blockDim.x) A_(i, k) = AG(i, k) / d11;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        out->k = k;
+        out->kstep = 1;
+        out->mode = mode;
+        out->nswap = 0;
+        out->d11 = d11;
+        out->d12 = out->d22 = out->t = 0.0;
+        ipiv[k - 1] = k;
+        s_ok = true;
+    }
+    __syncthreads();
+    return s_ok;
+}
+
+__global__ void __launch_bounds__(PIV_THREADS) rook_pivot_kernel(double *A, int64_t lda, int k, int32_t *ipiv,
+                                                                 RookState *st, int32_t *perm, double *wk,
+                                                                 double *wkm1, double *u, double *v) {
     __shared__ ArgMax red[32];
-    rook_decide(A, lda, ipiv, st, perm, wk, wkm1, u, v, red);
+    rook_decide(A, lda, k, ipiv, st, &st->step[0], perm, wk, wkm1, u, v, red);
 }
 
-// The update of step kk: rank-1 / rank-2 update of the leading upper triangle and the step's
-// interchanges applied to the factor columns kk+1..nt (the converted form).  The last block to
-// finish (an atomic count, no waiting) makes the next pivot decision.
+// The update of step kk: rank-1 / rank-2 update of the leading upper triangle (one column per
+// block at a time, each block's columns largest first) and the step's interchanges applied to
+// the factor columns kk+1..nt (the converted form).  The block that owns the next pivot column
+// updates it first and decides the next step when the common case allows; the last block to
+// finish (an atomic count, no waiting) writes this step's columns and makes the decision
+// otherwise.
 constexpr int UPD_THREADS = 256;
 constexpr int UPD_UNROLL = 4;
 
-__global__ void __launch_bounds__(UPD_THREADS) rook_step_kernel(double *A, int64_t lda, int kk, int nt, int32_t *ipiv,
-                                                                RookState *st, int32_t *perm, double *wk,
-                                                                double *wkm1, double *u, double *v,
-                                                                unsigned int *count) {
+__global__ void __launch_bounds__(UPD_THREADS, 6) rook_step_kernel(double *A, int64_t lda, int kk, int nt, int32_t *ipiv,
+                                                                   RookState *st, int32_t *perm, double *wk,
+                                                                   double *wkm1, double *u, double *v,
+                                                                   unsigned int *count) {
     __shared__ ArgMax red[32];
     __shared__ bool s_last;
-    if (st->k != kk) return;
-    const int k = kk, mode = st->mode;
-    const int nb = gridDim.x;
-    if (mode == 0 || mode == 1) {
-        const double d11 = st->d11;
+    const int slot = st->slot;
+    const RookStep *S = &st->step[slot];
+    if (S->k != kk) return;
+    const int k = kk, mode = S->mode, next = k - S->kstep;
+    const int nb = gridDim.x, bid = blockIdx.x;
+    RookStep *nxt = &st->step[1 - slot];
+    bool spec = next >= 1 && bid == (next - 1) % nb;
+    const int hi = mode == 0 || mode == 1 ? k - 1 : (mode == 2 ? k - 2 : 0);
+    if (bid + 1 <= hi) {
         const double *colk = &A_(1, k);
-        for (int j = blockIdx.x + 1; j <= k - 1; j += nb) {
-            const double xj = colk[j - 1];
-            if (xj == 0.0) continue;
-            const double temp = dmul(-d11, xj);
+        for (int j = bid + 1 + ((hi - bid - 1) / nb) * nb; j >= 1; j -= nb) {
             double *colj = &A_(1, j);
-            for (int i0 = threadIdx.x; i0 < j; i0 += UPD_UNROLL * UPD_THREADS) {
-                double c[UPD_UNROLL], x[UPD_UNROLL];
+            if (mode == 2) {
+                const double a = wk[j - 1], b = wkm1[j - 1];
+                for (int i = threadIdx.x; i < j; i += blockDim.x) colj[i] = __fma_rn(-v[i], b, __fma_rn(-u[i], a, colj[i]));
+            } else {
+                const double xj = colk[j - 1];
+                if (xj != 0.0) {
+                    const double temp = dmul(-S->d11, xj);
+                    for (int i0 = threadIdx.x; i0 < j; i0 += UPD_UNROLL * UPD_THREADS) {
+                        double c[UPD_UNROLL], x[UPD_UNROLL];
 #pragma unroll
-                for (int q = 0; q < UPD_UNROLL; q++) {
-                    const int i = i0 + q * UPD_THREADS;
-                    if (i < j) {
-                        c[q] = colj[i];
-                        x[q] = colk[i];
+                        for (int q = 0; q < UPD_UNROLL; q++) {
+                            const int i = i0 + q * UPD_THREADS;
+                            if (i < j) {
+                                c[q] = colj[i];
+                                x[q] = colk[i];
+                            }
+                        }
+#pragma unroll
+                        for (int q = 0; q < UPD_UNROLL; q++) {
+                            const int i = i0 + q * UPD_THREADS;
+                            if (i < j) colj[i] = __fma_rn(x[q], temp, c[q]);
+                        }
                     }
                 }
-#pragma unroll
-                for (int q = 0; q < UPD_UNROLL; q++) {
-                    const int i = i0 + q * UPD_THREADS;
-                    if (i < j) colj[i] = dadd(c[q], dmul(x[q], temp));
+            }
+            if (spec && j == next) {
+                __syncthreads();
+                if (rook_speculate(A, lda, next, ipiv, nxt, red) && threadIdx.x == 0) {
+                    __threadfence();
+                    st->spec = 1;
                 }
+                spec = false;
             }
         }
-    } else if (mode == 2) {
-        for (int j = blockIdx.x + 1; j <= k - 2; j += nb) {
-            const double a = wk[j - 1], b = wkm1[j - 1];
-            double *colj = &A_(1, j);
-            for (int i = threadIdx.x; i < j; i += blockDim.x) colj[i] = dsub(dsub(colj[i], dmul(u[i], a)), dmul(v[i], b));
+    }
+    if (spec) {  // the owner had no column to update (a step without update)
+        __syncthreads();
+        if (rook_speculate(A, lda, next, ipiv, nxt, red) && threadIdx.x == 0) {
+            __threadfence();
+            st->spec = 1;
         }
     }
-    const int ns = st->nswap;
+    const int ns = S->nswap;
     if (ns) {
-        const int a0 = st->sw_a[0], b0 = st->sw_b[0], a1 = st->sw_a[1], b1 = st->sw_b[1];
-        const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)nb * blockDim.x;
+        const int a0 = S->sw_a[0], b0 = S->sw_b[0], a1 = S->sw_a[1], b1 = S->sw_b[1];
+        const int64_t tid = (int64_t)bid * blockDim.x + threadIdx.x, nth = (int64_t)nb * blockDim.x;
         for (int64_t j = k + 1 + tid; j <= nt; j += nth) {
             swap_el(A, lda, a0, (int)j, b0, (int)j);
             if (ns > 1) swap_el(A, lda, a1, (int)j, b1, (int)j);
@@ -382,28 +436,19 @@ __global__ void __launch_bounds__(UPD_THREADS) rook_step_kernel(double *A, int64
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    if (threadIdx.x == 0) *count = 0;
-    rook_decide(A, lda, ipiv, st, perm, wk, wkm1, u, v, red);
-}
-
-__global__ void rook_finish_kernel(double *A, int64_t lda, RookState *st, const double *wk, const double *wkm1) {
-    __shared__ int s_pend, s_pk;
-    __shared__ double s_pd11, s_pd12;
+    finish_step(A, lda, *S, wk, wkm1);
+    if (next >= 1 && __ldcg(&st->spec) == 0) rook_decide(A, lda, next, ipiv, st, nxt, perm, wk, wkm1, u, v, red);
     if (threadIdx.x == 0) {
-        s_pend = st->pend;
-        s_pk = st->pk;
-        s_pd11 = st->pd11;
-        s_pd12 = st->pd12;
+        st->spec = 0;
+        st->slot = 1 - slot;
+        *count = 0;
     }
-    __syncthreads();
-    if (s_pend) finish_pending(A, lda, st, wk, wkm1, s_pend, s_pk, s_pd11, s_pd12);
 }
 
 __global__ void rook_init_kernel(RookState *st, int nt, int32_t *perm) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t == 0) {
         RookState s = {};
-        s.cur = nt;
         *st = s;
     }
     for (int64_t i = t; i < nt; i += (int64_t)gridDim.x * blockDim.x) perm[i] = (int32_t)i;
@@ -660,14 +705,18 @@ int rbf_sytrf_rook_device(rbf_ctx *ctx, int nt, double *dA, int64_t lda, int32_t
     unsigned int *count = reinterpret_cast<unsigned int *>(s + 1);
     RBF_CUDA(ctx, cudaMemsetAsync(count, 0, sizeof(unsigned int), ctx->stream));
     rook_init_kernel<<<std::max(1, std::min(ctx->num_sms * 4, (nt + 255) / 256)), 256, 0, ctx->stream>>>(s, nt, dperm);
-    rook_pivot_kernel<<<1, PIV_THREADS, 0, ctx->stream>>>(dA, lda, dipiv, s, dperm, wk, wkm1, u, v);
+    rook_pivot_kernel<<<1, PIV_THREADS, 0, ctx->stream>>>(dA, lda, nt, dipiv, s, dperm, wk, wkm1, u, v);
     RBF_CHECK_LAUNCH(ctx);
-    const int maxb = ctx->num_sms * 8;
+    // one wave of resident blocks: the columns are dealt round-robin, no second wave's tail
+    int per_sm = 0;
+    RBF_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rook_step_kernel, UPD_THREADS, 0));
+    const int maxb = ctx->num_sms * std::max(1, per_sm);
     for (int k = nt; k >= 1; k--) {
+        // one block per column of the leading triangle (grid-stride), at least one block,
+        // which makes the next decision
         const int nb = std::max(1, std::min(maxb, k - 1));
         rook_step_kernel<<<nb, UPD_THREADS, 0, ctx->stream>>>(dA, lda, k, nt, dipiv, s, dperm, wk, wkm1, u, v, count);
     }
-    rook_finish_kernel<<<1, PIV_THREADS, 0, ctx->stream>>>(dA, lda, s, wk, wkm1);
     RBF_CHECK_LAUNCH(ctx);
     RookState h;
     RBF_CUDA(ctx, cudaMemcpyAsync(&h, s, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));

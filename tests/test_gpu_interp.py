@@ -1,7 +1,8 @@
 """Global interpolation on the GPU (rbf_interp_fit / rbf_interp_eval, rbf_sytrf_rook /
 rbf_sytrs_rook) against the oracle: the rook Bunch-Kaufman factors and pivots bit-exact
-against the restated dsytf2_rook (after its interchanges are carried to the earlier factor
-columns, the form the GPU keeps), the solve and the fitted weights within rounding, the
+against the restated dsytf2_rook with its updates as fused multiply-adds (after its
+interchanges are carried to the earlier factor columns, the form the GPU keeps), the solve
+and the fitted weights within rounding, the
 evaluation bit-exact for the same weights; the reference's own tests
 (test/operators/interpolation.jl): Franke's function on 10,000 Halton points,
 |interp(0.5, 0.5) - franke| < 1e-5, and the two-point PHS1 case."""
@@ -51,7 +52,7 @@ def test_factor_bit_exact(pkg, orc, dim, phs, deg, n):
     rng = np.random.default_rng(dim * 10 + phs)
     x = rng.uniform(0, 1, (n, dim))
     A = np.ascontiguousarray(orc.interp_matrix(x, phs, deg))
-    F0, ip0, info0 = orc.sytrf_rook_restated(A)
+    F0, ip0, info0 = orc.sytrf_rook_restated(A, fused=True)
     want = orc.convert_rook_factor(F0, ip0)
     F, ip, info = pkg.sytrf_rook(torch.from_numpy(A).cuda())
     assert info == info0 == 0
@@ -74,7 +75,7 @@ def test_indefinite_and_singular(pkg, orc):
     A = M + M.T
     A[:, 7] = A[7, :] = 0.0
     A[100, 100] = 0.0
-    F0, ip0, info0 = orc.sytrf_rook_restated(A)
+    F0, ip0, info0 = orc.sytrf_rook_restated(A, fused=True)
     F, ip, info = pkg.sytrf_rook(torch.from_numpy(A).cuda())
     assert info == info0 and info > 0
     assert np.array_equal(ip.cpu().numpy(), ip0)
@@ -128,7 +129,7 @@ def test_singular_systems(pkg, orc):
     exactly zero columns (SingularException, as bunchkaufman!(A, true) raises)."""
     x = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [1.0, 1.0], [1.0, 1.0], [0.5, 0.3]])
     A = np.ascontiguousarray(orc.interp_matrix(x, 3, 1))
-    F0, ip0, info0 = orc.sytrf_rook_restated(A)
+    F0, ip0, info0 = orc.sytrf_rook_restated(A, fused=True)
     F, ip, info = pkg.sytrf_rook(torch.from_numpy(A).cuda())
     assert info == info0 == 0 and np.array_equal(ip.cpu().numpy(), ip0)
     with pytest.raises(pkg.SingularException):
