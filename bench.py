@@ -511,10 +511,18 @@ def main():
         dW = torch.rand((len(cfg["ops"]), n * k), generator=gen, device=dev, dtype=torch.float64) - 0.5
         ms_adj = timed(lambda: pkg.build_weights_backward(cfg["ops"], Xd, None, adj_b, basis, rp, dW, ctx=ctx),
                        2, 1)
-        adjoint = {"ms": ms_adj, "stencils_per_s": n / (ms_adj * 1e-3), "ms_fp64_build": ms_b_64,
-                   "kernel": "build_backward_kernel (FP64, one warp per stencil: assembly, LU with the weights' "
-                             "and the adjoint's right-hand sides, pair gradients, atomic scatter)"}
-        del dW, rp, adj_b
+        ms_adj_r = timed(lambda: pkg.build_weights_backward(cfg["ops"], Xd, None, adj_b, basis, rp, dW, ctx=ctx,
+                                                            precision="fp32_refined"), 2, 1)
+        g64 = sum(pkg.build_weights_backward(cfg["ops"], Xd, None, adj_b, basis, rp, dW, ctx=ctx))
+        g32 = sum(pkg.build_weights_backward(cfg["ops"], Xd, None, adj_b, basis, rp, dW, ctx=ctx,
+                                             precision="fp32_refined"))
+        adjoint = {"ms": ms_adj, "stencils_per_s": n / (ms_adj * 1e-3), "ms_fp32_refined": ms_adj_r,
+                   "refined_max_rel_diff_vs_fp64": float((g32 - g64).abs().max() / g64.abs().max()),
+                   "ms_fp64_build": ms_b_64,
+                   "kernel": "build_backward_kernel (FP64, one warp per stencil: assembly, LU with the weights' and "
+                             "the adjoint's right-hand sides, pair gradients, atomic scatter); refined: "
+                             "build_backward_refined_kernel (FP32 factor refined in FP64, FP64 fallback)"}
+        del dW, rp, adj_b, g64, g32
 
     # ---- the same workload after reorder_points (Morton order, the reference's locality
     # utility applied once): the apply's gathers become local

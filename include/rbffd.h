@@ -177,8 +177,11 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
  * pullback of _build_weights (src/solve/ad_shared.jl:63-157 with the stencil rules of
  * src/solve/backward.jl:31-222: backward_linear_solve!, backward_collocation!,
  * backward_rhs!).  Supports PHS 1/3/5/7, the identity, first partials and the Laplacian,
- * interior stencils (no Hermite rows; every row holds k entries).  Each stencil system
- * is re-assembled and factorised once in FP64 for the weights and the adjoint. */
+ * interior stencils (no Hermite rows; every row holds k entries), up to RBF_MAX_OPS / 2
+ * operators.  Each stencil system is re-assembled and solved once for the weights and the
+ * adjoint together: cfg->precision RBF_PREC_FP64 factorises in FP64; otherwise an FP32
+ * factorisation is refined with FP64 residuals to cfg->tol (default 1e-11, relative) with the
+ * FP64 solve as fallback, as the refined build does. */
 int rbf_build_backward(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns,
                        const double *eval, int64_t ne, const int32_t *adjl, int32_t k,
                        const int64_t *row_ptr, const double *dW, double *ddata, double *deval);

@@ -613,13 +613,16 @@ def build_weights(ops, data, eval_points, adjl, basis, hermite=None, precision="
     return Ws
 
 
-def build_weights_backward(ops, data, eval_points, adjl, basis, row_ptr, dW, *, ctx=None, flags=0):
+def build_weights_backward(ops, data, eval_points, adjl, basis, row_ptr, dW, *, ctx=None, flags=0,
+                           precision="fp64", tol=0.0):
     """Gradients (ddata, deval) of L = sum(dW * val) for the build
     build_weights(ops, data, eval_points, adjl, basis, flags=flags) whose CSR row_ptr is
     given, dW shaped like its values (len(ops), nnz).  The pullback of _build_weights
     (src/solve/ad_shared.jl:63-157, src/solve/backward.jl:31-222); eval_points None means
-    the data points, whose full gradient is then ddata + deval.  PHS 3/5/7; the identity,
-    first partials and the Laplacian; interior stencils."""
+    the data points, whose full gradient is then ddata + deval.  PHS 1/3/5/7; the identity,
+    first partials and the Laplacian; interior stencils.  precision "fp64" solves each stencil
+    in FP64; "fp32_refined" refines an FP32 factorisation to tol (default 1e-11) with the FP64
+    solve as fallback."""
     torch = _torch()
     d = _points(data)
     q = None if eval_points is None else _points(eval_points, "eval_points")
@@ -643,6 +646,8 @@ def build_weights_backward(ops, data, eval_points, adjl, basis, row_ptr, dW, *, 
         cfg.op_code[i] = c
         cfg.op_dim[i] = od
     cfg.flags = flags
+    cfg.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    cfg.tol = tol
     ddata = torch.empty((ns, dim), dtype=torch.float64, device=dev)
     deval = torch.empty((ne, dim), dtype=torch.float64, device=dev)
     ctx.check(ctx.lib.rbf_build_backward(ctx.h, ctypes.byref(cfg), _ptr(d), ns, _ptr(q), ne, _ptr(a), k,
@@ -650,7 +655,7 @@ def build_weights_backward(ops, data, eval_points, adjl, basis, row_ptr, dW, *, 
     return ddata, deval
 
 
-def build_weights_differentiable(ops, data, eval_points, adjl, basis, *, ctx=None, flags=0):
+def build_weights_differentiable(ops, data, eval_points, adjl, basis, *, ctx=None, flags=0, precision="fp64"):
     """build_weights as a torch autograd function of the point positions (the rrule of
     _build_weights, src/solve/ad_shared.jl:130-157): returns (row_ptr, col, val) with
     val (len(ops), nnz) differentiable with respect to data and eval_points (CUDA float64
@@ -661,7 +666,7 @@ def build_weights_differentiable(ops, data, eval_points, adjl, basis, *, ctx=Non
         @staticmethod
         def forward(fctx, x, y):
             Ws = build_weights(ops, x.detach(), None if y is None else y.detach(), adjl, basis, ctx=ctx,
-                               flags=flags)
+                               flags=flags, precision=precision)
             val = torch.stack([W.val for W in Ws])
             fctx.save_for_backward(x, y if y is not None else x)
             fctx.row_ptr = Ws[0].row_ptr
@@ -673,7 +678,8 @@ def build_weights_differentiable(ops, data, eval_points, adjl, basis, *, ctx=Non
         def backward(fctx, _g_rp, _g_col, g_val):
             x, y = fctx.saved_tensors
             gd, ge = build_weights_backward(ops, x.detach(), None if fctx.same else y.detach(), adjl, basis,
-                                            fctx.row_ptr, g_val.contiguous(), ctx=ctx, flags=flags)
+                                            fctx.row_ptr, g_val.contiguous(), ctx=ctx, flags=flags,
+                                            precision=precision)
             if fctx.same:
                 return gd + ge, None
             return gd, ge

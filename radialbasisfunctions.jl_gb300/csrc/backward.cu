@@ -68,158 +68,191 @@ __device__ __forceinline__ void grad_lphi(int p, int op, int od, const double *D
     for (int d = 0; d < dim; d++) g[d] = a * dd * D[d] + (d == od ? b : 0.0);
 }
 
-// per warp: the forward system with 2 * nops right-hand sides (b, then the adjoint's), the
-// local coordinates and column indices
-struct BackSmem {
-    double *M, *X;
-    int *cols;
-};
+// The kernels see the build's parameters with the operator list doubled (P2.nops = 2 nops):
+// columns n .. n+nops-1 of the stencil system hold the forward right-hand sides, columns
+// n+nops .. n+2nops-1 are assembled as a copy and overwritten with the adjoint's.
 
-__host__ __device__ inline size_t back_warp_bytes(int n, int k, int nops) {
-    const size_t d = (size_t)n * mat_ld(n, 2 * nops) + 3 * (size_t)k;
-    return ((d * sizeof(double) + sizeof(int) * (size_t)k) + 15) & ~(size_t)15;
+// The adjoint right-hand sides of stencil e: dW in the weights' CSR order, in local units,
+// zero on the polynomial rows; scaled by a power of two that brings their largest entry to
+// the forward right-hand sides' (so the refinement's relative acceptance weighs the weights
+// and the adjoint alike; exact, undone on the solution).  Returns the inverse scale.
+__device__ double adjoint_rhs(const StencilParams &P2, int nops, double *M, const int *cols, const double *dW,
+                              int64_t e, int es, int lane) {
+    const int k = P2.k, n = P2.n, ld = mat_ld(n, P2.nops);
+    const int64_t rp = P2.row_ptr[e];
+    const bool sorted = !(P2.flags & RBF_FLAG_STENCIL_ORDER);
+    const bool local = (P2.flags & RBF_FLAG_LOCAL_UNITS) != 0;
+    double amax = 0.0, bmax = 0.0;
+    for (int i = lane; i < n; i += 32) {
+        int rank = i;
+        if (i < k && sorted) {
+            rank = 0;
+            const int ci = cols[i];
+            for (int j = 0; j < k; j++) {
+                const int cj = cols[j];
+                rank += (cj < ci) || (cj == ci && j < i);
+            }
+        }
+        for (int q = 0; q < nops; q++) {
+            const double g = i < k ? dW[(int64_t)q * P2.nnz + rp + rank] : 0.0;
+            const double v = local ? g : ldexp(g, -es * P2.op_order[q]);
+            M[i * ld + n + nops + q] = v;
+            amax = fmax(amax, fabs(v));
+            bmax = fmax(bmax, fabs(M[i * ld + n + q]));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+        bmax = fmax(bmax, __shfl_xor_sync(0xffffffffu, bmax, o));
+    }
+    int ea = 0, eb = 0;
+    if (amax > 0.0 && bmax > 0.0 && isfinite(amax) && isfinite(bmax)) {
+        frexp(amax, &ea);
+        frexp(bmax, &eb);
+    }
+    const int sh = eb - ea;
+    __syncwarp();
+    if (sh != 0)
+        for (int i = lane; i < n; i += 32)
+            for (int q = 0; q < nops; q++) M[i * ld + n + nops + q] = ldexp(M[i * ld + n + nops + q], sh);
+    __syncwarp();
+    return ldexp(1.0, -sh);
 }
 
-__global__ void build_backward_kernel(StencilParams P, int wpb, size_t warp_bytes, const double *__restrict__ dW,
+// ∂L/∂X_i for lane i from the weights λ (sol[i * rs + q]) and the scaled adjoint η
+// (sol[i * rs + nops + q] * inv), then Δdata += s ∂L/∂X_i (atomics) and Δeval = -s Σ_i ∂L/∂X_i.
+__device__ void accumulate_gradients(const StencilParams &P2, int nops, const double *X, const int *cols,
+                                     const double *sol, int rs, double inv, int es, int64_t e, double *ddata,
+                                     double *deval, int lane) {
+    const int k = P2.k, dim = P2.dim, nmon = P2.nmon;
+    const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
+    const double r0 = ldexp(1e-12, -es);  // PHS1's zero radius, local units
+    const double s = ldexp(1.0, -es);
+    double G[3] = {0.0, 0.0, 0.0};
+    for (int i = lane; i < k; i += 32) {
+        double gi[3] = {0.0, 0.0, 0.0};
+        const double *xi = &X[i * 3];
+        for (int q = 0; q < nops; q++) {
+            const double lam_i = sol[i * rs + q], eta_i = sol[i * rs + nops + q] * inv;
+            for (int j = 0; j < k; j++) {
+                if (j == i) continue;
+                const double sc = -(eta_i * sol[j * rs + q] + (sol[j * rs + nops + q] * inv) * lam_i);
+                double D[3], g[3];
+                for (int d = 0; d < dim; d++) D[d] = xi[d] - X[j * 3 + d];
+                grad_phi(P2.phs, D, dim, sqrt(sq_norm(D, dim)), AI.a1, g);
+                for (int d = 0; d < dim; d++) gi[d] += sc * g[d];
+            }
+            for (int m = 0; m < nmon; m++) {
+                const double sc = -(eta_i * sol[(k + m) * rs + q] + (sol[(k + m) * rs + nops + q] * inv) * lam_i);
+                for (int d = 0; d < dim; d++) gi[d] += sc * mono_d1<double>(P2, m, d, xi);
+            }
+            double D[3], g[3];
+            for (int d = 0; d < dim; d++) D[d] = -xi[d];
+            grad_lphi(P2.phs, P2.op_code[q], P2.op_dim[q], D, dim, sqrt(sq_norm(D, dim)), AI.a1, r0, g);
+            for (int d = 0; d < dim; d++) gi[d] -= eta_i * g[d];
+        }
+        for (int d = 0; d < dim; d++) {
+            atomicAdd(&ddata[(int64_t)cols[i] * dim + d], s * gi[d]);
+            G[d] += gi[d];
+        }
+    }
+    for (int d = 0; d < 3; d++)
+        for (int o = 16; o > 0; o >>= 1) G[d] += __shfl_xor_sync(0xffffffffu, G[d], o);
+    if (lane < dim) deval[e * dim + lane] = -s * (lane == 0 ? G[0] : (lane == 1 ? G[1] : G[2]));
+    __syncwarp();
+}
+
+// FP64: re-assemble, LU with both right-hand-side blocks, gradients
+__global__ void build_backward_kernel(StencilParams P2, int nops, int wpb, size_t warp_bytes, const double *__restrict__ dW,
                                       double *__restrict__ ddata, double *__restrict__ deval) {
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    char *base = smem + wib * warp_bytes;
-    const int k = P.k, n = P.n, nops = P.nops, dim = P.dim, nmon = P.nmon;
-    const int ld = mat_ld(n, 2 * nops);
-    BackSmem b;
-    b.M = reinterpret_cast<double *>(base);
-    b.X = b.M + (size_t)n * ld;
-    b.cols = reinterpret_cast<int *>(b.X + 3 * k);
-    // load_stencil and the forward assembly work on a WarpSmem whose matrix has room for
-    // nops right-hand sides; the backward matrix (2 * nops) reuses its storage
-    WarpSmem w;
-    w.M = b.M;
-    w.X = b.X;
-    w.cols = b.cols;
+    WarpSmem w = carve(smem + wib * warp_bytes, P2.n, P2.k, P2.nops);
+    const int n = P2.n, ld = mat_ld(n, P2.nops);
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
-    for (int64_t e = (int64_t)blockIdx.x * wpb + wib; e < P.ne; e += nwarps) {
+    for (int64_t e = (int64_t)blockIdx.x * wpb + wib; e < P2.ne; e += nwarps) {
         int es = 0, eval_local = -2;
-        // interior stencils only (the entry point rejects boundary data): no Hermite arrays
-        {
-            const int32_t *nbr = P.adjl + e * k;
-            double x0[3] = {0, 0, 0};
-            for (int d = 0; d < dim; d++) x0[d] = P.eval[e * dim + d];
-            double r2max = 0.0;
-            for (int i = lane; i < k; i += 32) {
-                const int g = nbr[i];
-                b.cols[i] = g;
-                double r2 = 0.0;
-                for (int d = 0; d < 3; d++) {
-                    const double dd = d < dim ? P.data[(int64_t)g * dim + d] - x0[d] : 0.0;
-                    b.X[i * 3 + d] = dd;
-                    r2 += dd * dd;
-                }
-                r2max = fmax(r2max, r2);
-            }
-            for (int o = 16; o > 0; o >>= 1) r2max = fmax(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
-            if (r2max > 0.0) frexp(sqrt(r2max), &es);
-            __syncwarp();
-            for (int i = lane; i < k; i += 32)
-                for (int d = 0; d < dim; d++) b.X[i * 3 + d] = ldexp(b.X[i * 3 + d], -es);
-            __syncwarp();
-        }
-        // forward system with its nops right-hand sides (row stride mat_ld(n, nops)), then
-        // moved in place to the wider stride ld, last row first
-        assemble_fp64(P, w, lane, es, eval_local);
-        const int ld0 = mat_ld(n, nops);
-        for (int r = n - 1; r >= 1; r--) {
-            // rows move to higher addresses: read the whole row before writing it
-            double v0 = lane < n + nops ? b.M[r * ld0 + lane] : 0.0;
-            double v1 = lane + 32 < n + nops ? b.M[r * ld0 + lane + 32] : 0.0;
-            double v2 = lane + 64 < n + nops ? b.M[r * ld0 + lane + 64] : 0.0;
-            __syncwarp();
-            if (lane < n + nops) b.M[r * ld + lane] = v0;
-            if (lane + 32 < n + nops) b.M[r * ld + lane + 32] = v1;
-            if (lane + 64 < n + nops) b.M[r * ld + lane + 64] = v2;
-            __syncwarp();
-        }
-        // adjoint right-hand sides: dW in the weights' CSR order, scaled to local units
-        const int64_t rp = P.row_ptr[e];
-        const bool sorted = !(P.flags & RBF_FLAG_STENCIL_ORDER);
-        const bool local = (P.flags & RBF_FLAG_LOCAL_UNITS) != 0;
-        for (int i = lane; i < n; i += 32) {
-            int rank = i;
-            if (i < k && sorted) {
-                rank = 0;
-                const int ci = b.cols[i];
-                for (int j = 0; j < k; j++) {
-                    const int cj = b.cols[j];
-                    rank += (cj < ci) || (cj == ci && j < i);
-                }
-            }
-            for (int q = 0; q < nops; q++) {
-                const double g = i < k ? dW[(int64_t)q * P.nnz + rp + rank] : 0.0;
-                b.M[i * ld + n + nops + q] = local ? g : ldexp(g, -es * P.op_order[q]);
-            }
-        }
-        __syncwarp();
-        const bool ok = lu_solve_fp64(b.M, n, 2 * nops, lane);
-        if (!ok) {
-            if (lane == 0) atomicAdd(&P.counters[0], 1ull);
+        load_stencil(P2, e, w, lane, &es, &eval_local);  // interior stencils: the entry point rejects boundary data
+        assemble_fp64(P2, w, lane, es, -2);
+        const double inv = adjoint_rhs(P2, nops, w.M, w.cols, dW, e, es, lane);
+        if (!lu_solve_fp64(w.M, n, P2.nops, lane)) {
+            if (lane == 0) atomicAdd(&P2.counters[0], 1ull);
             __syncwarp();
             continue;
         }
-        const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
-        const double r0 = ldexp(1e-12, -es);  // PHS1's zero radius, local units
-        // ∂L/∂X_i, lane i
-        double G[3] = {0.0, 0.0, 0.0};
-        for (int i = lane; i < k; i += 32) {
-            double gi[3] = {0.0, 0.0, 0.0};
-            const double *xi = &b.X[i * 3];
-            for (int q = 0; q < nops; q++) {
-                const double lam_i = b.M[i * ld + n + q], eta_i = b.M[i * ld + n + nops + q];
-                for (int j = 0; j < k; j++) {
-                    if (j == i) continue;
-                    const double sc = -(eta_i * b.M[j * ld + n + q] + b.M[j * ld + n + nops + q] * lam_i);
-                    double D[3], g[3];
-                    for (int d = 0; d < dim; d++) D[d] = xi[d] - b.X[j * 3 + d];
-                    grad_phi(P.phs, D, dim, sqrt(sq_norm(D, dim)), AI.a1, g);
-                    for (int d = 0; d < dim; d++) gi[d] += sc * g[d];
-                }
-                for (int m = 0; m < nmon; m++) {
-                    const double sc = -(eta_i * b.M[(k + m) * ld + n + q] + b.M[(k + m) * ld + n + nops + q] * lam_i);
-                    for (int d = 0; d < dim; d++) gi[d] += sc * mono_d1<double>(P, m, d, xi);
-                }
-                double D[3], g[3];
-                for (int d = 0; d < dim; d++) D[d] = -xi[d];
-                grad_lphi(P.phs, P.op_code[q], P.op_dim[q], D, dim, sqrt(sq_norm(D, dim)), AI.a1, r0, g);
-                for (int d = 0; d < dim; d++) gi[d] -= eta_i * g[d];
-            }
-            const double s = ldexp(1.0, -es);
-            for (int d = 0; d < dim; d++) {
-                atomicAdd(&ddata[(int64_t)b.cols[i] * dim + d], s * gi[d]);
-                G[d] += gi[d];
-            }
-        }
-        for (int d = 0; d < 3; d++)
-            for (int o = 16; o > 0; o >>= 1) G[d] += __shfl_xor_sync(0xffffffffu, G[d], o);
-        if (lane < dim) {
-            const double s = ldexp(1.0, -es);
-            deval[e * dim + lane] = -s * (lane == 0 ? G[0] : (lane == 1 ? G[1] : G[2]));
-        }
-        __syncwarp();
+        accumulate_gradients(P2, nops, w.X, w.cols, w.M + n, ld, inv, es, e, ddata, deval, lane);
     }
+}
+
+// FP32 factor + FP64-residual refinement of the weights and the adjoint together (the forward
+// build's refined solve), FP64 fallback; then the gradients
+__global__ void build_backward_refined_kernel(StencilParams P2, int nops, int wpb, size_t warp_bytes,
+                                              const double *__restrict__ dW, double *__restrict__ ddata,
+                                              double *__restrict__ deval) {
+    extern __shared__ __align__(16) char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    char *base = smem + wib * warp_bytes;
+    WarpSmem w = carve(base, P2.n, P2.k, P2.nops);
+    Warp32 u = carve32(base, P2.n, P2.k, P2.nops);
+    const int n = P2.n, ld = mat_ld(n, P2.nops);
+    const int64_t nwarps = (int64_t)gridDim.x * wpb;
+    for (int64_t e = (int64_t)blockIdx.x * wpb + wib; e < P2.ne; e += nwarps) {
+        int es = 0, eval_local = -2;
+        load_stencil(P2, e, w, lane, &es, &eval_local);
+        assemble_refined(P2, w, u, lane, es, -2);
+        double inv = adjoint_rhs(P2, nops, w.M, w.cols, dW, e, es, lane);
+        const bool ok = lu_factor_fp32(u.F, u.piv, n, lane);
+        double est = 0.0;
+        if (ok && refine_fp32_warp(P2, w, u, lane, &est)) {
+            accumulate_gradients(P2, nops, w.X, w.cols, u.x, P2.nops, inv, es, e, ddata, deval, lane);
+            continue;
+        }
+        if (lane == 0) atomicAdd(&P2.counters[2], 1ull);
+        assemble_fp64(P2, w, lane, es, -2);
+        inv = adjoint_rhs(P2, nops, w.M, w.cols, dW, e, es, lane);
+        if (!lu_solve_fp64(w.M, n, P2.nops, lane)) {
+            if (lane == 0) atomicAdd(&P2.counters[0], 1ull);
+            __syncwarp();
+            continue;
+        }
+        accumulate_gradients(P2, nops, w.X, w.cols, w.M + n, ld, inv, es, e, ddata, deval, lane);
+    }
+}
+
+template <class K>
+int launch_backward(rbf_ctx *ctx, K kernel, size_t wb, const StencilParams &P2, int nops, const double *dW,
+                    double *ddata, double *deval) {
+    wb = (wb + 15) & ~(size_t)15;
+    const int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (100 * 1024) / wb));
+    const size_t smem = wb * wpb;
+    RBF_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    RBF_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, wpb * 32, smem));
+    if (per_sm < 1) per_sm = 1;
+    const int64_t blocks = std::min<int64_t>((P2.ne + wpb - 1) / wpb, (int64_t)ctx->num_sms * per_sm);
+    kernel<<<(unsigned)blocks, wpb * 32, smem, ctx->stream>>>(P2, nops, wpb, wb, dW, ddata, deval);
+    RBF_CHECK_LAUNCH(ctx);
+    return RBF_OK;
 }
 
 }  // namespace
 
-int rbf_backward_launch(rbf_ctx *ctx, const StencilParams &P, const double *dW, double *ddata, double *deval) {
+// P: the build's parameters (nops operators); refined: FP32 factor + FP64 refinement
+int rbf_backward_launch(rbf_ctx *ctx, const StencilParams &P, bool refined, const double *dW, double *ddata,
+                        double *deval) {
     if (P.ne == 0) return RBF_OK;
-    const size_t wb = back_warp_bytes(P.n, P.k, P.nops);
-    const int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (100 * 1024) / wb));
-    const size_t smem = wb * wpb;
-    RBF_CUDA(ctx, cudaFuncSetAttribute(build_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    RBF_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, build_backward_kernel, wpb * 32, smem));
-    if (per_sm < 1) per_sm = 1;
-    const int64_t blocks = std::min<int64_t>((P.ne + wpb - 1) / wpb, (int64_t)ctx->num_sms * per_sm);
-    build_backward_kernel<<<(unsigned)blocks, wpb * 32, smem, ctx->stream>>>(P, wpb, wb, dW, ddata, deval);
-    RBF_CHECK_LAUNCH(ctx);
-    return RBF_OK;
+    if (2 * P.nops > RBF_MAX_OPS) return rbf_fail(ctx, RBF_ERR_UNSUPPORTED, "the weight adjoint takes up to %d operators",
+                                                  RBF_MAX_OPS / 2);
+    StencilParams P2 = P;
+    const int nops = P.nops;
+    P2.nops = 2 * nops;
+    for (int q = 0; q < nops; q++) {
+        P2.op_code[nops + q] = P.op_code[q];
+        P2.op_dim[nops + q] = P.op_dim[q];
+        P2.op_order[nops + q] = P.op_order[q];
+    }
+    if (refined)
+        return launch_backward(ctx, build_backward_refined_kernel, warp_smem_bytes32(P2.n, P2.k, P2.nops), P2, nops, dW,
+                               ddata, deval);
+    return launch_backward(ctx, build_backward_kernel, warp_smem_bytes(P2.n, P2.k, P2.nops), P2, nops, dW, ddata, deval);
 }

@@ -604,7 +604,11 @@ int rbf_build_backward(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *dat
     P.row_ptr = rp.as<int64_t>();
     P.counters = counters.as<unsigned long long>();
     P.max_resid = reinterpret_cast<double *>(counters.as<unsigned long long>() + 8);
-    RBF_TRY(rbf_backward_launch(ctx, P, gw.as<double>(), od.as<double>(), oe.as<double>()));
+    // the adjoint's refinement aims below the forward's default tolerance: the gradients
+    // combine the weights and the adjoint, and are checked against FP64 to 1e-9
+    P.tol = cfg->tol > 0 ? cfg->tol : 1e-11;
+    RBF_TRY(rbf_backward_launch(ctx, P, cfg->precision != RBF_PREC_FP64, gw.as<double>(), od.as<double>(),
+                                oe.as<double>()));
     unsigned long long nsing = 0;
     RBF_CUDA(ctx, cudaMemcpyAsync(&nsing, counters.ptr, sizeof nsing, cudaMemcpyDeviceToHost, ctx->stream));
     RBF_TRY(od.finish(ctx));

@@ -118,7 +118,8 @@ int rbf_boundary_map_device(rbf_ctx *ctx, int64_t n, const uint8_t *d_isb, int32
                             int64_t *n_boundary);
 
 int rbf_check_indices(rbf_ctx *ctx, const int32_t *d_idx, int64_t n, int32_t hi, bool *ok);
-int rbf_backward_launch(rbf_ctx *ctx, const StencilParams &P, const double *dW, double *ddata, double *deval);
+int rbf_backward_launch(rbf_ctx *ctx, const StencilParams &P, bool refined, const double *dW, double *ddata,
+                        double *deval);
 int rbf_sytrf_rook_device(rbf_ctx *ctx, int nt, double *dA, int64_t lda, int32_t *dipiv, int32_t *dperm,
                           int64_t *info);
 int rbf_check_ipiv_device(rbf_ctx *ctx, int nt, const int32_t *dipiv, bool *ok);

@@ -52,11 +52,12 @@ def to_csr_order(adjl, x):
     return np.stack([np.take_along_axis(x[q], order, axis=1).reshape(-1) for q in range(x.shape[0])])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
 @pytest.mark.parametrize("phs,deg,op", [(3, 2, (OP_D1, 0)), (3, 2, (OP_LAP, 0)), (1, 1, (OP_D1, 0)),
                                         (3, 1, (OP_D1, 0)), (5, 1, (OP_D1, 0)), (7, 1, (OP_D1, 0)),
                                         (5, 2, (OP_LAP, 0)), (7, 2, (OP_LAP, 0)), (1, 1, (OP_LAP, 0)),
                                         (3, 2, (OP_D1, 1))])
-def test_reference_grid_case(pkg, orc, bo, phs, deg, op):
+def test_reference_grid_case(pkg, orc, bo, phs, deg, op, precision):
     X = grid_points()
     adjl = orc.knn(X, X, 10)
     basis = pkg.PHS(phs, poly_deg=deg)
@@ -64,7 +65,7 @@ def test_reference_grid_case(pkg, orc, bo, phs, deg, op):
     W = pkg.build_weights([op], Xd, None, adjl, basis)
     w = stencil_order(pkg, W, adjl)
     dW = torch.from_numpy(2.0 * to_csr_order(adjl, w)).cuda()  # d/dW of sum(W.^2)
-    gd, ge = pkg.build_weights_backward([op], Xd, None, adjl, basis, W[0].row_ptr, dW)
+    gd, ge = pkg.build_weights_backward([op], Xd, None, adjl, basis, W[0].row_ptr, dW, precision=precision)
     got = (gd + ge).cpu().numpy()
     od, oe = bo.build_backward(X, X, adjl, 2, phs, deg, [op], 2.0 * w)
     want = od + oe
@@ -83,10 +84,11 @@ def test_regrid_at_the_data_points(pkg, orc, bo):
     assert float((gd + ge).abs().max()) < 1e-12
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
 @pytest.mark.parametrize("phs,ops", [(3, [(OP_LAP, 0)]), (5, [(OP_D1, 0), (OP_D1, 1), (OP_D1, 2)]),
                                      (7, [(OP_IDENT, 0)]), (3, [(OP_IDENT, 0), (OP_LAP, 0)]),
                                      (1, [(OP_D1, 2)])])
-def test_cloud3d_separate_eval(pkg, orc, bo, phs, ops):
+def test_cloud3d_separate_eval(pkg, orc, bo, phs, ops, precision):
     rng = np.random.default_rng(8)
     data = rng.uniform(0, 1, (400, 3))
     ev = rng.uniform(0.1, 0.9, (40, 3))
@@ -97,7 +99,7 @@ def test_cloud3d_separate_eval(pkg, orc, bo, phs, ops):
     Xd, Ed = torch.from_numpy(data).cuda(), torch.from_numpy(ev).cuda()
     W = pkg.build_weights(ops, Xd, Ed, adjl, basis)
     gd, ge = pkg.build_weights_backward(ops, Xd, Ed, adjl, basis, W[0].row_ptr,
-                                        torch.from_numpy(to_csr_order(adjl, dW)).cuda())
+                                        torch.from_numpy(to_csr_order(adjl, dW)).cuda(), precision=precision)
     od, oe = bo.build_backward(data, ev, adjl, 3, phs, 2, ops, dW)
     assert np.abs(gd.cpu().numpy() - od).max() <= TOL * np.abs(od).max()
     assert np.abs(ge.cpu().numpy() - oe).max() <= TOL * np.abs(oe).max()
@@ -168,8 +170,9 @@ def test_rejects_unsupported(pkg, orc):
         pkg.build_weights_backward([(OP_LAP, 0)], X, None, adjl, basis, W[0].row_ptr, W[0].val[None, :10])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
 @pytest.mark.parametrize("ops,q", [([(OP_LAP, 0)], 2), ([(OP_D1, 0), (OP_D1, 1), (OP_D1, 2)], 1)])
-def test_invariances_full_size(pkg, ops, q):
+def test_invariances_full_size(pkg, ops, q, precision):
     """200k eval points in 3D, k = 30: the weights are unchanged by a translation of all
     points (sum of all gradients = 0) and scale as c^-q (sum_i x_i . g_i = -q L)."""
     g = torch.Generator(device="cuda").manual_seed(11)
@@ -178,9 +181,12 @@ def test_invariances_full_size(pkg, ops, q):
     basis = pkg.PHS(3, poly_deg=2)
     W = pkg.build_weights(ops, X, None, adjl, basis)
     dW = torch.stack([torch.rand(w.val.shape, generator=g, device="cuda", dtype=torch.float64) - 0.5 for w in W])
-    gd, ge = pkg.build_weights_backward(ops, X, None, adjl, basis, W[0].row_ptr, dW)
+    gd, ge = pkg.build_weights_backward(ops, X, None, adjl, basis, W[0].row_ptr, dW, precision=precision)
     G = gd + ge
     L = float(sum((dW[i] * W[i].val).sum() for i in range(len(W))))
     gscale = float((G.abs() * X.abs().max()).sum())
     assert float(G.sum(0).abs().max()) <= 1e-9 * float(G.abs().sum())
     assert abs(float((X * G).sum()) + q * L) <= 1e-9 * gscale
+    if precision != "fp64":  # the refined adjoint against the FP64 one, point by point
+        gd0, ge0 = pkg.build_weights_backward(ops, X, None, adjl, basis, W[0].row_ptr, dW, precision="fp64")
+        assert float((G - (gd0 + ge0)).abs().max()) <= 1e-9 * float((gd0 + ge0).abs().max())
