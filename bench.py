@@ -224,7 +224,7 @@ def interp_bench(pkg, torch, stream, n_points, cpu):
            "eval_pairs_per_s": m * n_points / (ms_eval * 1e-3), "max_abs_err_vs_franke": err,
            "factor_fp64_tflops": fl / (ms_fit * 1e-3) / 1e12,
            "factor_update_gbs": by / (ms_fit * 1e-3) / 1e9,
-           "kernels": "interp_assemble_kernel, rook_pivot_kernel + rook_update_kernel per column (unblocked "
+           "kernels": "interp_assemble_kernel, rook_step_kernel per column (unblocked "
                       "dsytf2_rook order), blocked solve, interp_eval_kernel"}
     if cpu:
         from oracle import oracle as O
