@@ -167,6 +167,23 @@ def cpu_baseline(cfg, n, sample, steps=1):
             "cores": O.num_threads(), "sample": sample}
 
 
+def max_over_ranks(ms, world, device=None):
+    """The job's time: the slowest rank's (every rank passes its own; a no-op on one rank)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, ms):
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time
+    (replicas: every rank processes its own cloud of the same size)."""
+    return units_per_rank * world / (ms * 1e-3)
+
+
 def halton(n, base):
     """Radical-inverse sequence of base `base`, indices 1..n."""
     out = np.zeros(n)
@@ -338,12 +355,7 @@ def main():
             fn()
         e1.record(stream)
         barrier()
-        ms = e0.elapsed_time(e1) / steps
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(e0.elapsed_time(e1) / steps, world, dev)
 
     if learned_on:
         # ---- surrogate training (untimed): plain FP64 solves on independent seeded clouds,
@@ -396,13 +408,9 @@ def main():
     e1.record(stream)
     barrier()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
     launches = (ctx.lib.rbf_ctx_kernel_launches(ctx.handle) - launches0) // args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = n * world / (ms * 1e-3)
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
+    value = job_rate(n, world, ms)
 
     # ---- the same step with the plain FP64 build (and without the learned seed) beside it
     ms_fp64 = timed(lambda: step("fp64"), max(1, args.steps // 2), 1)
