@@ -134,3 +134,40 @@ def test_singular_systems(pkg, orc):
     assert info == info0 == 0 and np.array_equal(ip.cpu().numpy(), ip0)
     with pytest.raises(pkg.SingularException):
         pkg.Interpolator(np.zeros((2, 2)), np.arange(2.0), pkg.PHS(3, poly_deg=1))
+
+
+def test_c_abi_host_pointers(pkg, orc):
+    """The entry points with host (numpy) arrays, as a ccall with Julia Vectors passes them:
+    the same results as with device arrays; a malformed ipiv is rejected."""
+    import ctypes
+    ctx = pkg.Context.default(0)
+    L, h = ctx.lib, ctx.h
+    P = ctypes.c_void_p
+    rng = np.random.default_rng(12)
+    x = rng.uniform(0, 1, (300, 2))
+    y = np.cos(2 * x[:, 0]) * x[:, 1]
+    coef = np.zeros(306)
+    ctx.check(L.rbf_interp_fit(h, 2, 3, 2, x.ctypes.data_as(P), 300, y.ctypes.data_as(P), coef.ctypes.data_as(P)))
+    I = pkg.Interpolator(torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda(), pkg.PHS(3, poly_deg=2))
+    assert np.array_equal(coef, I.coef.cpu().numpy())
+    xe = rng.uniform(0, 1, (500, 2))
+    out = np.zeros(500)
+    ctx.check(L.rbf_interp_eval(h, 2, 3, 2, x.ctypes.data_as(P), 300, coef.ctypes.data_as(P), xe.ctypes.data_as(P), 500,
+                                out.ctypes.data_as(P)))
+    assert np.array_equal(out, I(xe))
+    # dense factorisation and solve on host arrays (column-major)
+    A = np.asfortranarray(orc.interp_matrix(x, 3, 2))
+    ipiv = np.zeros(306, dtype=np.int32)
+    info = ctypes.c_int64(-1)
+    ctx.check(L.rbf_sytrf_rook(h, 306, A.ctypes.data_as(P), 306, ipiv.ctypes.data_as(P), ctypes.byref(info)))
+    F0, ip0, _ = orc.sytrf_rook_restated(orc.interp_matrix(x, 3, 2), fused=True)
+    assert info.value == 0 and np.array_equal(ipiv, ip0)
+    assert np.array_equal(np.triu(A), np.triu(orc.convert_rook_factor(F0, ip0)))
+    b = np.asfortranarray(np.r_[y, np.zeros(6)].reshape(306, 1))
+    ctx.check(L.rbf_sytrs_rook(h, 306, 1, A.ctypes.data_as(P), 306, ipiv.ctypes.data_as(P), b.ctypes.data_as(P), 306))
+    assert np.abs(b[:, 0] - coef).max() <= 1e-9 * np.abs(coef).max()
+    bad = ipiv.copy()
+    bad[5] = 400
+    with pytest.raises(ValueError, match="ipiv"):
+        ctx.check(L.rbf_sytrs_rook(h, 306, 1, A.ctypes.data_as(P), 306, bad.ctypes.data_as(P), b.ctypes.data_as(P),
+                                   306))
