@@ -79,8 +79,8 @@ def parse():
     p.add_argument("--reorder", action="store_true",
                    help="with --profile-once: put the cloud in Morton order first (reorder_points)")
     p.add_argument("--profile-once", action="store_true",
-                   help="run each hot kernel once (kNN, FP64 build, FP32-refined build, apply) and exit; "
-                        "the driver for ncu captures")
+                   help="run each hot kernel once (kNN, FP64 build, FP32-refined build, apply) and exit "
+                        "(a short command to capture under ncu)")
     return p.parse_args()
 
 
