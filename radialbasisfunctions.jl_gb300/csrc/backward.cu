@@ -121,6 +121,9 @@ __device__ double adjoint_rhs(const StencilParams &P2, int nops, double *M, cons
 
 // ∂L/∂X_i for lane i from the weights λ (sol[i * rs + q]) and the scaled adjoint η
 // (sol[i * rs + nops + q] * inv), then Δdata += s ∂L/∂X_i (atomics) and Δeval = -s Σ_i ∂L/∂X_i.
+// The pair term -(η_i λ_j + η_j λ_i) ∇φ(X_i - X_j) is odd in (i, j): for k <= 32 each pair is
+// evaluated once, in cyclic rounds (round d: lane i takes the pair (i, i + d mod k)), and the
+// partner's share reaches its lane by a shuffle.
 __device__ void accumulate_gradients(const StencilParams &P2, int nops, const double *X, const int *cols,
                                      const double *sol, int rs, double inv, int es, int64_t e, double *ddata,
                                      double *deval, int lane) {
@@ -134,13 +137,15 @@ __device__ void accumulate_gradients(const StencilParams &P2, int nops, const do
         const double *xi = &X[i * 3];
         for (int q = 0; q < nops; q++) {
             const double lam_i = sol[i * rs + q], eta_i = sol[i * rs + nops + q] * inv;
-            for (int j = 0; j < k; j++) {
-                if (j == i) continue;
-                const double sc = -(eta_i * sol[j * rs + q] + (sol[j * rs + nops + q] * inv) * lam_i);
-                double D[3], g[3];
-                for (int d = 0; d < dim; d++) D[d] = xi[d] - X[j * 3 + d];
-                grad_phi(P2.phs, D, dim, sqrt(sq_norm(D, dim)), AI.a1, g);
-                for (int d = 0; d < dim; d++) gi[d] += sc * g[d];
+            if (k > 32) {
+                for (int j = 0; j < k; j++) {
+                    if (j == i) continue;
+                    const double sc = -(eta_i * sol[j * rs + q] + (sol[j * rs + nops + q] * inv) * lam_i);
+                    double D[3], g[3];
+                    for (int d = 0; d < dim; d++) D[d] = xi[d] - X[j * 3 + d];
+                    grad_phi(P2.phs, D, dim, sqrt(sq_norm(D, dim)), AI.a1, g);
+                    for (int d = 0; d < dim; d++) gi[d] += sc * g[d];
+                }
             }
             for (int m = 0; m < nmon; m++) {
                 const double sc = -(eta_i * sol[(k + m) * rs + q] + (sol[(k + m) * rs + nops + q] * inv) * lam_i);
@@ -151,10 +156,46 @@ __device__ void accumulate_gradients(const StencilParams &P2, int nops, const do
             grad_lphi(P2.phs, P2.op_code[q], P2.op_dim[q], D, dim, sqrt(sq_norm(D, dim)), AI.a1, r0, g);
             for (int d = 0; d < dim; d++) gi[d] -= eta_i * g[d];
         }
-        for (int d = 0; d < dim; d++) {
-            atomicAdd(&ddata[(int64_t)cols[i] * dim + d], s * gi[d]);
-            G[d] += gi[d];
+        for (int d = 0; d < dim; d++) G[d] += gi[d];
+        if (k > 32)
+            for (int d = 0; d < dim; d++) atomicAdd(&ddata[(int64_t)cols[i] * dim + d], s * gi[d]);
+        else
+            for (int d = 0; d < 3; d++) G[d] = gi[d];  // pair terms follow; G is lane i's point here
+    }
+    if (k <= 32) {
+        // pair terms, each pair once; G holds lane i's sum so far (lanes >= k hold zeros)
+        const bool act = lane < k;
+        const double *xi = &X[(act ? lane : 0) * 3];
+        for (int q = 0; q < nops; q++) {
+            const double lam_i = act ? sol[lane * rs + q] : 0.0;
+            const double eta_i = act ? sol[lane * rs + nops + q] * inv : 0.0;
+            for (int dd = 1; dd <= k / 2; dd++) {
+                int j = lane + dd;
+                if (j >= k) j -= k;
+                // round k/2 of an even k meets every pair twice: the lower lane takes it
+                const bool use = act && (2 * dd != k || lane < dd);
+                double c[3] = {0.0, 0.0, 0.0};
+                if (use) {
+                    const double sc = -(eta_i * sol[j * rs + q] + (sol[j * rs + nops + q] * inv) * lam_i);
+                    double D[3], g[3];
+                    for (int d = 0; d < dim; d++) D[d] = xi[d] - X[j * 3 + d];
+                    grad_phi(P2.phs, D, dim, sqrt(sq_norm(D, dim)), AI.a1, g);
+                    for (int d = 0; d < dim; d++) {
+                        G[d] += sc * g[d];
+                        c[d] = -sc * g[d];
+                    }
+                }
+                int src = lane - dd;  // the lane whose pair ends at this lane's point
+                if (src < 0) src += k;
+                if (!act) src = lane;
+                for (int d = 0; d < 3; d++) {
+                    const double recv = __shfl_sync(0xffffffffu, c[d], src);
+                    if (act) G[d] += recv;
+                }
+            }
         }
+        if (act)
+            for (int d = 0; d < dim; d++) atomicAdd(&ddata[(int64_t)cols[lane] * dim + d], s * G[d]);
     }
     for (int d = 0; d < 3; d++)
         for (int o = 16; o > 0; o >>= 1) G[d] += __shfl_xor_sync(0xffffffffu, G[d], o);
