@@ -72,6 +72,9 @@ def parse():
     p.add_argument("--n", type=int, default=0, help="override the point count (development runs)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--interp-n", type=int, default=10_000, help="points of the Interpolator leg (0: skip)")
+    p.add_argument("--all-configs", action="store_true",
+                   help="time the other workloads (2D 10k, 3D gradient+Laplacian 1M, 2D disk Hermite 2M, "
+                        "3D regrid 8M) on one GPU, one JSON line each, and exit")
     p.add_argument("--cpu-sample", type=int, default=0, help="stencils in the CPU baseline sample")
     p.add_argument("--train-stencils", type=int, default=2_000_000, help="solver stencils the surrogate trains on")
     p.add_argument("--train-epochs", type=int, default=12)
@@ -259,6 +262,180 @@ def interp_bench(pkg, torch, stream, n_points, cpu):
     return out
 
 
+def unit_disk(n_interior, n_boundary, seed):
+    """Jittered grid clipped to the open unit disk plus equispaced boundary points with outward
+    normals; Dirichlet on the upper half-circle, Neumann on the lower."""
+    rng = np.random.default_rng(seed)
+    m = int(math.sqrt(n_interior * 4 / math.pi))
+    h = 2.0 / m
+    g = np.stack(np.meshgrid(np.arange(m), np.arange(m), indexing="ij"), -1).reshape(-1, 2)
+    P = -1 + (g + 0.5) * h + rng.uniform(-0.3 * h, 0.3 * h, g.shape)
+    P = P[np.hypot(P[:, 0], P[:, 1]) < 1 - 0.5 * h]
+    t = 2 * math.pi * (np.arange(n_boundary) + 0.5) / n_boundary
+    B = np.stack([np.cos(t), np.sin(t)], 1)
+    isb = np.zeros(len(P) + n_boundary, dtype=bool)
+    isb[len(P):] = True
+    dirichlet = B[:, 1] > 0
+    return np.concatenate([P, B]), isb, B, np.where(dirichlet, 1.0, 0.0), np.where(dirichlet, 0.0, 1.0)
+
+
+def mixture_targets(n, seed):
+    """Half uniform in the unit cube, half from 8 isotropic Gaussians (sigma 0.05), clipped."""
+    rng = np.random.default_rng(seed)
+    half = n // 2
+    centres = rng.uniform(0.1, 0.9, (8, 3))
+    G = centres[rng.integers(0, 8, n - half)] + rng.normal(0, 0.05, (n - half, 3))
+    return np.clip(np.concatenate([rng.uniform(0, 1, (half, 3)), G]), 0.0, 1.0)
+
+
+def fourier_fields(torch, X, nf, seed):
+    """nf seeded smooth fields, each a sum of 8 Fourier modes (wavenumbers uniform in [1, 4] per
+    axis, N(0, 1) amplitudes), as an (n, nf) tensor on X's device."""
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    kv = torch.rand((nf, 8, X.shape[1]), generator=g, dtype=torch.float64) * 3 + 1
+    a = torch.randn((nf, 8), generator=g, dtype=torch.float64)
+    F = torch.empty((X.shape[0], nf), dtype=torch.float64, device=X.device)
+    for f in range(nf):
+        F[:, f] = (torch.sin(X @ kv[f].T.to(X.device)) * a[f].to(X.device)).sum(1)
+    return F
+
+
+def all_configs(pkg, torch, ctx, stream):
+    """The other workloads of the benchmark's configuration list, each timed once on the GPU:
+    kNN, plain FP64 and FP32-refined builds (stencils/s, build only), the refined weights'
+    max row-relative difference to the FP64 ones, and the apply (algorithmic bytes over the
+    library's kernel time, fraction of the measured copy rate).  One JSON line per workload."""
+    hbm = PEAKS.get("hbm_gbs", 6800.0)
+
+    def ev_ms(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, out
+
+    def kernel_ms(fn):
+        ctx.lib.rbf_ctx_set_timing(ctx.h, 1)
+        fn()
+        fn()
+        v = pkg.ctypes.c_float(0.0)
+        ctx.lib.rbf_ctx_last_ms(ctx.h, pkg.ctypes.byref(v))
+        ctx.lib.rbf_ctx_set_timing(ctx.h, 0)
+        return float(v.value)
+
+    def row_diff(W, Wr):
+        rp = W.row_ptr
+        rows = torch.repeat_interleave(torch.arange(W.shape[0], device=rp.device), rp[1:] - rp[:-1])
+        num = torch.zeros(W.shape[0], dtype=torch.float64, device=rp.device)
+        den = torch.zeros_like(num)
+        num.scatter_reduce_(0, rows, (W.val - Wr.val).abs(), "amax")
+        den.scatter_reduce_(0, rows, Wr.val.abs(), "amax")
+        ok = den > 0
+        return float((num[ok] / den[ok]).max())
+
+    fma64 = pkg.ctypes.c_double(0.0)
+    ctx.check(ctx.lib.rbf_diag_fma_peak(ctx.h, 1, pkg.ctypes.byref(fma64)))
+    fma_peak = fma64.value / 2.0  # FP64 FMA per second (the peak counts 2 flops per FMA), in T
+
+    def report(name, desc, ne, ms_knn, ms64, ms32, err, W, nf, ms_apply, extra=None):
+        by = W.nnz * 12 + (ne + 1) * 8 + nf * (W.shape[1] + ne) * 8
+        fmas = W.nnz * nf / (ms_apply * 1e-3) / 1e12
+        line = {"workload": name, "desc": desc, "stencils": ne, "ms_knn": ms_knn,
+                "fp64": {"ms_build": ms64, "stencils_per_s": ne / (ms64 * 1e-3)},
+                "fp32_refined": {"ms_build": ms32, "stencils_per_s": ne / (ms32 * 1e-3), "speedup_vs_fp64": ms64 / ms32},
+                "max_row_rel_diff_refined_vs_fp64": err, "bar": 1e-8,
+                "apply": {"fields": nf, "nnz": W.nnz, "ms": ms_apply, "GB_s": by / (ms_apply * 1e-3) / 1e9,
+                          "frac_of_hbm": by / (ms_apply * 1e-3) / 1e9 / hbm,
+                          "fp64_fma_T_per_s": fmas, "frac_of_fp64_fma": fmas / fma_peak,
+                          "bound": "hbm" if by / (W.nnz * nf) > hbm / (fma_peak * 1e3) else "fp64 FMA (nnz x fields)"}}
+        if extra:
+            line.update(extra)
+        print(json.dumps(line), flush=True)
+
+    dev = torch.device("cuda", ctx.device)
+    # C1: 2D Laplacian, 10,000 uniform points, PHS3 degree 2, k = 20
+    rng = np.random.default_rng(101)
+    X = torch.from_numpy(rng.uniform(0, 1, (10_000, 2))).to(dev)
+    ms_knn, a = ev_ms(lambda: pkg.find_neighbors(X, k=20, ctx=ctx))
+    b = pkg.PHS(3, poly_deg=2)
+    ms64, W64 = ev_ms(lambda: pkg.build_weights([(3, 0)], X, None, a, b, ctx=ctx)[0])
+    ms32, W32 = ev_ms(lambda: pkg.build_weights([(3, 0)], X, None, a, b, ctx=ctx, precision="fp32_refined")[0])
+    f = torch.sin(4 * X[:, 0]) * torch.cos(3 * X[:, 1])
+    lap = W32.apply(f)
+    inner = ((X > 0.1) & (X < 0.9)).all(1)
+    err_f = float(((lap + 25 * f)[inner]).abs().max() / (25 * f[inner]).abs().max())
+    report("lap2d_10k", "2D Laplacian, 10,000 uniform points, PHS3 degree 2, k = 20 (26 x 26)", 10_000, ms_knn,
+           ms64, ms32, row_diff(W32, W64), W32, 1, kernel_ms(lambda: W32.apply(f)),
+           {"laplacian_rel_err_vs_analytic_interior": err_f, "note": "L2-resident sizes: launch-bound, not a roofline case"})
+    # C2: 3D gradient + Laplacian, 100^3 jittered lattice, PHS5 degree 2, k = 40, 16 fields
+    cfg = CONFIGS["gradlap3d_1M"]
+    X = torch.from_numpy(make_points(cfg, 1_000_000, 102)).to(dev)
+    ms_knn, a = ev_ms(lambda: pkg.find_neighbors(X, k=40, ctx=ctx))
+    b = pkg.PHS(5, poly_deg=2)
+    ms64, W64 = ev_ms(lambda: pkg.build_weights(cfg["ops"], X, None, a, b, ctx=ctx))
+    st = pkg._native.BuildStats()
+    ms32, W32 = ev_ms(lambda: pkg.build_weights(cfg["ops"], X, None, a, b, ctx=ctx, precision="fp32_refined",
+                                                stats=st))
+    err = max(row_diff(w, w0) for w, w0 in zip(W32, W64))
+    F = fourier_fields(torch, X, 16, 103)
+    stats = {"refined_fallback_stencils": int(st.n_fallback),
+             "refined_residuals_per_stencil": float(st.n_residuals) / max(1, int(st.n_stencils))}
+    report("gradlap3d_1M", "3D gradient + Laplacian (4 operators, one factorisation), 100^3 jittered lattice, "
+           "PHS5 degree 2, k = 40 (50 x 50); 16 fields per operator", 1_000_000, ms_knn, ms64, ms32, err, W32[3], 16,
+           kernel_ms(lambda: W32[3].apply(F)), stats)
+    del W64, W32, F, a, X
+    # C3: 2D unit disk, 2,000,000 interior + 5,000 boundary points, Dirichlet / Neumann, PHS3 degree 3, k = 30
+    Xh, isb, nrm, al, be = unit_disk(2_000_000, 5_000, 104)
+    X = torch.from_numpy(Xh).to(dev)
+    ms_knn, a = ev_ms(lambda: pkg.find_neighbors(X, k=30, ctx=ctx))
+    herm = dict(is_boundary=isb, bc=[pkg.BoundaryCondition(x, y) for x, y in zip(al, be)], normals=nrm)
+    ap, ai = pkg.ragged_stencils(a, torch.full((len(Xh),), 30, device=dev))
+    b = pkg.PHS(3, poly_deg=3)
+    st = pkg._native.BuildStats()
+    run = lambda prec: pkg.build_weights_batched([(3, 0)], X, None, ap, ai, b, hermite=herm, precision=prec,
+                                                 tune=1, ctx=ctx, stats=st)[0]
+    ms64, W64 = ev_ms(lambda: run("fp64"))
+    ms32, W32 = ev_ms(lambda: run("fp32_refined"))
+    stats = {"refined_fallback_stencils": int(st.n_fallback),
+             "refined_residuals_per_stencil": float(st.n_residuals) / max(1, int(st.n_stencils))}
+    u = X[:, 0] ** 2 + X[:, 1] ** 2 + 1.0
+    report("disk_hermite_2M", f"2D unit disk, {len(Xh) - 5000} interior + 5,000 boundary points (Dirichlet upper, "
+           "Neumann lower half-circle), PHS3 degree 3, k = 30 (40 x 40, Hermite rows on boundary stencils), one "
+           "persistent batched launch with autotuned tiles", len(Xh), ms_knn, ms64, ms32, row_diff(W32, W64), W32, 1,
+           kernel_ms(lambda: W32.apply(u)), stats)
+    del W64, W32, a, ap, ai, X
+    # C5: 3D regrid, 8,000,000 uniform sources onto 8,000,000 mixture targets, PHS3 degree 1, k = 20, 32 fields
+    rng = np.random.default_rng(105)
+    S = torch.from_numpy(rng.uniform(0, 1, (8_000_000, 3))).to(dev)
+    T = torch.from_numpy(mixture_targets(8_000_000, 106)).to(dev)
+    ms_knn, a = ev_ms(lambda: pkg.find_neighbors(S, T, k=20, ctx=ctx), reps=1)
+    b = pkg.PHS(3, poly_deg=1)
+    ms64, W64 = ev_ms(lambda: pkg.build_weights([(0, 0)], S, T, a, b, ctx=ctx)[0], reps=1)
+    ms32, W32 = ev_ms(lambda: pkg.build_weights([(0, 0)], S, T, a, b, ctx=ctx, precision="fp32_refined")[0], reps=1)
+    err = row_diff(W32, W64)
+    del W64
+    F = fourier_fields(torch, S, 32, 107)
+    ms_apply = kernel_ms(lambda: W32.apply(F))
+    # the same operator on Morton-ordered sources and targets (reorder_points): the gathers of
+    # the 32-field rows become local, so each source row is read from HBM about once
+    del W32, a
+    ps, So = pkg.reorder_points(S, ctx=ctx)
+    pt, To = pkg.reorder_points(T, ctx=ctx)
+    ao = pkg.find_neighbors(So, To, k=20, ctx=ctx)
+    Wo = pkg.build_weights([(0, 0)], So, To, ao, b, ctx=ctx, precision="fp32_refined")[0]
+    Fo = F[ps.long()].contiguous()
+    ms_o = kernel_ms(lambda: Wo.apply(Fo))
+    by = Wo.nnz * 12 + (8_000_001) * 8 + 32 * 16_000_000 * 8
+    report("regrid3d_8M", "3D regrid, 8,000,000 uniform sources onto 8,000,000 targets (50 % uniform, 50 % from 8 "
+           "Gaussians), PHS3 degree 1, k = 20 (24 x 24); 32 fields", 8_000_000, ms_knn, ms64, ms32, err, Wo, 32,
+           ms_apply, {"apply_morton_order": {"ms": ms_o, "GB_s": by / (ms_o * 1e-3) / 1e9,
+                                             "frac_of_hbm": by / (ms_o * 1e-3) / 1e9 / hbm}})
+
+
 def run_reference(args, cfg, n):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -308,6 +485,9 @@ def main():
     ctx = pkg.Context.default(local)
     stream = torch.cuda.current_stream()  # the package binds the library to this stream
     dev = torch.device("cuda", local)
+    if args.all_configs:
+        all_configs(pkg, torch, ctx, stream)
+        return
 
     # independent seeded cloud per rank (weak scaling: per-GPU work fixed)
     X_h = make_points(cfg, n, 1000 + rank)

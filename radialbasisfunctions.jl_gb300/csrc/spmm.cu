@@ -161,13 +161,26 @@ __global__ void __launch_bounds__(256) spmm_interleaved_kernel(int64_t ne, const
         const int64_t r = r0 + lane / nfp;
         if (r >= ne || f >= nf) continue;
         const int64_t a = rp[r], b = rp[r + 1];
+        // eight entries at a time: their indices and values first, then eight gathers in flight
         double s0 = 0.0, s1 = 0.0;
         int64_t p = a;
-        for (; p + 1 < b; p += 2) {
-            s0 = fma(__ldg(&val[p]), __ldg(&X[(int64_t)__ldg(&col[p]) * ldx + f]), s0);
-            s1 = fma(__ldg(&val[p + 1]), __ldg(&X[(int64_t)__ldg(&col[p + 1]) * ldx + f]), s1);
+        for (; p + 7 < b; p += 8) {
+            int c[8];
+            double v[8], xg[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                c[u] = __ldg(&col[p + u]);
+                v[u] = __ldg(&val[p + u]);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) xg[u] = __ldg(&X[(int64_t)c[u] * ldx + f]);
+#pragma unroll
+            for (int u = 0; u < 8; u += 2) {
+                s0 = fma(v[u], xg[u], s0);
+                s1 = fma(v[u + 1], xg[u + 1], s1);
+            }
         }
-        if (p < b) s0 = fma(__ldg(&val[p]), __ldg(&X[(int64_t)__ldg(&col[p]) * ldx + f]), s0);
+        for (; p < b; p++) s0 = fma(__ldg(&val[p]), __ldg(&X[(int64_t)__ldg(&col[p]) * ldx + f]), s0);
         const double s = s0 + s1;
         double *yp = &Y[r * ldy + f];
         *yp = (beta == 0.0) ? alpha * s : fma(alpha, s, beta * *yp);
