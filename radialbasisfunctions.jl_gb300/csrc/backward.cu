@@ -3,16 +3,18 @@
 // src/solve/ad_shared.jl:63-157).  Given the cotangent dW of the weights (CSR order), the
 // gradients Δdata (ns x dim) and Δeval (ne x dim) of L = <dW, W>.
 //
-// Per stencil, one warp in FP64.  The forward system is assembled in the stencil's local
-// coordinates X_i = (x_i - x0) s, s = 2^-es (as the forward build), factorised once and
-// solved for the weights λ (A λ = b) and the adjoint η (A η = [dW_i s^q; 0]: A is symmetric,
-// and the global weights are λ s^q for an operator of order q).  With the implicit-function
+// Per stencil, one warp.  The forward system is assembled in the stencil's local coordinates
+// X_i = (x_i - x0) s, s = 2^-es (as the forward build) and solved once for the weights λ
+// (A λ = b) and the adjoint η (A η = [dW_i s^q; 0]: A is symmetric, and the global weights are
+// λ s^q for an operator of order q): by an FP64 LU, or by the forward's FP32 factorisation
+// refined with FP64 residuals (FP64 fallback).  With the implicit-function
 // rule ΔA = -η λᵀ, Δb = η (backward.jl:31-58) and b_i = ℒφ(x0 - x_i):
 //   ∂L/∂X_i = Σ_ops [ Σ_{j≠i} -(η_i λ_j + η_j λ_i) ∇φ(X_i - X_j)            (backward.jl:85-120)
 //                     + Σ_m -(η_i λ_{k+m} + η_{k+m} λ_i) ∇p_m(X_i)        (backward.jl:122-145)
 //                     - η_i ∇ℒφ(-X_i) ]                                   (backward.jl:160-200)
-// Lane i owns point i and sums over all j (each pair is evaluated twice, no atomics).  The
-// weights depend on the positions only through X, so Δdata[x_i] += s ∂L/∂X_i (atomics: a
+// Lane i owns point i; for k <= 32 each pair term is evaluated once and its odd partner share
+// passed by a shuffle (otherwise lane i sums over all j).  The weights depend on the positions
+// only through X, so Δdata[x_i] += s ∂L/∂X_i (atomics: a
 // point belongs to many stencils) and Δeval[e] = -s Σ_i ∂L/∂X_i.  The polynomial
 // right-hand side ℒp_m(x0) is constant in local coordinates.
 // Supported: PHS 1/3/5/7, the identity (regrid), the Laplacian and first partials, interior
