@@ -37,7 +37,7 @@ __all__ = [
     "laplacian", "partial", "gradient", "jacobian", "regrid", "directional", "Directional", "RadialBasisOperator",
     "WeightsCSR", "WeightsSELL",
     "weights", "update_weights", "mul", "DimensionMismatch", "SingularException", "Context", "build_library",
-    "Interpolator", "sytrf_rook", "sytrs_rook", "build_weights", "build_weights_backward", "build_weights_differentiable", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph", "reorder_points",
+    "Interpolator", "sytrf_rook", "sytrs_rook", "apply_differentiable", "build_weights", "build_weights_backward", "build_weights_differentiable", "build_weights_batched", "ragged_stencils", "tuning_report", "BuildApplyGraph", "reorder_points",
 ]
 
 build_library = _native.build_library
@@ -779,6 +779,43 @@ def sytrs_rook(F, ipiv, b, *, ctx: Context | None = None):
     ctx.check(ctx.lib.rbf_sytrs_rook(ctx.h, n, Bc.shape[0], _ptr(Fc), n, _ptr(ipiv.to(torch.int32).contiguous()),
                                      _ptr(Bc), n))
     return Bc[0] if one else Bc.t()
+
+
+def apply_differentiable(W, x, val=None):
+    """y = W x as a torch autograd function of the field x (n, or (n, nf)) and of the values
+    `val` (W's values by default; pass the differentiable values of
+    build_weights_differentiable to reach the point positions).  The backward applies W^T to
+    the cotangent through the library (the transposed CSR from rbf_csr_to_csc, then the same
+    apply) and gives the values' cotangent g[row] x[col] -- the rules the reference's AD
+    extensions define for op(x) (ext/RadialBasisFunctionsMooncakeExt / EnzymeExt, on
+    _eval_op, src/operators/operators.jl:217-218)."""
+    torch = _torch()
+
+    class _ApplyFn(torch.autograd.Function):
+        @staticmethod
+        def forward(fctx, v, xx):
+            Wv = WeightsCSR(W.row_ptr, W.col, v.detach().contiguous(), W.shape, W.ctx)
+            fctx.save_for_backward(v, xx)
+            return Wv.apply(xx.detach().contiguous())
+
+        @staticmethod
+        def backward(fctx, g):
+            v, xx = fctx.saved_tensors
+            ne, ns = W.shape
+            g = g.contiguous()
+            dv = dx = None
+            if fctx.needs_input_grad[1]:
+                cp, rw, vv = WeightsCSR(W.row_ptr, W.col, v.detach().contiguous(), W.shape, W.ctx).to_csc()
+                dx = WeightsCSR(cp, rw, vv, (ns, ne), W.ctx).apply(g)
+            if fctx.needs_input_grad[0]:
+                rows = torch.repeat_interleave(torch.arange(ne, device=g.device), W.row_ptr[1:] - W.row_ptr[:-1])
+                cols = W.col.long()
+                prod = g[rows] * xx.detach()[cols]
+                dv = prod if prod.ndim == 1 else prod.sum(-1)
+            return dv, dx
+
+    v = W.val if val is None else val
+    return _ApplyFn.apply(v, x)
 
 
 def reorder_points(data, k=None, ctx=None):
