@@ -98,3 +98,23 @@ def test_regrid(pkg):
     r = pkg.regrid(X, X2)  # default basis
     assert isinstance(r, pkg.RadialBasisOperator) and mpe(r(y), f(X2)) < 0.1
     assert isinstance(pkg.regrid(X, X2, basis=pkg.PHS(5, poly_deg=3)), pkg.RadialBasisOperator)
+
+
+def test_directional(pkg):
+    """test/operators/directional.jl: one direction, one per point, other eval points, and the
+    reference's errors for a direction of the wrong dimension or count."""
+    y = f(X)
+    rng = np.random.default_rng(456)
+    v = np.array([2.0, 1.0]) / np.hypot(2.0, 1.0)
+    d = pkg.directional(X, v, pkg.PHS(3, poly_deg=2))(y)
+    assert mpe(d, df_dx(X) * v[0] + df_dy(X) * v[1]) < 10
+    V = rng.uniform(0, 1, (10_000, 2))
+    V /= np.linalg.norm(V, axis=1, keepdims=True)
+    d = pkg.directional(X, V, pkg.PHS(3, poly_deg=2))(y)
+    assert mpe(d, df_dx(X) * V[:, 0] + df_dy(X) * V[:, 1]) < 10
+    d = pkg.directional(X, V, eval_points=X.copy(), basis=pkg.PHS(3, poly_deg=2))(y)
+    assert mpe(d, df_dx(X) * V[:, 0] + df_dy(X) * V[:, 1]) < 10
+    with pytest.raises(ValueError):
+        pkg.directional(X, np.array([2.0, 1.0, 0.5]))(y)
+    with pytest.raises(ValueError):
+        pkg.directional(X, V[:-1])(y)
