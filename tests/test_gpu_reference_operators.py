@@ -118,3 +118,21 @@ def test_directional(pkg):
         pkg.directional(X, np.array([2.0, 1.0, 0.5]))(y)
     with pytest.raises(ValueError):
         pkg.directional(X, V[:-1])(y)
+
+
+def test_operator_algebra(pkg):
+    """test/operators/operator_algebra.jl:9-35: sums and differences of partials reproduce the
+    derivatives of a linear field exactly (MPE < 1e-6); operators on other data or other
+    stencils cannot be combined."""
+    x = X[:1000]
+    y = 2 * x[:, 0] + 3 * x[:, 1]
+    dx = pkg.partial(x, 1, 1)
+    dy = pkg.partial(x, 1, 2)
+    assert mpe((dx + dy)(y), np.full(1000, 5.0)) < 1e-6
+    assert mpe((dx - dy)(y), np.full(1000, -1.0)) < 1e-6
+    with pytest.raises(ValueError):
+        dx + pkg.partial(x[:500], 1, 2)
+    adjl = np.asarray(dx.adjl.cpu() if hasattr(dx.adjl, "cpu") else dx.adjl).copy()
+    adjl[[0, 1]] = adjl[[1, 0]]
+    with pytest.raises(ValueError):
+        dx + pkg.partial(x, 1, 2, adjl=adjl)
