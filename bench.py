@@ -710,6 +710,19 @@ def main():
                    "kernel": "build_backward_kernel (FP64, one warp per stencil: assembly, LU with the weights' and "
                              "the adjoint's right-hand sides, pair gradients, atomic scatter); refined: "
                              "build_backward_refined_kernel (FP32 factor refined in FP64, FP64 fallback)"}
+        if world == 1 and not args.no_cpu_baseline:
+            # the reference's pullback restated in C (global coordinates, rook Bunch-Kaufman,
+            # OpenMP on all host cores) on a sample of the same stencils
+            from oracle import oracle as O
+            m = 100_000
+            a_h = adj_b[:m].cpu().numpy()
+            dW_h = np.random.default_rng(8).random((len(cfg["ops"]), m, k)) - 0.5
+            t0 = time.perf_counter()
+            O.build_backward_c(X_h, X_h[:m], a_h, cfg["dim"], cfg["phs"], cfg["deg"], cfg["ops"], dW_h)
+            t1 = time.perf_counter()
+            adjoint["cpu"] = {"stencils_per_s": m / (t1 - t0), "cores": O.num_threads(), "kind": "port",
+                              "sample": f"{m} stencils of the same cloud: the C restatement of the reference's "
+                                        "pullback (global coordinates, rook Bunch-Kaufman)"}
         del dW, rp, adj_b, g64, g32
 
     # ---- the same workload after reorder_points (Morton order, the reference's locality

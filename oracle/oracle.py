@@ -84,6 +84,8 @@ def lib():
         L.orc_knn_grid.restype = ctypes.c_int
         L.orc_knn_grid.argtypes = [P, i64, P, i64, ctypes.c_int, ctypes.c_int, P, ctypes.c_int]
         L.orc_num_threads.restype = ctypes.c_int
+        L.orc_build_backward.restype = ctypes.c_int
+        L.orc_build_backward.argtypes = [P, P, i64, P, i64, P, ctypes.c_int, P, P, P, ctypes.c_int]
         L.orc_interp_matrix.restype = ctypes.c_int
         L.orc_interp_matrix.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, i64, P]
         L.orc_interp_eval.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, i64, P, P, i64, P, ctypes.c_int]
@@ -420,3 +422,21 @@ def lapack_rook_solver():
                              ctypes.byref(info), ctypes.c_size_t(1))
         return B[:, 0]
     return solve
+
+
+def build_backward_c(data, eval_points, adjl, dim, phs, poly_deg, ops, dW, nthreads=0):
+    """The pullback of the weight build in C (OpenMP): the same rules as
+    backward_oracle.build_backward (dW: (len(ops), ne, k), stencil order); returns
+    (ddata, deval)."""
+    data, eval_points = _f64(data), _f64(eval_points)
+    adjl = np.ascontiguousarray(adjl, dtype=np.int32)
+    dW = np.ascontiguousarray(dW, dtype=np.float64)
+    ns, ne, k = data.shape[0], eval_points.shape[0], adjl.shape[1]
+    ddata = np.zeros((ns, dim))
+    deval = np.zeros((ne, dim))
+    cfg = make_cfg(dim, phs, poly_deg, ops)
+    bad = lib().orc_build_backward(ctypes.byref(cfg), _p(data), ns, _p(eval_points), ne, _p(adjl), k, _p(dW),
+                                   _p(ddata), _p(deval), nthreads)
+    if bad:
+        raise np.linalg.LinAlgError(f"{bad} singular stencil systems")
+    return ddata, deval

@@ -954,3 +954,160 @@ void orc_interp_eval(int dim, int phs, int poly_deg, const double *x, int64_t n,
         out[t] = rbf + poly;
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* pullback of the weight build (reverse-mode sensitivities to the points):  */
+/* src/solve/ad_shared.jl:63-127 with src/solve/backward.jl:31-363, in the   */
+/* reference's global coordinates                                            */
+/* ------------------------------------------------------------------------ */
+/* d^alpha of monomial e at x */
+static double mono_dalpha(const int *e, const int *alpha, const double *x, int dim) {
+    double v = 1.0;
+    for (int d = 0; d < dim; d++) {
+        if (alpha[d] > e[d]) return 0.0;
+        double c = 1.0;
+        for (int t = 0; t < alpha[d]; t++) c *= (double)(e[d] - t);
+        v *= c;
+        for (int t = 0; t < e[d] - alpha[d]; t++) v *= x[d];
+    }
+    return v;
+}
+
+/* d/dx of (L phi)(x, xi) at D = x - xi (operator_second_derivatives.jl; PHS1 rows vanish
+   below r = 1e-12; the identity uses the basis gradient) */
+static void grad_applied(int p, int op, int od, const double *D, int dim, double *g) {
+    double r2 = 0.0;
+    for (int d = 0; d < dim; d++) r2 = r2 + D[d] * D[d];
+    const double r = sqrt(r2);
+    if (op == OP_IDENT) {
+        const double c = p == 1 ? 1.0 / (r + AVOID_INF) : (p == 3 ? 3.0 * r : (p == 5 ? 5.0 * pw3(r) : 7.0 * pw5(r)));
+        for (int d = 0; d < dim; d++) g[d] = c * D[d];
+        return;
+    }
+    if (p == 1 && r < 1.0e-12) {
+        for (int d = 0; d < dim; d++) g[d] = 0.0;
+        return;
+    }
+    if (op == OP_LAP) {
+        const double c = p == 1 ? -2.0 / pw3(r) : (p == 3 ? 12.0 / (r + AVOID_INF) : (p == 5 ? 90.0 * r : 280.0 * pw3(r)));
+        for (int d = 0; d < dim; d++) g[d] = c * D[d];
+        return;
+    }
+    const double dd = D[od];
+    double a, b;
+    if (p == 1) { a = -1.0 / pw3(r); b = 1.0 / r; }
+    else if (p == 3) { a = 3.0 / (r + AVOID_INF); b = 3.0 * r; }
+    else if (p == 5) { a = 15.0 * r; b = 5.0 * pw3(r); }
+    else { a = 35.0 * pw3(r); b = 7.0 * pw5(r); }
+    for (int d = 0; d < dim; d++) g[d] = a * dd * D[d] + (d == od ? b : 0.0);
+}
+
+/* Gradients of L = sum dW .* w (w the weights in stencil order, dW: nops x ne x k) with
+   respect to the data points (ddata, ns x dim, accumulated) and the eval points (deval,
+   ne x dim).  Interior stencils; PHS 1/3/5/7; identity, first partials, Laplacian.
+   Returns the number of singular stencils. */
+int orc_build_backward(const orc_cfg *c, const double *data, int64_t ns, const double *eval, int64_t ne,
+                       const int32_t *adjl, int k, const double *dW, double *ddata, double *deval, int nthreads) {
+    (void)ns;
+    const int dim = c->dim, nops = c->nops;
+    int exps[64 * MAXDIM];
+    const int nmon = orc_monomial_exponents(dim, c->poly_deg, exps);
+    const int n = k + nmon;
+    int bad = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : bad)
+#endif
+    for (int64_t e = 0; e < ne; e++) {
+        const int32_t *nb = adjl + e * (int64_t)k;
+        const double *x0 = eval + e * dim;
+        double X[MAXN * MAXDIM];
+        double *A = (double *)malloc(sizeof(double) * n * n);
+        double *S = (double *)malloc(sizeof(double) * n * 2 * nops);  /* [lambda | eta], column-major */
+        int *ipiv = (int *)malloc(sizeof(int) * n);
+        for (int i = 0; i < k; i++)
+            for (int d = 0; d < dim; d++) X[i * dim + d] = data[(int64_t)nb[i] * dim + d];
+        orc_assemble(c, X, k, x0, NULL, A, S);
+        for (int q = 0; q < nops; q++)
+            for (int i = 0; i < n; i++)
+                S[(nops + q) * n + i] = i < k ? dW[((int64_t)q * ne + e) * k + i] : 0.0;
+        if (sytrf_rook_u(n, A, n, ipiv, 0) != 0) {
+            bad++;
+            free(A); free(S); free(ipiv);
+            continue;
+        }
+        orc_sytrs_rook_u(n, 2 * nops, A, n, ipiv, S, n);
+        const double *lam = S, *eta = S + (size_t)nops * n;
+        double dX[MAXN * MAXDIM];
+        double de[MAXDIM] = {0.0, 0.0, 0.0};
+        for (int t = 0; t < k * dim; t++) dX[t] = 0.0;
+        /* collocation: RBF pairs (backward.jl:85-131) and the polynomial block (:133-160) */
+        for (int j = 0; j < k; j++)
+            for (int i = 0; i < j; i++) {
+                double sc = 0.0;
+                for (int q = 0; q < nops; q++)
+                    sc = sc - (eta[q * n + i] * lam[q * n + j] + eta[q * n + j] * lam[q * n + i]);
+                double g[MAXDIM];
+                orc_phs_grad(c->phs, X + i * dim, X + j * dim, dim, g);
+                for (int d = 0; d < dim; d++) {
+                    dX[i * dim + d] += sc * g[d];
+                    dX[j * dim + d] -= sc * g[d];
+                }
+            }
+        for (int i = 0; i < k; i++)
+            for (int m = 0; m < nmon; m++) {
+                double sc = 0.0;
+                for (int q = 0; q < nops; q++)
+                    sc = sc - (eta[q * n + i] * lam[q * n + k + m] + eta[q * n + k + m] * lam[q * n + i]);
+                for (int d = 0; d < dim; d++) {
+                    int al[MAXDIM] = {0, 0, 0};
+                    al[d] = 1;
+                    dX[i * dim + d] += sc * mono_dalpha(exps + m * dim, al, X + i * dim, dim);
+                }
+            }
+        /* right-hand side: b_i = L phi(x0, x_i) (backward.jl:163-222) and L p_m(x0) (:223-363) */
+        for (int q = 0; q < nops; q++) {
+            const int op = c->op_code[q], od = c->op_dim[q];
+            for (int i = 0; i < k; i++) {
+                double D[MAXDIM], g[MAXDIM];
+                for (int d = 0; d < dim; d++) D[d] = x0[d] - X[i * dim + d];
+                grad_applied(c->phs, op, od, D, dim, g);
+                for (int d = 0; d < dim; d++) {
+                    de[d] += eta[q * n + i] * g[d];
+                    dX[i * dim + d] -= eta[q * n + i] * g[d];
+                }
+            }
+            for (int m = 0; m < nmon; m++)
+                for (int d = 0; d < dim; d++) {
+                    int al[MAXDIM] = {0, 0, 0};
+                    double v = 0.0;
+                    al[d] = 1;
+                    if (op == OP_IDENT) {
+                        v = mono_dalpha(exps + m * dim, al, x0, dim);
+                    } else if (op == OP_D1) {
+                        al[od] += 1;
+                        v = mono_dalpha(exps + m * dim, al, x0, dim);
+                    } else if (op == OP_LAP) {
+                        for (int cc = 0; cc < dim; cc++) {
+                            int b2[MAXDIM] = {al[0], al[1], al[2]};
+                            b2[cc] += 2;
+                            v += mono_dalpha(exps + m * dim, b2, x0, dim);
+                        }
+                    }
+                    de[d] += eta[q * n + k + m] * v;
+                }
+        }
+        for (int i = 0; i < k; i++)
+            for (int d = 0; d < dim; d++) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                ddata[(int64_t)nb[i] * dim + d] += dX[i * dim + d];
+            }
+        for (int d = 0; d < dim; d++) deval[e * dim + d] = de[d];
+        free(A);
+        free(S);
+        free(ipiv);
+    }
+    return bad;
+}

@@ -71,3 +71,21 @@ def test_cloud3d_separate_eval(orc, bo, phs, ops):
     used = np.zeros(len(data), bool)
     used[np.unique(adjl)] = True
     assert np.all(gd[~used] == 0.0)
+
+
+@pytest.mark.parametrize("phs,ops,dim", [(3, [(OP_LAP, 0)], 3), (5, [(OP_D1, 0), (OP_D1, 1), (OP_D1, 2)], 3),
+                                         (1, [(OP_D1, 1), (OP_LAP, 0)], 2), (7, [(OP_IDENT, 0)], 3)])
+def test_c_pullback_matches(orc, bo, phs, ops, dim):
+    """The C restatement (timed as the CPU baseline of the adjoint) equals the Python one to
+    the rounding of their solvers (rook Bunch-Kaufman there, numpy's LU here; 1.4e-12 apart on
+    PHS7's poorly conditioned systems)."""
+    rng = np.random.default_rng(21)
+    data = rng.uniform(0, 1, (200, dim))
+    ev = rng.uniform(0.2, 0.8, (30, dim))
+    k = 20
+    adjl = orc.knn(data, ev, k)
+    dW = rng.standard_normal((len(ops), len(ev), k))
+    pd, pe = bo.build_backward(data, ev, adjl, dim, phs, 2, ops, dW)
+    cd, ce = orc.build_backward_c(data, ev, adjl, dim, phs, 2, ops, dW)
+    assert np.abs(cd - pd).max() <= 1e-10 * np.abs(pd).max()
+    assert np.abs(ce - pe).max() <= 1e-10 * np.abs(pe).max()
