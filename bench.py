@@ -662,7 +662,17 @@ def main():
     csr_bytes = nnz * 12 + (n + 1) * 8 + 2 * n * 8
     apply_gbs = apply_bytes / (ms_spmv * 1e-3) / 1e9
     csr_gbs = csr_bytes / (ms_spmv_csr * 1e-3) / 1e9
-    del W, W_sell
+    # operator algebra on the device (a + 2 b over two value arrays of one structure, as a sum of
+    # two operators on the same stencils):
+    # one entry-wise pass over the value arrays, 24 bytes per entry (two reads, one write)
+    alg_out = torch.empty_like(W.val)
+    alg_b = W.val.clone()  # a second operand in its own memory
+    ms_axpby = timed(lambda: ctx.check(ctx.lib.rbf_weights_axpby(ctx.h, nnz, 1.0, pkg._ptr(W.val), 2.0,
+                                                                  pkg._ptr(alg_b), pkg._ptr(alg_out))), 5, 2)
+    alg_gbs = 24 * nnz / (ms_axpby * 1e-3) / 1e9
+    algebra = {"kernel": "axpby_kernel (rbf_weights_axpby: out = a + 2 b over the values)", "nnz": nnz,
+               "ms": ms_axpby, "GB_s": alg_gbs, "frac_of_hbm": alg_gbs / PEAKS.get("hbm_gbs", 6800.0)}
+    del W, W_sell, alg_out, alg_b
     hbm_peak = PEAKS.get("hbm_gbs", 6800.0)
     hbm_src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in PEAKS else "fallback"
     fp64_peak = pkg.ctypes.c_double(0.0)
@@ -813,6 +823,7 @@ def main():
                               "kernel": "spmv_pair_kernel", "bytes": "nnz*12 + (ne+1)*8 + 2*n*8"}},
             "reordered": reordered,
             "adjoint": adjoint,
+            "algebra": algebra,
             "interpolator": interp,
             "kernels_ms": {"knn": ms_knn_kernel, "knn_per_call_api": ms_knn, "build_headline": ms_kernel,
                            "build_fp64": float(st64.ms_build), "spmv": ms_spmv},
