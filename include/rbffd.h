@@ -297,6 +297,13 @@ int rbf_mlp_gemm_tc(rbf_ctx *ctx, int32_t M, int32_t N, int32_t K, const void *A
 /* *failed = 1 if a tensor-core GEMM since the last call gave up waiting on its pipeline
  * (its output is then incomplete); synchronises the context's stream. */
 int rbf_mlp_tc_status(rbf_ctx *ctx, int32_t *failed);
+/* Self-test of the tensor-core GEMM's bounded waits: one small launch (M = 256, N = 32,
+ * K = 64) whose producer issues no copy and whose waits give up after 4096 polls, so that
+ * the timeout path runs with nothing in flight: the block raises its abort flag, frees its
+ * tensor memory and returns.  *failed receives the error flag that launch left (1 means the
+ * timeout was detected and reported); an error flag left by an earlier GEMM stays set for
+ * the next rbf_mlp_tc_status. */
+int rbf_mlp_tc_selftest_timeout(rbf_ctx *ctx, int32_t *failed);
 /* mean squared error over rows x cols and its gradient (bf16, zero in the padding) */
 int rbf_mlp_mse(rbf_ctx *ctx, int32_t rows, int32_t cols, const float *Y, int32_t ldy, const float *T,
                 int32_t ldt, void *dY, int32_t ldd, int32_t pad_cols, float *loss);
@@ -365,7 +372,9 @@ int rbf_plan_destroy(rbf_plan *plan);
  * loaded on until exit: it is rejected (RBF_ERR_ARGUMENT) when nf*(ns+ne) exceeds
  * 4,194,304 doubles.  The first call on a device looks up that array's address (set-up
  * once per device); make that first call before any stream capture.  All calls share the
- * array, so calls that overlap on the GPU race; each call overwrites what it reads. */
+ * array, so calls that overlap on the GPU race; each call overwrites what it reads.  Like
+ * every entry point it returns after its work on the context's stream is complete; with
+ * rbf_ctx_set_timing on, rbf_ctx_last_ms gives its device time. */
 int rbf_spmm_noalloc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const int32_t *col,
                      const double *val, int32_t nf, int32_t layout, const double *X, int64_t ldx,
                      double alpha, double beta, double *Y, int64_t ldy);

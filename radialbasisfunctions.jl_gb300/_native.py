@@ -145,6 +145,7 @@ SIGNATURES = {
     "rbf_ctx_last_ms": (_I, [_P, _P]),
     "rbf_mlp_gemm_tc": (_I, [_P, _I32, _I32, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _P, _I32]),
     "rbf_mlp_tc_status": (_I, [_P, _P]),
+    "rbf_mlp_tc_selftest_timeout": (_I, [_P, _P]),
     "rbf_mlp_features": (_I, [_P, _P, _I64, _P, _I32, _P, _I64, _I32, _P, _I32]),
     "rbf_mlp_to_bf16": (_I, [_P, _I32, _I32, _I32, _P, _I32, _P, _I32]),
     "rbf_mlp_mse": (_I, [_P, _I32, _I32, _P, _I32, _P, _I32, _P, _I32, _I32, _P]),

@@ -290,8 +290,9 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
            (2ull << 61);
 }
 
-__device__ __forceinline__ bool mbar_wait_abort(uint32_t bar, uint32_t parity, volatile int *abort_flag) {
-    for (unsigned it = 0; it < kWaitLimit; it++) {
+__device__ __forceinline__ bool mbar_wait_abort(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                                unsigned limit = kWaitLimit) {
+    for (unsigned it = 0; it < limit; it++) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -309,7 +310,9 @@ template <int BN>
 __global__ void __launch_bounds__(tp_threads(BN), 1)
     gemm_tc_persistent_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int M,
                               int N, int K, const float *__restrict__ bias, int gelu_on, float *__restrict__ Cf,
-                              __nv_bfloat16 *__restrict__ Cb, int ldc) {
+                              __nv_bfloat16 *__restrict__ Cb, int ldc, unsigned wait_limit, int issue_loads) {
+    // issue_loads == 0 (self-test only): the producer issues no copy at all, so every wait of
+    // the other roles runs out after wait_limit polls with nothing in flight
     constexpr int A_BYTES = TC_M * TP_KB * 2, B_BOX = BN * TP_KB * 2;
     constexpr uint32_t TMEM_COLS = 2 * BN;  // two accumulators; BN in {32, 64, 128, 256}
     constexpr int EPI = tp_epi_warps(BN), PARTS = EPI / 4, PCOLS = BN / PARTS;
@@ -352,7 +355,7 @@ __global__ void __launch_bounds__(tp_threads(BN), 1)
     int issued = 0;
 
     if (warp == 0) {
-        if (lane == 0 && !abort_flag) {
+        if (lane == 0 && !abort_flag && issue_loads) {
             // B once: nkb boxes of 64 K-elements x BN rows (zero-filled past K)
             const uint32_t bb = smem_u32(&bfull);
             mbar_expect(bb, (uint32_t)nkb * B_BOX);
@@ -363,7 +366,7 @@ __global__ void __launch_bounds__(tp_threads(BN), 1)
                 for (int kb = 0; kb < nkb; kb++, it++) {
                     const int s = it % TP_STAGES;
                     if (it >= TP_STAGES &&
-                        !mbar_wait_abort(smem_u32(&empty[s]), ((it / TP_STAGES) - 1) & 1, &abort_flag))
+                        !mbar_wait_abort(smem_u32(&empty[s]), ((it / TP_STAGES) - 1) & 1, &abort_flag, wait_limit))
                         break;
                     const uint32_t a0 = smem_u32(asm_ring + s * A_BYTES), bar = smem_u32(&full[s]);
                     mbar_expect(bar, A_BYTES);
@@ -373,17 +376,17 @@ __global__ void __launch_bounds__(tp_threads(BN), 1)
             }
         }
     } else if (warp == 1) {
-        if (lane == 0 && !abort_flag && mbar_wait_abort(smem_u32(&bfull), 0, &abort_flag)) {
+        if (lane == 0 && !abort_flag && mbar_wait_abort(smem_u32(&bfull), 0, &abort_flag, wait_limit)) {
             int it = 0, tc = 0;
             for (int t = blockIdx.x; t < ntiles && !abort_flag; t += gridDim.x, tc++) {
                 const int buf = tc & 1;
-                if (tc >= 2 && !mbar_wait_abort(smem_u32(&acce[buf]), ((tc >> 1) - 1) & 1, &abort_flag)) break;
+                if (tc >= 2 && !mbar_wait_abort(smem_u32(&acce[buf]), ((tc >> 1) - 1) & 1, &abort_flag, wait_limit)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                 const uint32_t d = tmem + (uint32_t)(buf * BN);
                 bool ok = true;
                 for (int kb = 0; kb < nkb; kb++, it++) {
                     const int s = it % TP_STAGES;
-                    if (!mbar_wait_abort(smem_u32(&full[s]), (it / TP_STAGES) & 1, &abort_flag)) {
+                    if (!mbar_wait_abort(smem_u32(&full[s]), (it / TP_STAGES) & 1, &abort_flag, wait_limit)) {
                         ok = false;
                         break;
                     }
@@ -418,7 +421,7 @@ __global__ void __launch_bounds__(tp_threads(BN), 1)
         int tc = 0;
         for (int t = blockIdx.x; t < ntiles && !abort_flag; t += gridDim.x, tc++) {
             const int buf = tc & 1;
-            if (!mbar_wait_abort(smem_u32(&accf[buf]), (tc >> 1) & 1, &abort_flag)) break;
+            if (!mbar_wait_abort(smem_u32(&accf[buf]), (tc >> 1) & 1, &abort_flag, wait_limit)) break;
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             char *stg = stg_all + (warp - 2) * TP_STG_WARP;
             const int esz = Cb ? 2 : 4, seg_cols = 64 / esz;  // 32 bf16 or 16 FP32 columns per piece
@@ -507,7 +510,7 @@ __global__ void __launch_bounds__(tp_threads(BN), 1)
             for (int it = consumed; it < issued; it++) {
                 const int s = it % TP_STAGES;
                 volatile int never = 0;
-                mbar_wait_abort(smem_u32(&full[s]), (it / TP_STAGES) & 1, &never);
+                mbar_wait_abort(smem_u32(&full[s]), (it / TP_STAGES) & 1, &never);  // full limit
             }
             atomicExch(&g_tc_error, 1u);
         }
@@ -568,7 +571,8 @@ int launch_tc(rbf_ctx *ctx, int M, int N, int K, const void *A, int lda, const v
 
 template <int BN>
 int launch_tc_persistent(rbf_ctx *ctx, int M, int N, int K, const void *A, int lda, const void *B, int ldb,
-                         const float *bias, int gelu_on, float *Cf, void *Cb, int ldc) {
+                         const float *bias, int gelu_on, float *Cf, void *Cb, int ldc, unsigned wait_limit = kWaitLimit,
+                         int issue_loads = 1) {
     const int nkb = (K + TP_KB - 1) / TP_KB;
     const size_t smem = (size_t)nkb * BN * TP_KB * 2 + (size_t)TP_STAGES * TC_M * TP_KB * 2 +
                         (size_t)tp_epi_warps(BN) * TP_STG_WARP;
@@ -580,7 +584,8 @@ int launch_tc_persistent(rbf_ctx *ctx, int M, int N, int K, const void *A, int l
     const int ntiles = (M + TC_M - 1) / TC_M;
     const int grid = std::max(1, std::min(ntiles, ctx->num_sms));
     gemm_tc_persistent_kernel<BN><<<grid, tp_threads(BN), smem, ctx->stream>>>(ma, mb, M, N, K, bias, gelu_on, Cf,
-                                                                           (__nv_bfloat16 *)Cb, ldc);
+                                                                           (__nv_bfloat16 *)Cb, ldc, wait_limit,
+                                                                           issue_loads);
     RBF_CHECK_LAUNCH(ctx);
     return RBF_OK;
 }
@@ -611,6 +616,32 @@ int rbf_mlp_gemm_tc(rbf_ctx *ctx, int32_t M, int32_t N, int32_t K, const void *A
     if (N <= 64) return launch_tc<64>(ctx, M, N, K, A, lda, B, ldb, bias, gelu_on, Cf, Cb, ldc);
     if (N <= 128) return launch_tc<128>(ctx, M, N, K, A, lda, B, ldb, bias, gelu_on, Cf, Cb, ldc);
     return launch_tc<256>(ctx, M, N, K, A, lda, B, ldb, bias, gelu_on, Cf, Cb, ldc);
+}
+
+// Self-test of the bounded waits: one persistent GEMM (M = 256, N = 32, K = 64) whose
+// producer issues no copy, with a wait limit of 4096 polls.  The MMA warp's wait for the
+// resident weights runs out, it raises the abort flag, the epilogue warps give up their
+// waits, and the block frees its tensor memory and returns: no copy and no MMA was ever in
+// flight.  *failed receives the error flag that launch left (1 when the timeout path works).
+int rbf_mlp_tc_selftest_timeout(rbf_ctx *ctx, int32_t *failed) {
+    if (!ctx || !failed) return RBF_ERR_ARGUMENT;
+    RBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    int32_t before = 0;
+    RBF_TRY(rbf_mlp_tc_status(ctx, &before));  // clear what earlier launches left
+    constexpr int M = 256, N = 32, K = 64;
+    DevBuf a, b, c;
+    RBF_TRY(a.alloc(ctx, sizeof(__nv_bfloat16) * M * K));
+    RBF_TRY(b.alloc(ctx, sizeof(__nv_bfloat16) * N * K));
+    RBF_TRY(c.alloc(ctx, sizeof(float) * M * N));
+    RBF_CUDA(ctx, cudaMemsetAsync(a.ptr, 0, sizeof(__nv_bfloat16) * M * K, ctx->stream));
+    RBF_CUDA(ctx, cudaMemsetAsync(b.ptr, 0, sizeof(__nv_bfloat16) * N * K, ctx->stream));
+    RBF_TRY(launch_tc_persistent<32>(ctx, M, N, K, a.ptr, K, b.ptr, K, nullptr, 0, c.as<float>(), nullptr, N, 4096u, 0));
+    RBF_TRY(rbf_mlp_tc_status(ctx, failed));
+    if (before) {  // keep an earlier failure visible to the next status call
+        unsigned int one = 1;
+        RBF_CUDA(ctx, cudaMemcpyToSymbol(g_tc_error, &one, sizeof one));
+    }
+    return RBF_OK;
 }
 
 // 0: every tensor-core GEMM since the last call completed; 1: one gave up waiting (its

@@ -298,9 +298,11 @@ int rbf_spmm_device(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *d_rp, c
         RBF_TRY(xs.alloc(ctx, sizeof(double) * ns * nf));
         RBF_TRY(ys.alloc(ctx, sizeof(double) * ne * nf));
         dim3 tb(32, 8);
-        to_interleaved_kernel<<<dim3((unsigned)((ns + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
-            ns, nf, d_X, ldx, xs.as<double>());
-        RBF_CHECK_LAUNCH(ctx);
+        if (ns > 0) {  // with no data points every row is empty and X is never read
+            to_interleaved_kernel<<<dim3((unsigned)((ns + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0,
+                                    ctx->stream>>>(ns, nf, d_X, ldx, xs.as<double>());
+            RBF_CHECK_LAUNCH(ctx);
+        }
         if (beta != 0.0) {
             to_interleaved_kernel<<<dim3((unsigned)((ne + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
                 ne, nf, d_Y, ldy, ys.as<double>());
@@ -373,7 +375,10 @@ constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 double *g_noalloc_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (set up once per device).
+// Device address of the scratch array on the current device, looked up once per device with
+// that device current.  The cached address belongs to the device's primary context: after a
+// cudaDeviceReset every context of this library is invalid as well and the library must not
+// be called again in that process.
 int noalloc_scratch(rbf_ctx *ctx, double **out) {
     if (ctx->device < 0 || ctx->device >= kMaxDevices)
         return rbf_fail(ctx, RBF_ERR_ARGUMENT, "device %d out of range for the no-alloc apply", ctx->device);
@@ -387,6 +392,56 @@ int noalloc_scratch(rbf_ctx *ctx, double **out) {
         g_noalloc_ptr[ctx->device] = static_cast<double *>(p);
     }
     *out = g_noalloc_ptr[ctx->device];
+    return RBF_OK;
+}
+}  // namespace
+
+namespace {
+// The device work of the allocation-free apply (arguments already checked).
+int noalloc_apply(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const int32_t *col,
+                  const double *val, int32_t nf, int32_t layout, const double *X, int64_t ldx, double alpha,
+                  double beta, double *Y, int64_t ldy) {
+    const bool staged = (layout == 0 && nf > 1);
+    if (!staged) {
+        if (nf == 1) {
+            RBF_TRY(spmv_launch(ctx, ne, row_ptr, col, val, X, alpha, beta, Y));
+        } else {
+            for (int f0 = 0; f0 < nf; f0 += 32) {
+                int nfc = std::min(32, nf - f0), nfp = 1;
+                while (nfp < nfc) nfp <<= 1;
+                int64_t warps = (ne + (32 / nfp) - 1) / (32 / nfp);
+                spmm_interleaved_kernel<<<blocks_for(ctx, warps * 32, 256, 16), 256, 0, ctx->stream>>>(
+                    ne, row_ptr, col, val, nfc, nfp, X + f0, ldx, alpha, beta, Y + f0, ldy);
+                RBF_CHECK_LAUNCH(ctx);
+            }
+        }
+    } else {
+        double *scratch = nullptr;
+        RBF_TRY(noalloc_scratch(ctx, &scratch));
+        double *xs = scratch, *ys = scratch + (size_t)nf * ns;
+        dim3 tb(32, 8);
+        if (ns > 0) {  // with no data points every row is empty and X is never read
+            to_interleaved_kernel<<<dim3((unsigned)((ns + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0,
+                                    ctx->stream>>>(ns, nf, X, ldx, xs);
+            RBF_CHECK_LAUNCH(ctx);
+        }
+        if (beta != 0.0) {
+            to_interleaved_kernel<<<dim3((unsigned)((ne + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
+                ne, nf, Y, ldy, ys);
+            RBF_CHECK_LAUNCH(ctx);
+        }
+        for (int f0 = 0; f0 < nf; f0 += 32) {
+            int nfc = std::min(32, nf - f0), nfp = 1;
+            while (nfp < nfc) nfp <<= 1;
+            int64_t warps = (ne + (32 / nfp) - 1) / (32 / nfp);
+            spmm_interleaved_kernel<<<blocks_for(ctx, warps * 32, 256, 16), 256, 0, ctx->stream>>>(
+                ne, row_ptr, col, val, nfc, nfp, xs + f0, nf, alpha, beta, ys + f0, nf);
+            RBF_CHECK_LAUNCH(ctx);
+        }
+        from_interleaved_kernel<<<dim3((unsigned)((ne + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
+            ne, nf, ys, Y, ldy);
+        RBF_CHECK_LAUNCH(ctx);
+    }
     return RBF_OK;
 }
 }  // namespace
@@ -410,44 +465,22 @@ extern "C" int rbf_spmm_noalloc(rbf_ctx *ctx, int64_t ne, int64_t ns, const int6
         !rbf_is_device_ptr(Y))
         return rbf_fail(ctx, RBF_ERR_ARGUMENT, "no-alloc apply: every array must be a device pointer");
     if (ne == 0) return RBF_OK;
-    if (!staged) {
-        if (nf == 1) {
-            RBF_TRY(spmv_launch(ctx, ne, row_ptr, col, val, X, alpha, beta, Y));
-        } else {
-            for (int f0 = 0; f0 < nf; f0 += 32) {
-                int nfc = std::min(32, nf - f0), nfp = 1;
-                while (nfp < nfc) nfp <<= 1;
-                int64_t warps = (ne + (32 / nfp) - 1) / (32 / nfp);
-                spmm_interleaved_kernel<<<blocks_for(ctx, warps * 32, 256, 16), 256, 0, ctx->stream>>>(
-                    ne, row_ptr, col, val, nfc, nfp, X + f0, ldx, alpha, beta, Y + f0, ldy);
-                RBF_CHECK_LAUNCH(ctx);
-            }
-        }
-    } else {
-        double *scratch = nullptr;
-        RBF_TRY(noalloc_scratch(ctx, &scratch));
-        double *xs = scratch, *ys = scratch + (size_t)nf * ns;
-        dim3 tb(32, 8);
-        to_interleaved_kernel<<<dim3((unsigned)((ns + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
-            ns, nf, X, ldx, xs);
-        RBF_CHECK_LAUNCH(ctx);
-        if (beta != 0.0) {
-            to_interleaved_kernel<<<dim3((unsigned)((ne + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
-                ne, nf, Y, ldy, ys);
-            RBF_CHECK_LAUNCH(ctx);
-        }
-        for (int f0 = 0; f0 < nf; f0 += 32) {
-            int nfc = std::min(32, nf - f0), nfp = 1;
-            while (nfp < nfc) nfp <<= 1;
-            int64_t warps = (ne + (32 / nfp) - 1) / (32 / nfp);
-            spmm_interleaved_kernel<<<blocks_for(ctx, warps * 32, 256, 16), 256, 0, ctx->stream>>>(
-                ne, row_ptr, col, val, nfc, nfp, xs + f0, nf, alpha, beta, ys + f0, nf);
-            RBF_CHECK_LAUNCH(ctx);
-        }
-        from_interleaved_kernel<<<dim3((unsigned)((ne + 31) / 32), (unsigned)((nf + 31) / 32)), tb, 0, ctx->stream>>>(
-            ne, nf, ys, Y, ldy);
-        RBF_CHECK_LAUNCH(ctx);
+    // with timing on, CUDA events bracket the device work (as in rbf_spmm)
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (ctx->timing) {
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, ctx->stream);
     }
+    const int st = noalloc_apply(ctx, ne, ns, row_ptr, col, val, nf, layout, X, ldx, alpha, beta, Y, ldy);
+    if (ctx->timing) {
+        cudaEventRecord(t1, ctx->stream);
+        cudaEventSynchronize(t1);
+        cudaEventElapsedTime(&ctx->last_ms, t0, t1);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
+    RBF_TRY(st);
     RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return RBF_OK;
 }

@@ -92,3 +92,30 @@ def test_directional_constant_and_per_point(pkg, cloud):
     assert np.abs(got - nrm @ np.array([2.0, 3.0, -1.0])).max() < 1e-9
     with pytest.raises(ValueError):
         pkg.directional(X, np.ones(5), k=30, adjl=J.adjl)
+
+
+def test_axpby_power_of_two_scalings_exact(pkg):
+    """Scalings by +-1 and other powers of two move the exponent on the integer pipe; the
+    results must equal the rounded products and sums bit for bit, also where the product
+    leaves the normal range (zeros, subnormals, overflow to infinity) or the input is not
+    finite."""
+    ctx = pkg.Context.default(0)
+    rng = np.random.default_rng(5)
+    special = np.array([0.0, -0.0, 5e-324, -2.5e-310, 2.2250738585072014e-308, 1e308, -1.7e308, np.inf, -np.inf,
+                        1.0, -3.0, 0.1])
+    a = np.concatenate([special, rng.standard_normal(4000) * 10.0 ** rng.integers(-300, 300, 4000)])
+    b = np.concatenate([special[::-1], rng.standard_normal(4000)])
+    ad, bd = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    out = torch.empty_like(ad)
+    for alpha, beta in [(1.0, 2.0), (-1.0, 1.0), (0.5, -0.25), (2.0 ** 600, 1.0), (3.0, -1.0), (1.0, 0.3),
+                        (-0.7, 1.1)]:
+        for with_b in (True, False):
+            st = ctx.lib.rbf_weights_axpby(ctx.h, len(a), alpha, pkg._ptr(ad), beta,
+                                           pkg._ptr(bd) if with_b else None, pkg._ptr(out))
+            assert st == 0
+            torch.cuda.synchronize()
+            with np.errstate(over="ignore", invalid="ignore"):
+                ref = alpha * a + beta * b if with_b else alpha * a
+            got = out.cpu().numpy()
+            same = (got.view(np.int64) == ref.view(np.int64)) | (np.isnan(got) & np.isnan(ref))
+            assert same.all(), (alpha, beta, with_b, a[~same][:4], got[~same][:4], ref[~same][:4])

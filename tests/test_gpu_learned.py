@@ -163,3 +163,31 @@ def test_predict_tensor_cores(pkg):
     p_tc = model.predict(Xb)
     p_ms = model.predict(Xb, tensor_cores=False)
     assert float((p_tc - p_ms).abs().max() / p_ms.abs().max()) < 2e-2
+
+
+def test_tc_gemm_wait_timeout_is_reported(pkg):
+    """The tensor-core GEMM's waits are bounded: a launch whose producer issues no copy (the
+    library's self-test, nothing in flight) gives up after a short wait limit, returns, and
+    leaves the error flag that rbf_mlp_tc_status reports; the next GEMM on the same context
+    runs normally and reports no failure."""
+    import ctypes
+    ctx = pkg.Context.default(0)
+    failed = ctypes.c_int32(-1)
+    assert ctx.lib.rbf_mlp_tc_selftest_timeout(ctx.h, ctypes.byref(failed)) == 0, ctx.lib.rbf_last_error(ctx.handle)
+    assert failed.value == 1
+    ok = ctypes.c_int32(-1)
+    assert ctx.lib.rbf_mlp_tc_status(ctx.h, ctypes.byref(ok)) == 0
+    assert ok.value == 0  # the self-test cleared what it set
+    L = pkg.learned
+    model = L.StencilMLP(k=30, dim=3, hidden=(64,), seed=0)
+    rng = np.random.default_rng(2)
+    M, N, K = 640, 64, 64
+    A = torch.from_numpy(rng.integers(-4, 5, (M, K)).astype(np.float32)).cuda().to(torch.bfloat16)
+    B = torch.from_numpy(rng.integers(-4, 5, (N, K)).astype(np.float32)).cuda().to(torch.bfloat16)
+    C0 = torch.empty((M, N), dtype=torch.float32, device="cuda")
+    C1 = torch.empty_like(C0)
+    model._gemm(A, B, M, N, K, Cf=C0)
+    model._gemm_tc(A, B, M, N, K, Cf=C1)
+    assert ctx.lib.rbf_mlp_tc_status(ctx.h, ctypes.byref(ok)) == 0
+    assert ok.value == 0
+    assert torch.equal(C0, C1)

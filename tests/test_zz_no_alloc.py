@@ -81,3 +81,52 @@ def test_noalloc_rejects_oversize_and_host_pointers(setup):
     st = L.rbf_spmm_noalloc(W.ctx.handle, ne, ns, _p(W.row_ptr), _p(W.col), _p(W.val), 2, 0,
                             xh.ctypes.data_as(ctypes.c_void_p), ns, 1.0, 0.0, yh.ctypes.data_as(ctypes.c_void_p), ne)
     assert st == -1 and b"device pointer" in L.rbf_last_error(W.ctx.handle)
+
+
+def test_noalloc_many_fields_and_interleaved(setup):
+    """Past 32 fields the staged apply runs in chunks of 32 over the scratch; the interleaved
+    layout needs no staging but takes the same chunked kernel loop.  Both against rbf_spmm,
+    two calls in a row each."""
+    pkg, W = setup
+    L = W.ctx.lib
+    ne, ns = W.shape
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    for call in range(2):
+        nf = 40
+        Xcm = torch.randn((nf, ns), generator=gen, dtype=torch.float64, device="cuda")
+        Y0 = torch.randn((nf, ne), generator=gen, dtype=torch.float64, device="cuda")
+        Yref, Ynoa = Y0.clone(), Y0.clone()
+        beta = 0.0 if call == 0 else 0.5
+        assert _apply(pkg, W, L.rbf_spmm, Xcm, Yref, nf, -0.75, beta) == 0
+        assert _apply(pkg, W, L.rbf_spmm_noalloc, Xcm, Ynoa, nf, -0.75, beta) == 0, \
+            L.rbf_last_error(W.ctx.handle).decode()
+        torch.cuda.synchronize()
+        assert float((Ynoa - Yref).abs().max()) <= APPLY_TOL * float(Yref.abs().max())
+        nf = 7  # interleaved: field f of point i at X[i * nf + f]
+        Xil = torch.randn((ns, nf), generator=gen, dtype=torch.float64, device="cuda")
+        Y0 = torch.randn((ne, nf), generator=gen, dtype=torch.float64, device="cuda")
+        Yref, Ynoa = Y0.clone(), Y0.clone()
+        for fn, Yt in ((L.rbf_spmm, Yref), (L.rbf_spmm_noalloc, Ynoa)):
+            st = fn(W.ctx.handle, ne, ns, _p(W.row_ptr), _p(W.col), _p(W.val), nf, 1, _p(Xil), nf, 2.0, beta,
+                    _p(Yt), nf)
+            assert st == 0, L.rbf_last_error(W.ctx.handle).decode()
+        torch.cuda.synchronize()
+        assert float((Ynoa - Yref).abs().max()) <= APPLY_TOL * float(Yref.abs().max())
+
+
+def test_noalloc_operator_without_data_points(setup):
+    """An operator with no data points has only empty rows: Y = beta * Y, and the staged
+    path must not launch its copy of X (zero blocks)."""
+    pkg, W = setup
+    L = W.ctx.lib
+    ne, nf = 5, 3
+    rp = torch.zeros(ne + 1, dtype=torch.int64, device="cuda")
+    col = torch.zeros(1, dtype=torch.int32, device="cuda")
+    val = torch.zeros(1, dtype=torch.float64, device="cuda")
+    x = torch.zeros(1, dtype=torch.float64, device="cuda")
+    Y = torch.arange(nf * ne, dtype=torch.float64, device="cuda").reshape(nf, ne)
+    Y0 = Y.clone()
+    st = L.rbf_spmm_noalloc(W.ctx.handle, ne, 0, _p(rp), _p(col), _p(val), nf, 0, _p(x), 0, 1.0, 0.5, _p(Y), ne)
+    assert st == 0, L.rbf_last_error(W.ctx.handle).decode()
+    torch.cuda.synchronize()
+    assert torch.equal(Y, 0.5 * Y0)
