@@ -53,9 +53,11 @@ CONFIGS = {
 PEAKS = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
     os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
 
-# DRAM bytes (read + write) per stencil of the headline build kernel, from one ncu capture of
-# that kernel at N = 1,000,000 (3D Laplacian, k = 30); traffic grows with the stencil count.
-KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": 481.4, "learned": 611.9}
+# DRAM bytes (read + write) per stencil of the headline build kernel: constants from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on a 1,000,000-point
+# case of this workload (`python bench.py --case build_learned --n 1000000` under ncu), scaled by
+# the stencil count (the kernel's traffic grows in proportion).  None: not captured.
+KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": None, "learned": None}
 
 
 def peaks_bf16():
@@ -81,10 +83,91 @@ def parse():
     p.add_argument("--no-learned", action="store_true", help="headline without the learned seed")
     p.add_argument("--reorder", action="store_true",
                    help="with --profile-once: put the cloud in Morton order first (reorder_points)")
+    p.add_argument("--case", default=None, choices=sorted(CASES),
+                   help="run one kernel on a small case of the workload (--n points, 1,000,000 by default), "
+                        "once to warm up and --reps more times, and exit: the command to capture under ncu")
+    p.add_argument("--reps", type=int, default=2)
     p.add_argument("--profile-once", action="store_true",
                    help="run each hot kernel once (kNN, FP64 build, FP32-refined build, apply) and exit "
                         "(a short command to capture under ncu)")
     return p.parse_args()
+
+
+CASES = {
+    "knn": "rbf_knn on the cloud (knn_fast_kernel)",
+    "build_fp64": "plain FP64 weight build (build_fp64_kernel)",
+    "build_refined": "FP32-factorised FP64-refined build (build_refined_split_kernel<40> + build_deferred_kernel)",
+    "build_learned": "learned + refined build (features, tcgen05 inference, seeded split-row kernel)",
+    "features": "surrogate inputs (features_kernel)",
+    "mlp_infer": "surrogate inference, four tcgen05 GEMMs (gemm_tc_persistent_kernel)",
+    "mlp_train": "surrogate training steps, batch 4096 (gemm_bf16_kernel and the Adam / loss kernels)",
+    "spmv_sell": "single-field apply of the built operator, sliced-ELL copy (spmv_sell_kernel)",
+    "spmv_csr": "single-field apply of the built operator, CSR (spmv_pair_kernel)",
+    "spmm16": "16-field apply of the built operator, column-major fields (spmm_interleaved_kernel)",
+}
+
+
+def run_case(args, pkg, ctx, torch, dev):
+    """One kernel of the headline workload on a small cloud: set-up, one warm-up call, then
+    args.reps calls of the kernel named by args.case (for ncu -k ... -s ... -c ...)."""
+    cfg = CONFIGS[args.config]
+    n = args.n or 1_000_000
+    X_h = make_points(cfg, n, 1000)
+    if args.reorder:
+        X_h = X_h[np.lexsort(np.floor(X_h * 64).T[::-1])]  # cell-sorted points (locality)
+    Xd = torch.from_numpy(X_h).to(dev)
+    k = cfg["k"]
+    basis = pkg.PHS(cfg["phs"], poly_deg=cfg["deg"])
+    case = args.case
+    from importlib import import_module
+    L = import_module(pkg.__name__ + ".learned")
+    adjl = pkg.find_neighbors(Xd, k=k, ctx=ctx) if case != "knn" else None
+    model = None
+    if case == "build_learned":  # a trained surrogate: its seed decides the refinement's path
+        Xb, T = L.training_set(100_000, 100_000, k, cfg["dim"], basis, cfg["ops"], seed=5000, ctx=ctx)
+        model, _ = L.train_surrogate(Xb, T, k, cfg["dim"], epochs=3, batch=4096, ctx=ctx)
+    elif case in ("features", "mlp_infer", "mlp_train"):  # the kernels' work does not depend on the weights
+        model = L.StencilMLP(k, cfg["dim"], ctx=ctx, seed=0)
+    W = None
+    if case.startswith("spm"):
+        W = pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision="fp32_refined", ctx=ctx,
+                              sell=case == "spmv_sell")[-1]
+        if case == "spmv_csr":
+            W.sell = None
+    f = torch.from_numpy(np.sin(4 * X_h[:, 0]) * np.cos(3 * X_h[:, 1])).to(dev)
+    F16 = torch.randn((16, n), dtype=torch.float64, device=dev) if case == "spmm16" else None
+    feats = model.features(Xd, None, adjl) if case == "mlp_infer" else None
+    if case == "mlp_train":
+        Xt = model.features(Xd, None, adjl[:4096])
+        Tt = torch.zeros((4096, model.dims[-1]), dtype=torch.float32, device=dev)
+        Tt[:, :k] = torch.randn((4096, k), dtype=torch.float32, device=dev)
+    st = pkg._native.BuildStats()
+    fns = {
+        "knn": lambda: pkg.find_neighbors(Xd, k=k, ctx=ctx),
+        "build_fp64": lambda: pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision="fp64", ctx=ctx, stats=st),
+        "build_refined": lambda: pkg.build_weights(cfg["ops"], Xd, None, adjl, basis, precision="fp32_refined",
+                                                   ctx=ctx, stats=st),
+        "build_learned": lambda: L.build_learned(model, cfg["ops"], Xd, adjl, basis, ctx=ctx, stats=st),
+        "features": lambda: model.features(Xd, None, adjl),
+        "mlp_infer": lambda: model.predict(feats),
+        "mlp_train": lambda: model.train_step(Xt, Tt, lr=1e-3),
+        "spmv_sell": lambda: W.apply(f),
+        "spmv_csr": lambda: W.apply(f),
+        "spmm16": lambda: W.apply(F16.T),
+    }
+    fn = fns[case]
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream()
+    e0.record(stream)
+    for _ in range(args.reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": case, "what": CASES[case], "n": n, "reps": args.reps,
+                      "ms_per_call": e0.elapsed_time(e1) / args.reps, "ms_build": float(st.ms_build),
+                      "note": "a development timing, not a bench value"}), flush=True)
 
 
 def make_points(cfg, n, seed, torch=None, device=None):
@@ -156,18 +239,48 @@ def row_rel_err_torch(torch, row_ptr, k, v, vref):
     return float((d / s).max())
 
 
-def cpu_baseline(cfg, n, sample, steps=1):
-    """The oracle (C restatement of the reference algorithm) on host cores, bounded sample."""
+def cpu_baseline(cfg, n, sample, X=None, seed=1000):
+    """The oracle (C restatement of the reference algorithm) on host cores, bounded sample: the
+    grid kNN of the first `sample` points over the whole cloud and their weights.  X: the
+    cloud the GPU builds (the same seeded cloud is made here otherwise).  Returns the timing
+    and the oracle's CSR of those rows."""
     from oracle import oracle as O
-    X = make_points(cfg, n, 12345)
+    if X is None:
+        X = make_points(cfg, n, seed)
     q = X[:sample]
     t0 = time.perf_counter()
     adjl = O.knn(X, q, cfg["k"])
     t1 = time.perf_counter()
-    O.build(X, q, adjl, cfg["dim"], cfg["phs"], cfg["deg"], cfg["ops"])
+    ref = O.build(X, q, adjl, cfg["dim"], cfg["phs"], cfg["deg"], cfg["ops"])
     t2 = time.perf_counter()
     return {"stencils_per_s": sample / (t2 - t0), "knn_s": t1 - t0, "build_s": t2 - t1,
-            "cores": O.num_threads(), "sample": sample}
+            "cores": O.num_threads(), "sample": sample, "ref": ref, "adjl": adjl}
+
+
+def oracle_errors(torch, W, ref, f, op_index=0):
+    """A GPU operator's first rows against the oracle's weights of the same stencils: max and RMS
+    of the row-relative weight difference (row max-norm), and the relative max difference of
+    the operator applied to the test function f (numpy, all data points)."""
+    from oracle import oracle as O
+    ne = len(ref.row_ptr) - 1
+    m = int(ref.row_ptr[-1])
+    rp = W.row_ptr[: ne + 1].cpu().numpy()
+    if not np.array_equal(rp, ref.row_ptr) or not np.array_equal(W.col[:m].cpu().numpy(), ref.col):
+        return {"structure_equal": False}
+    v = W.val[:m].cpu().numpy()
+    vr = ref.val[op_index]
+    rows = np.repeat(np.arange(ne), np.diff(ref.row_ptr))
+    num, den = np.zeros(ne), np.zeros(ne)
+    np.maximum.at(num, rows, np.abs(v - vr))
+    np.maximum.at(den, rows, np.abs(vr))
+    ok = den > 0
+    rel = num[ok] / den[ok]
+    y = np.zeros(ne)
+    np.add.at(y, rows, v * f[ref.col])
+    yr = O.spmm(ref, f, op_index)
+    return {"structure_equal": True, "max_row_rel_weight_err": float(rel.max()),
+            "rms_row_rel_weight_err": float(np.sqrt((rel ** 2).mean())),
+            "operator_on_test_function_rel_err": float(np.abs(y - yr).max() / np.abs(yr).max())}
 
 
 def max_over_ranks(ms, world, device=None):
@@ -443,8 +556,9 @@ def run_reference(args, cfg, n):
     sample = args.cpu_sample or (200_000 if cfg["n"] >= 1_000_000 else n)
     times = []
     res = None
+    X = make_points(cfg, n, 1000)  # the cloud rank 0 of the GPU arm builds
     for s in range(args.warmup + args.steps):
-        res = cpu_baseline(cfg, n, sample)
+        res = cpu_baseline(cfg, n, sample, X=X)
         if s >= args.warmup:
             times.append(sample / res["stencils_per_s"])
     v = sample * len(times) / sum(times)
@@ -455,7 +569,10 @@ def run_reference(args, cfg, n):
         "data": "synthetic (seeded)",
         "config": {"workload": cfg["desc"], "sample_stencils": sample},
         "cpu_baseline": {"value": v, "unit": "stencils/s", "cores": res["cores"], "kind": "port",
-                         "sample": f"{sample} stencils (kNN over all {n} points + build) per step"},
+                         "sample": f"the first {sample} stencils of the same seeded {n}-point cloud (kNN over "
+                                   "all points + build) per step; value = their rate, the full cloud's time "
+                                   "extrapolated from it"},
+        "extrapolated_full_step_s": n / v,
         "e2e": {"value": v, "unit": "stencils/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference Julia path: unavailable on this box (no Julia); CPU oracle timed instead",
     }
@@ -487,6 +604,9 @@ def main():
     dev = torch.device("cuda", local)
     if args.all_configs:
         all_configs(pkg, torch, ctx, stream)
+        return
+    if args.case:
+        run_case(args, pkg, ctx, torch, dev)
         return
 
     # independent seeded cloud per rank (weak scaling: per-GPU work fixed)
@@ -596,7 +716,15 @@ def main():
     ms_fp64 = timed(lambda: step("fp64"), max(1, args.steps // 2), 1)
     ms_fp32r = timed(lambda: step("fp32_refined"), max(1, args.steps // 2), 1) if learned_on else ms
 
-    # ---- equal-error check against the plain GPU build (max row-relative weight difference)
+    # ---- the CPU baseline (untimed for the GPU numbers): the oracle on the first stencils of
+    # this cloud; its weights are the reference for the equal-error check below
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sample = args.cpu_sample or (200_000 if n >= 1_000_000 else n)
+        cb = cpu_baseline(cfg, n, sample, X=X_h)
+
+    # ---- equal-error check: every GPU build against the oracle's weights of the sampled
+    # stencils, and over all stencils against the plain GPU build
     adjl = pkg.find_neighbors(Xd, k=k, ctx=ctx)
     st64 = pkg._native.BuildStats()
     W64 = build("fp64", Xd, adjl, st64)
@@ -609,12 +737,21 @@ def main():
     op_err = float((yh - y64).abs().max() / y64.abs().max())
     st32 = st_h
     err32 = err
+    W32 = W_h
     if learned_on:
         st32 = pkg._native.BuildStats()
         W32 = build("fp32_refined", Xd, adjl, st32)
         err32 = max(row_rel_err_torch(torch, a.row_ptr, k, a.val, b.val) for a, b in zip(W32, W64))
-        del W32
-    del W64, W_h
+    vs_oracle = None
+    if cb is not None:
+        ops_last = len(cfg["ops"]) - 1
+        vs_oracle = {"sample_stencils": cb["sample"],
+                     "neighbour_lists_equal": bool(np.array_equal(adjl[: cb["sample"]].cpu().numpy(), cb["adjl"])),
+                     headline: oracle_errors(torch, W_h[-1], cb["ref"], f_h, ops_last),
+                     "fp64": oracle_errors(torch, W64[-1], cb["ref"], f_h, ops_last)}
+        if learned_on:
+            vs_oracle["fp32_refined"] = oracle_errors(torch, W32[-1], cb["ref"], f_h, ops_last)
+    del W64, W_h, W32
     # ---- per-stage timings (device-resident, events on the launching stream)
     ms_b_h = timed(lambda: build(headline, Xd, adjl), 3, 1)
     ms_b_32 = timed(lambda: build("fp32_refined", Xd, adjl), 3, 1) if learned_on else ms_b_h
@@ -653,6 +790,7 @@ def main():
     ms_spmv_csr = kernel_ms(lambda: W.apply(fd))  # the CSR apply of the same operator
     W.sell = W_sell
     ms_knn_kernel = kernel_ms(lambda: pkg.find_neighbors(Xd, k=k, ctx=ctx), 3)
+    knn_bytes = 2 * n * cfg["dim"] * 8 + n * k * 4
     nnz = W.nnz
     sell_nnz = int(W.sell.col.shape[0])
     # algorithmic bytes of one apply: val (8 B) + col (4 B) per entry, the row offsets (8 B
@@ -688,16 +826,22 @@ def main():
     ach = flops_stencil * n / (ms_kernel * 1e-3) / 1e12
     kbase = f"build_refined_split_kernel<{nsys}>" if (33 <= nsys <= 40 and R == 1) else f"build_refined_reg_kernel<{nsys},{R}>"
     kname = kbase + (" (learned seed)" if learned_on else "")
+    tps = KERNEL_TRAFFIC_PER_STENCIL.get(headline)
+    # the FP64 work the refined kernel itself does: its FP64 residuals (n^2 R FMAs each, counted
+    # by the build), at the FP64 FMA rate measured in this run
+    res_fma = float(st_h.n_residuals) * nsys * nsys * R
     roof = {"kernel": kname, "bound": "fp64 pipe", "achieved": ach, "peak": fp64_peak.value, "unit": "TFLOP/s",
-            "frac": ach / fp64_peak.value, "traffic": KERNEL_TRAFFIC_PER_STENCIL.get(headline, 0) * n or None,
+            "frac": ach / fp64_peak.value, "traffic": tps * n if tps else None,
             "flops": f"reference FP64 algorithm count per stencil ({flops_stencil:.0f}: n^3/3 + 2n^2R + assembly)",
             "peak_source": "FP64 FMA loop measured in this run (rbf_diag_fma_peak)",
             "fp32_pipe": {"peak": fp32_peak.value, "frac": ach / fp32_peak.value},
-            "traffic_source": "ncu dram__bytes_read+write of the same kernel at N=1M, scaled by stencils",
-            "note": "frac counts the reference's FP64 algorithm at the FP64 peak; the kernel does most of it "
-                    "on the FP32 pipe, so the pipes it actually uses are below (ncu, N = 1M)",
-            "pipes_measured": {"fp64": 0.439, "fma_fp32": 0.162, "alu": 0.308, "issue_active": 0.457,
-                               "source": "profiles/build_refined_split_40_lap3d_1M.md"}}
+            "traffic_source": "ncu dram__bytes_read+write of the same kernel on a 1M-point case, scaled by stencils"
+                              if tps else "not captured",
+            "note": "frac: the reference's FP64 algorithm at the FP64 peak, i.e. the speed of light of a plain FP64 "
+                    "build; the kernel factorises on the FP32 pipe and is latency-bound",
+            "fp64_residual_work": {"fma_per_s": res_fma / (ms_kernel * 1e-3),
+                                   "frac_of_fp64_fma_rate": res_fma / (ms_kernel * 1e-3) / (fp64_peak.value * 0.5e12),
+                                   "count": "FP64 residuals counted by the build x n^2 R FMAs"}}
 
     # ---- the adjoint of the build: gradients of <dW, W> with respect to the points (the
     # pullback of _build_weights), for a random cotangent of the headline operator
@@ -778,11 +922,10 @@ def main():
         interp = interp_bench(pkg, torch, stream, args.interp_n, world == 1 and not args.no_cpu_baseline)
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sample = args.cpu_sample or (200_000 if n >= 1_000_000 else n)
-        cb = cpu_baseline(cfg, n, sample)
+    if cb is not None:
         cpu = {"value": cb["stencils_per_s"], "unit": "stencils/s", "cores": cb["cores"], "kind": "port",
-               "sample": f"{sample} stencils: grid kNN over all {n} points + raw-coordinate rook-BK build"}
+               "sample": f"the first {cb['sample']} stencils of the same cloud: grid kNN over all {n} points + "
+                         "raw-coordinate rook-BK build (rate extrapolated to the full cloud)"}
 
     if rank == 0:
         res = lambda s: float(s.n_residuals) / max(1, int(s.n_stencils))
@@ -807,10 +950,11 @@ def main():
                            "fp64_stencils_per_s": n / (ms_b_64 * 1e-3),
                            "kernel_ms": {"headline": ms_kernel, "fp32_refined": float(st32.ms_build),
                                          "fp64": float(st64.ms_build)}},
-            "equal_error": {"max_row_rel_weight_diff_vs_fp64": err, "rms_rel_weight_diff": rms,
-                            "operator_on_test_function_rel_diff": op_err, "bar": 1e-8,
-                            "fallback_stencils": int(st_h.n_fallback),
-                            "fp32_refined_unseeded_max_diff": err32},
+            "equal_error": {"vs_oracle": vs_oracle, "bar": 1e-8,
+                            "vs_gpu_fp64_all_stencils": {"max_row_rel_weight_diff": err, "rms_rel_weight_diff": rms,
+                                                         "operator_on_test_function_rel_diff": op_err,
+                                                         "fp32_refined_unseeded_max_diff": err32},
+                            "fallback_stencils": int(st_h.n_fallback)},
             "refinement": {"residuals_per_stencil": res(st_h), "unseeded_residuals_per_stencil": res(st32),
                            "fallback_unseeded": int(st32.n_fallback),
                            "seed_rel_err_mean_judged_by_solve": float(st_h.seed_rel_err_mean) if learned_on else None},
@@ -825,6 +969,13 @@ def main():
             "adjoint": adjoint,
             "algebra": algebra,
             "interpolator": interp,
+            "knn": {"kernel": "knn_fast_kernel (grid buckets, FP32 keys, exact FP64 re-sort)", "ms": ms_knn_kernel,
+                    "queries_per_s": n / (ms_knn_kernel * 1e-3),
+                    "bytes": "(ns + ne) dim 8 + ne k 4 (points read, neighbour lists written)",
+                    "GB_s": knn_bytes / (ms_knn_kernel * 1e-3) / 1e9,
+                    "frac_of_hbm": knn_bytes / (ms_knn_kernel * 1e-3) / 1e9 / hbm_peak,
+                    "bound": "not HBM: candidate selection (distance keys and the sorted k+8 list) on the "
+                             "SM pipes; the HBM fraction shows how far it is from the traffic bound"},
             "kernels_ms": {"knn": ms_knn_kernel, "knn_per_call_api": ms_knn, "build_headline": ms_kernel,
                            "build_fp64": float(st64.ms_build), "spmv": ms_spmv},
             "peaks": {"fp64_tflops_measured": fp64_peak.value, "fp32_tflops_measured": fp32_peak.value,
