@@ -89,6 +89,9 @@ typedef struct rbf_build_cfg {
 #define RBF_FLAG_STENCIL_ORDER 1  /* write each row in stencil (adjl) order, not column order */
 #define RBF_FLAG_LOCAL_UNITS 2    /* weights in the stencil's local units: w * s^q, s the power of
                                      two above the stencil radius, q the operator order */
+#define RBF_FLAG_FP64_LU 4        /* RBF_PREC_FP64 in rbf_build: solve by LU with partial pivoting
+                                     (the batched build's solver, bit-identical to it) instead of
+                                     the default symmetric indefinite (Bunch-Kaufman) LDL^T */
 
 /* Hermite boundary description (src/solve/types.jl:18-42,178-182).  Boundary
  * conditions are B u = alpha*u + beta*du/dn; Dirichlet is (1,0), Neumann (0,1).

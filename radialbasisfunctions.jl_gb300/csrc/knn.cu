@@ -37,9 +37,33 @@ struct GridDesc {
     double lo[3];
     double h[3];
     double inv_h[3];
+    float lof[3], hf[3], inv_hf[3];  // FP32 copies (rounded on the host) for the FP32 search
     int nc[3];
     int64_t ncells;
 };
+
+// Round-to-nearest-even double -> float on the integer pipe (on GB300 the conversion
+// instruction runs on the FP64 pipe); values outside the FP32 normal range take it anyway.
+__device__ __forceinline__ float d2f_rn_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+    if (e <= 0 || e >= 255) return (float)x;
+    const unsigned long long m = b & 0xfffffffffffffull;
+    const unsigned long long rem = m & 0x1fffffffull, half = 1ull << 28;
+    unsigned r = ((unsigned)e << 23) | (unsigned)(m >> 29);
+    if (rem > half || (rem == half && (r & 1u))) r += 1u;  // a carry into the exponent is the right result
+    return __uint_as_float(((unsigned)(b >> 32) & 0x80000000u) | r);
+}
+
+// A non-negative double rounded up to a float, on the integer pipe (as __double2float_ru).
+__device__ __forceinline__ float d2f_ru_nonneg_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+    if (e <= 0 || e >= 255) return __double2float_ru(x);
+    unsigned r = ((unsigned)e << 23) | (unsigned)((b & 0xfffffffffffffull) >> 29);
+    if (b & 0x1fffffffull) r += 1u;
+    return __uint_as_float(r);
+}
 
 __device__ __forceinline__ double sqdist(const double *a, const double *b, int dim) {
     double t = __dsub_rn(a[0], b[0]);
@@ -408,19 +432,23 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
 #pragma unroll
         for (int d = 0; d < DIM; d++) {
             qp[d] = q[(int64_t)qi * DIM + d];
-            qf[d] = (float)qp[d];
+            qf[d] = d2f_rn_bits(qp[d]);
             qmag = fmaxf(qmag, fabsf(qf[d]));
         }
         const float errc = u8 * qmag * 1.0001f;
+        // the search starts in the query's cell, found in FP32: it only centres the search
+        // (the covered ball below is measured from the FP32 face positions with slack), so a
+        // neighbouring cell at a face changes nothing in the result
         int qc[3] = {0, 0, 0};
-        cell_of<DIM>(g, qp, qc);
         float lof[3], hf[3];
         float gmag = qmag;
 #pragma unroll
         for (int d = 0; d < DIM; d++) {
-            lof[d] = (float)g.lo[d];
-            hf[d] = (float)g.h[d];
+            lof[d] = g.lof[d];
+            hf[d] = g.hf[d];
             gmag = fmaxf(gmag, fabsf(lof[d]) + hf[d] * (float)g.nc[d]);
+            const float f = floorf((qf[d] - lof[d]) * g.inv_hf[d]);
+            qc[d] = !(f >= 0.0f) ? 0 : (f >= (float)(g.nc[d] - 1) ? g.nc[d] - 1 : (int)f);
         }
         const float slackf = 16.0f * 5.9604645e-08f * gmag + 1e-30f;
 
@@ -750,7 +778,7 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
             kk = __shfl_sync(0xffffffffu, kk, (k - 1) & 31);
             // exact k-th squared distance rounded up vs the squared lower bound of any unlisted
             // point's distance rounded down (no FP64 square roots)
-            const float dk2_up = __double2float_ru(__longlong_as_double((long long)kk));
+            const float dk2_up = d2f_ru_nonneg_bits(__longlong_as_double((long long)kk));
             const float dt = sqrtf(kth);
             const float floor_unlisted = dt - (errc + u8 * dt) * 1.0001f;
             certified = (kth < INFINITY) && (floor_unlisted > 0.0f) &&
@@ -842,6 +870,11 @@ int knn_dim(rbf_ctx *ctx, const double *d_data, int64_t ns, const double *d_eval
         }
     }
     g.ncells = ncells;
+    for (int d = 0; d < 3; d++) {
+        g.lof[d] = (float)g.lo[d];
+        g.hf[d] = (float)g.h[d];
+        g.inv_hf[d] = (float)g.inv_h[d];
+    }
 
     DevBuf cell, count, start, fill, sp, sp32, sidx, qcell, qcount, qstart, qfill, qorder, fb;
     RBF_TRY(cell.alloc(ctx, sizeof(int32_t) * ns));

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "stencil_bk.cuh"
 #include "stencil_solve.cuh"
 
 #define RBF_LAUNCH_NO_VARIANT 1000
@@ -36,6 +37,16 @@ __global__ void build_fp64_kernel(StencilParams P, int wpb, size_t warp_bytes) {
     WarpSmem w = carve(smem + wib * warp_bytes, P.n, P.k, P.nops);
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
     for (int64_t e = (int64_t)blockIdx.x * wpb + wib; e < P.ne; e += nwarps) solve_fp64_warp(P, e, w, lane);
+}
+
+// The default plain FP64 build: symmetric indefinite factorisation of the packed system
+// (stencil_bk.cuh), one warp per stencil.
+__global__ void build_fp64_bk_kernel(StencilParams P, int wpb, size_t warp_bytes) {
+    extern __shared__ __align__(16) char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const BKSmem s = carve_bk(smem + wib * warp_bytes, P.n, P.k, P.nops);
+    const int64_t nwarps = (int64_t)gridDim.x * wpb;
+    for (int64_t e = (int64_t)blockIdx.x * wpb + wib; e < P.ne; e += nwarps) solve_fp64_bk_warp(P, e, s, lane);
 }
 
 __global__ void build_fp32r_kernel(StencilParams P, int wpb, size_t warp_bytes) {
@@ -82,6 +93,20 @@ size_t rbf_fp64_warp_smem(int n, int k, int nops) { return (warp_smem_bytes(n, k
 
 int rbf_build_fp64_launch(rbf_ctx *ctx, const StencilParams &P) {
     if (P.ne == 0) return RBF_OK;
+    if (!(P.flags & RBF_FLAG_FP64_LU)) {
+        const size_t wb = bk_warp_bytes(P.n, P.k, P.nops);
+        const int wpb = 4;
+        const size_t smem = wb * wpb;
+        RBF_CUDA(ctx, cudaFuncSetAttribute(build_fp64_bk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+        int per_sm = 0;
+        RBF_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, build_fp64_bk_kernel, wpb * 32, smem));
+        if (per_sm < 1) per_sm = 1;
+        const int64_t blocks = std::min<int64_t>((P.ne + wpb - 1) / wpb, (int64_t)ctx->num_sms * per_sm);
+        build_fp64_bk_kernel<<<(unsigned)blocks, wpb * 32, smem, ctx->stream>>>(P, wpb, wb);
+        RBF_CHECK_LAUNCH(ctx);
+        return RBF_OK;
+    }
     const size_t wb = rbf_fp64_warp_smem(P.n, P.k, P.nops);
     int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (100 * 1024) / wb));
     size_t smem = wb * wpb;

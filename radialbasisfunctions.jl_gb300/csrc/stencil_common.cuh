@@ -79,9 +79,49 @@ struct BinDesc {
     int precision;          // RBF_PREC_FP64 or RBF_PREC_FP32_REFINED
 };
 
+// x * 2^e exactly, as ldexp gives it: when x and the result are normal numbers the exponent
+// field moves on the integer pipe; zeros, subnormals, infinities, NaNs and results leaving the
+// normal range take ldexp (on GB300 ldexp would otherwise cost several FP64-pipe instructions).
+__device__ __forceinline__ double scale2(double x, int e) {
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    if (ex != 0 && ex != 0x7ff && ex + e > 0 && ex + e < 0x7ff) return __longlong_as_double(b + ((long long)e << 52));
+    return ldexp(x, e);
+}
+
 template <class T> __device__ __forceinline__ T rbf_sqrt(T x);
 template <> __device__ __forceinline__ double rbf_sqrt<double>(double x) { return sqrt(x); }
 template <> __device__ __forceinline__ float rbf_sqrt<float>(float x) { return sqrtf(x); }
+
+// float -> double by rebuilding the bit pattern on the integer pipe (normal floats and
+// zero; subnormal floats, far below any entry scale here, map to zero)
+__device__ __forceinline__ double widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e == 0u) return 0.0;
+    const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
+                                    ((unsigned long long)(e + 896u) << 52) |
+                                    ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+// sqrt(s) by Newton's method (Heron) from the FP32 reciprocal square root of s's leading bits:
+// r0 = s y0 (relative error e ~ 2^-22), then twice r <- r + (s - r^2) y0 / 2; the first step
+// leaves ~1.5 e^2, the second ~e^3, below FP64 rounding.  Five FP64 operations against the
+// library square root's longer sequence; within an ulp or two of the correctly rounded root.
+// s below the FP32 normal range (coincident points) takes the library root.
+__device__ __forceinline__ double sqrt_newton(double s) {
+    const long long b = __double_as_longlong(s);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e <= 1023 - 120 || e >= 1023 + 120) return sqrt(s);
+    const float sf = __uint_as_float(((unsigned)(e - 1023 + 127) << 23) | (unsigned)((b >> 29) & 0x7fffff));
+    float yf;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(sf));
+    const float hf = 0.5f * yf;
+    const double y = widen(yf), h = widen(hf);
+    double r = s * y;
+    r = fma(h, fma(-r, r, s), r);
+    return fma(h, fma(-r, r, s), r);
+}
 
 template <class T> __device__ __forceinline__ T pw3(T r) { return r * r * r; }
 template <class T> __device__ __forceinline__ T pw5(T r) { return r * r * r * r * r; }
@@ -112,10 +152,10 @@ template <class T> struct AvoidInf {
 
 template <class T> __device__ __forceinline__ AvoidInf<T> avoid_inf_scaled(int es) {
     AvoidInf<T> a;
-    a.a1 = (T)ldexp(RBF_AVOID_INF, -es);
-    a.a2 = (T)ldexp(RBF_AVOID_INF, -2 * es);
-    a.a3 = (T)ldexp(RBF_AVOID_INF, -3 * es);
-    a.a5 = (T)ldexp(RBF_AVOID_INF, -5 * es);
+    a.a1 = (T)scale2(RBF_AVOID_INF, -es);
+    a.a2 = (T)scale2(RBF_AVOID_INF, -2 * es);
+    a.a3 = (T)scale2(RBF_AVOID_INF, -3 * es);
+    a.a5 = (T)scale2(RBF_AVOID_INF, -5 * es);
     return a;
 }
 

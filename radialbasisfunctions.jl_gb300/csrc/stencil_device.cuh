@@ -61,14 +61,19 @@ __device__ int load_stencil(const StencilParams &P, int64_t e, const WarpSmem &w
         r2max = fmax(r2max, r2);
         if (P.isb) anyb |= (P.isb[g] != 0);
     }
-    for (int o = 16; o > 0; o >>= 1) r2max = fmax(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
+    // r2max >= 0: its bit pattern orders like its value (an integer max, off the FP64 pipe)
+    {
+        long long m = __double_as_longlong(r2max);
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        r2max = __longlong_as_double(m);
+    }
     anyb = __any_sync(0xffffffffu, anyb);
     int es = 0;
     if (r2max > 0.0) frexp(sqrt(r2max), &es);
     *es_out = es;
     __syncwarp();
     for (int i = lane; i < k; i += 32)
-        for (int d = 0; d < dim; d++) w.X[i * 3 + d] = ldexp(w.X[i * 3 + d], -es);
+        for (int d = 0; d < dim; d++) w.X[i * 3 + d] = scale2(w.X[i * 3 + d], -es);
     int eval_local = -1;
     if (anyb) {
         // Dirichlet eval node: identity row (execution.jl:224-228, 297-303)
@@ -87,7 +92,7 @@ __device__ int load_stencil(const StencilParams &P, int64_t e, const WarpSmem &w
                 return 2;
             }
         }
-        const double sinv = ldexp(1.0, -es);
+        const double sinv = scale2(1.0, -es);
         bool found = false;
         int first = 0x7fffffff;
         for (int i = lane; i < k; i += 32) {
@@ -127,15 +132,78 @@ __device__ int load_stencil(const StencilParams &P, int64_t e, const WarpSmem &w
     return 0;
 }
 
-// Assemble [Phi P; P^T 0 | B] into M (full symmetric storage).
-__device__ void assemble_fp64(const StencilParams &P, const WarpSmem &w, int lane, int es, int eval_local) {
-    const int k = P.k, n = P.n, nops = P.nops, ld = mat_ld(n, nops), dim = P.dim, nmon = P.nmon;
+// Storage policies of the FP64 assembly.  FullStore: M[n][ld] holding both triangles and the
+// right-hand sides in columns n.. (the LU solves).  PackedStore: the lower triangle packed by
+// rows (entry (i, j), i >= j, at i (i + 1) / 2 + j) and the right-hand sides in B[n][nops]
+// (the symmetric indefinite solve).
+struct FullStore {
+    static constexpr bool kPacked = false;
+    double *M;
+    int n, ld;
+    __device__ void zero(int lane) const {
+        for (int t = lane; t < n * ld; t += 32) M[t] = 0.0;
+    }
+    __device__ void sym(int i, int j, double v) const {
+        M[i * ld + j] = v;
+        M[j * ld + i] = v;
+    }
+    __device__ void rhs(int i, int r, double v) const { M[i * ld + n + r] = v; }
+};
+
+__host__ __device__ __forceinline__ int pidx(int i, int j) { return ((i * (i + 1)) >> 1) + j; }  // i >= j
+
+struct PackedStore {
+    static constexpr bool kPacked = true;
+    double *P, *B;
+    int n, k, nops;
+    __device__ void zero(int lane) const {  // the zero block (rows and columns k..n-1)
+        const int m = n - k;
+        for (int t = lane; t < m * m; t += 32) {
+            const int a = t / m, b = t - (t / m) * m;
+            if (b <= a) P[pidx(k + a, k + b)] = 0.0;
+        }
+    }
+    __device__ void sym(int i, int j, double v) const { P[i >= j ? pidx(i, j) : pidx(j, i)] = v; }
+    __device__ void rhs(int i, int r, double v) const { B[i * nops + r] = v; }
+};
+
+// Assemble [Phi P; P^T 0 | B] into the storage S.
+template <class S>
+__device__ void assemble_fp64_into(const StencilParams &P, const WarpSmem &w, int lane, int es, int eval_local,
+                                   const S &st) {
+    const int k = P.k, nops = P.nops, dim = P.dim, nmon = P.nmon;
     const bool herm = eval_local != -2;
     const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
-    for (int t = lane; t < n * ld; t += 32) w.M[t] = 0.0;
+    st.zero(lane);
     __syncwarp();
+    if (S::kPacked && !herm) {
+        // interior stencil, packed storage: phi(0) = 0 on the diagonal, the strict upper
+        // triangle's pairs (i < j) with the Newton square root
+        for (int i = lane; i < k; i += 32) st.sym(i, i, 0.0);
+        const int nstrict = k * (k - 1) / 2;
+        for (int p = lane; p < nstrict; p += 32) {
+            int j = (int)((sqrtf(8.0f * (float)p + 1.0f) + 1.0f) * 0.5f);
+            while (j * (j - 1) / 2 > p) j--;
+            while ((j + 1) * j / 2 <= p) j++;
+            const int i = p - j * (j - 1) / 2;
+            // components held in registers (dimensions past dim contribute nothing)
+            const double d0 = w.X[i * 3] - w.X[j * 3];
+            const double d1 = dim > 1 ? w.X[i * 3 + 1] - w.X[j * 3 + 1] : 0.0;
+            const double d2 = dim > 2 ? w.X[i * 3 + 2] - w.X[j * 3 + 2] : 0.0;
+            const double r2 = dim == 1 ? d0 * d0 : (dim == 2 ? fma(d1, d1, d0 * d0) : fma(d2, d2, fma(d1, d1, d0 * d0)));
+            const double r = sqrt_newton(r2);
+            double v;
+            switch (P.phs) {
+            case 1: v = r; break;
+            case 3: v = r2 * r; break;
+            case 5: v = (r2 * r2) * r; break;
+            default: v = (r2 * r2 * r2) * r; break;
+            }
+            st.sym(i, j, v);
+        }
+    }
     // RBF block, upper triangle pairs (i <= j) mirrored
-    const int npairs = k * (k + 1) / 2;
+    const int npairs = (S::kPacked && !herm) ? 0 : k * (k + 1) / 2;
     for (int p = lane; p < npairs; p += 32) {
         int j = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
         while (j * (j + 1) / 2 > p) j--;
@@ -150,8 +218,7 @@ __device__ void assemble_fp64(const StencilParams &P, const WarpSmem &w, int lan
             v = colloc_entry<double>(P.phs, dim, &w.X[i * 3], &w.X[j * 3], w.ptype[i], w.ptype[j], w.HA[i], w.HB[i],
                                      &w.HN[i * 3], w.HA[j], w.HB[j], &w.HN[j * 3], AI);
         }
-        w.M[i * ld + j] = v;
-        w.M[j * ld + i] = v;
+        st.sym(i, j, v);
     }
     // polynomial block and RBF right-hand sides, one stencil point per lane
     for (int i = lane; i < k; i += 32) {
@@ -165,8 +232,7 @@ __device__ void assemble_fp64(const StencilParams &P, const WarpSmem &w, int lan
                     if (w.HN[i * 3 + d] != 0.0) dn += w.HN[i * 3 + d] * mono_d1<double>(P, m, d, xi);
                 v = w.HA[i] * v + w.HB[i] * dn;
             }
-            w.M[i * ld + k + m] = v;
-            w.M[(k + m) * ld + i] = v;
+            st.sym(i, k + m, v);
         }
         double D[3];
         for (int d = 0; d < dim; d++) D[d] = -xi[d];  // x0 - xi in local coordinates
@@ -175,7 +241,7 @@ __device__ void assemble_fp64(const StencilParams &P, const WarpSmem &w, int lan
             if (nr)
                 b = w.HA[i] * b +
                     w.HB[i] * phs_op_normal<double>(P.phs, P.op_code[r], P.op_dim[r], D, &w.HN[i * 3], dim, AI);
-            w.M[i * ld + n + r] = b;
+            st.rhs(i, r, b);
         }
     }
     // polynomial right-hand sides at the eval point (local origin)
@@ -187,13 +253,18 @@ __device__ void assemble_fp64(const StencilParams &P, const WarpSmem &w, int lan
             double nrm[3] = {w.HN[eval_local * 3], w.HN[eval_local * 3 + 1], w.HN[eval_local * 3 + 2]};
             v = w.HA[eval_local] * mono_op_at_origin(P, m, RBF_OP_IDENTITY, 0) +
                 w.HB[eval_local] * mono_normal_at_origin(P, m, nrm);
-            v = ldexp(v, es * P.op_order[r]);
+            v = scale2(v, es * P.op_order[r]);
         } else {
             v = mono_op_at_origin(P, m, P.op_code[r], P.op_dim[r]);
         }
-        w.M[(k + m) * ld + n + r] = v;
+        st.rhs(k + m, r, v);
     }
     __syncwarp();
+}
+
+// Assemble [Phi P; P^T 0 | B] into M (full symmetric storage).
+__device__ void assemble_fp64(const StencilParams &P, const WarpSmem &w, int lane, int es, int eval_local) {
+    assemble_fp64_into(P, w, lane, es, eval_local, FullStore{w.M, P.n, mat_ld(P.n, P.nops)});
 }
 
 // In-place LU with partial pivoting of M[:, 0:n] applied to the right-hand sides, then
@@ -282,7 +353,7 @@ __device__ void scatter_row(const StencilParams &P, int64_t e, const WarpSmem &w
         P.col[base + rank] = ci;
         for (int r = 0; r < P.nops; r++) {
             const double v = sol[i * sol_ld + r * sol_stride];
-            const double vo = local ? v : ldexp(v, -es * P.op_order[r]);
+            const double vo = local ? v : scale2(v, -es * P.op_order[r]);
             P.val[r * P.nnz + base + rank] = vo;
             if (P.sell_col) sell_put(P, e, rank, ci, r, vo);
         }
@@ -364,17 +435,6 @@ __device__ __forceinline__ dfl df_sqrt(dfl a) {
     const float e = fmaf(-s, s, a.hi) + a.lo;
     const dfl r = qts(s, e * h);
     return a.hi > 0.0f ? r : dfl{0.0f, 0.0f};
-}
-// float -> double by rebuilding the bit pattern on the integer pipe (normal floats and
-// zero; subnormal floats, far below any entry scale here, map to zero)
-__device__ __forceinline__ double widen(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xffu;
-    if (e == 0u) return 0.0;
-    const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
-                                    ((unsigned long long)(e + 896u) << 52) |
-                                    ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)bits);
 }
 __device__ __forceinline__ double df_to_double(dfl a) { return widen(a.hi) + widen(a.lo); }
 

@@ -93,13 +93,17 @@ __device__ int load_interior(const StencilParams &P, int64_t e, const SplitSmem 
         if (P.isb) anyb |= (P.isb[g] != 0);
     }
     if (__any_sync(0xffffffffu, anyb)) return 1;
-    for (int o = 16; o > 0; o >>= 1) r2max = fmax(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
+    {  // r2max >= 0: an integer max of its bit pattern
+        long long m = __double_as_longlong(r2max);
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        r2max = __longlong_as_double(m);
+    }
     int es = 0;
     if (r2max > 0.0) frexp(sqrt(r2max), &es);
     *es_out = es;
     __syncwarp();
     for (int i = lane; i < k; i += 32)
-        for (int d = 0; d < dim; d++) s.X[i * 3 + d] = ldexp(s.X[i * 3 + d], -es);
+        for (int d = 0; d < dim; d++) s.X[i * 3 + d] = scale2(s.X[i * 3 + d], -es);
     __syncwarp();
     return 0;
 }

@@ -6,6 +6,8 @@ import pytest
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
+LU = 4  # RBF_FLAG_FP64_LU: the one-size FP64 build with the batched build's LU solver
+
 
 @pytest.fixture(scope="module")
 def pkg():
@@ -26,17 +28,21 @@ def rows_of(W, rows):
 @pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
 def test_uniform_batch_equals_build(pkg, precision):
     """Uniform stencils through the batched path give the one-size build's weights: the same
-    per-stencil code, bit for bit in FP64 (warp tiles)."""
+    per-stencil code, bit for bit in FP64 (warp tiles; the one-size build with its LU solver,
+    RBF_FLAG_FP64_LU), within 1e-8 against the default symmetric indefinite solve."""
     rng = np.random.default_rng(1)
     X = torch.from_numpy(rng.uniform(0, 1, (20000, 3))).cuda()
     adjl = pkg.find_neighbors(X, k=30)
     basis = pkg.PHS(3, poly_deg=2)
-    W0 = pkg.build_weights([(3, 0)], X, None, adjl, basis, precision="fp64")[0]
+    W0 = pkg.build_weights([(3, 0)], X, None, adjl, basis, precision="fp64", flags=LU)[0]
     ap, ai = pkg.ragged_stencils(adjl, torch.full((20000,), 30))
     W1 = pkg.build_weights_batched([(3, 0)], X, None, ap, ai, basis, precision=precision, tune=0)[0]
     assert torch.equal(W1.row_ptr, W0.row_ptr) and torch.equal(W1.col, W0.col)
     if precision == "fp64":
         assert torch.equal(W1.val, W0.val)
+        Wbk = pkg.build_weights([(3, 0)], X, None, adjl, basis, precision="fp64")[0]
+        d = (W1.val - Wbk.val).abs().reshape(-1, 30).amax(1) / Wbk.val.abs().reshape(-1, 30).amax(1)
+        assert float(d.max()) <= 1e-8
     else:
         d = (W1.val - W0.val).abs().reshape(-1, 30).amax(1) / W0.val.abs().reshape(-1, 30).amax(1)
         assert float(d.max()) <= 1e-8
@@ -49,7 +55,7 @@ def test_block_tile_bit_identical(pkg):
     X = torch.from_numpy(rng.uniform(0, 1, (3000, 3))).cuda()
     adjl = pkg.find_neighbors(X, k=60)
     basis = pkg.PHS(3, poly_deg=2)  # n = 70
-    W0 = pkg.build_weights([(3, 0), (1, 0)], X, None, adjl, basis, precision="fp64")
+    W0 = pkg.build_weights([(3, 0), (1, 0)], X, None, adjl, basis, precision="fp64", flags=LU)
     ap, ai = pkg.ragged_stencils(adjl, torch.full((3000,), 60))
     W1 = pkg.build_weights_batched([(3, 0), (1, 0)], X, None, ap, ai, basis, precision="fp64", tune=0)
     for a, b in zip(W1, W0):
@@ -76,7 +82,7 @@ def test_mixed_sizes_and_degrees(pkg, precision):
         for dg in (1, 2):
             sel = np.nonzero((kp == k) & (deg == dg))[0]
             ref = pkg.build_weights([(3, 0)], X, X[torch.from_numpy(sel).cuda()], adjl[torch.from_numpy(sel).cuda(), :k],
-                                    pkg.PHS(3, poly_deg=dg), precision="fp64")[0]
+                                    pkg.PHS(3, poly_deg=dg), precision="fp64", flags=LU)[0]
             got = rows_of(W, sel)
             want = rows_of(ref, range(len(sel)))
             for (c1, v1), (c2, v2) in zip(got, want):
@@ -105,7 +111,7 @@ def test_hermite_in_batch(pkg):
     X = torch.from_numpy(g).cuda()
     adjl = pkg.find_neighbors(X, k=20)
     basis = pkg.PHS(3, poly_deg=2)
-    W0 = pkg.build_weights([(3, 0)], X, None, adjl, basis, hermite=herm, precision="fp64")[0]
+    W0 = pkg.build_weights([(3, 0)], X, None, adjl, basis, hermite=herm, precision="fp64", flags=LU)[0]
     ap, ai = pkg.ragged_stencils(adjl, torch.full((len(g),), 20))
     W1 = pkg.build_weights_batched([(3, 0)], X, None, ap, ai, basis, hermite=herm, precision="fp64", tune=0)[0]
     assert torch.equal(W1.row_ptr, W0.row_ptr) and torch.equal(W1.col, W0.col)
