@@ -104,6 +104,8 @@ CASES = {
     "spmv_sell": "single-field apply of the built operator, sliced-ELL copy (spmv_sell_kernel)",
     "spmv_csr": "single-field apply of the built operator, CSR (spmv_pair_kernel)",
     "spmm16": "16-field apply of the built operator, column-major fields (spmm_interleaved_kernel)",
+    "spmv_ordered": "single-field apply, sliced copy in the points' Morton order, x and y in the caller's order "
+                    "(gather_perm_kernel + spmv_sell_perm_kernel)",
 }
 
 
@@ -134,6 +136,8 @@ def run_case(args, pkg, ctx, torch, dev):
                               sell=case == "spmv_sell")[-1]
         if case == "spmv_csr":
             W.sell = None
+        if case == "spmv_ordered":
+            W = W.to_sell_ordered(Xd)
     f = torch.from_numpy(np.sin(4 * X_h[:, 0]) * np.cos(3 * X_h[:, 1])).to(dev)
     F16 = torch.randn((16, n), dtype=torch.float64, device=dev) if case == "spmm16" else None
     feats = model.features(Xd, None, adjl) if case == "mlp_infer" else None
@@ -154,6 +158,7 @@ def run_case(args, pkg, ctx, torch, dev):
         "spmv_sell": lambda: W.apply(f),
         "spmv_csr": lambda: W.apply(f),
         "spmm16": lambda: W.apply(F16.T),
+        "spmv_ordered": lambda: W.apply(f),
     }
     fn = fns[case]
     fn()
@@ -786,6 +791,14 @@ def main():
     W = build(headline, Xd, adjl)[-1]
     ms_spmv_api = timed(lambda: W.apply(fd), 10, 3)
     ms_spmv = kernel_ms(lambda: W.apply(fd))  # sliced-ELL apply
+    # the sliced copy in the points' Morton order, x and y in the caller's order (made once,
+    # for operators applied many times); its product equals the plain sliced copy's bit for bit
+    t0 = time.perf_counter()
+    W_ord = W.to_sell_ordered(Xd)
+    torch.cuda.synchronize()
+    ms_to_ordered = (time.perf_counter() - t0) * 1e3
+    ord_equal = bool(torch.equal(W_ord.apply(fd), W.apply(fd)))
+    ms_spmv_ord = kernel_ms(lambda: W_ord.apply(fd))
     W_sell, W.sell = W.sell, None
     ms_spmv_csr = kernel_ms(lambda: W.apply(fd))  # the CSR apply of the same operator
     W.sell = W_sell
@@ -800,6 +813,7 @@ def main():
     csr_bytes = nnz * 12 + (n + 1) * 8 + 2 * n * 8
     apply_gbs = apply_bytes / (ms_spmv * 1e-3) / 1e9
     csr_gbs = csr_bytes / (ms_spmv_csr * 1e-3) / 1e9
+    ord_gbs = apply_bytes / (ms_spmv_ord * 1e-3) / 1e9
     # operator algebra on the device (a + 2 b over two value arrays of one structure, as a sum of
     # two operators on the same stencils):
     # one entry-wise pass over the value arrays, 24 bytes per entry (two reads, one write)
@@ -810,7 +824,7 @@ def main():
     alg_gbs = 24 * nnz / (ms_axpby * 1e-3) / 1e9
     algebra = {"kernel": "axpby_kernel (rbf_weights_axpby: out = a + 2 b over the values)", "nnz": nnz,
                "ms": ms_axpby, "GB_s": alg_gbs, "frac_of_hbm": alg_gbs / PEAKS.get("hbm_gbs", 6800.0)}
-    del W, W_sell, alg_out, alg_b
+    del W, W_sell, W_ord, alg_out, alg_b
     hbm_peak = PEAKS.get("hbm_gbs", 6800.0)
     hbm_src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in PEAKS else "fallback"
     fp64_peak = pkg.ctypes.c_double(0.0)
@@ -959,10 +973,17 @@ def main():
                            "fallback_unseeded": int(st32.n_fallback),
                            "seed_rel_err_mean_judged_by_solve": float(st_h.seed_rel_err_mean) if learned_on else None},
             "surrogate": training, "mlp": mlp,
-            "apply": {"value": apply_gbs, "unit": "GB/s", "ms": ms_spmv, "ms_per_call_api": ms_spmv_api,
-                      "nnz": nnz, "frac_of_hbm": apply_gbs / hbm_peak, "peak_source": hbm_src,
-                      "kernel": "spmv_sell_kernel (sliced-ELL copy written by the build)",
-                      "bytes": "sell_nnz*12 + (ne/32+1)*8 + 2*n*8 per apply; ms = kernel time (library CUDA events)",
+            "apply": {"value": ord_gbs, "unit": "GB/s", "ms": ms_spmv_ord, "nnz": nnz,
+                      "frac_of_hbm": ord_gbs / hbm_peak, "peak_source": hbm_src,
+                      "kernel": "gather_perm_kernel + spmv_sell_perm_kernel (sliced copy in the points' Morton "
+                                "order, x and y in the caller's order; the gather of x is counted in the time)",
+                      "bytes": "sell_nnz*12 + (ne/32+1)*8 + 2*n*8 per apply (algorithmic); ms = kernel time "
+                               "(library CUDA events)",
+                      "ordered_copy_ms_once": ms_to_ordered, "equals_plain_sliced_bitwise": ord_equal,
+                      "sliced_caller_layout": {"value": apply_gbs, "unit": "GB/s", "ms": ms_spmv,
+                                               "ms_per_call_api": ms_spmv_api, "frac_of_hbm": apply_gbs / hbm_peak,
+                                               "kernel": "spmv_sell_kernel (sliced-ELL copy written by the build, "
+                                                         "rows in the caller's order)"},
                       "csr": {"value": csr_gbs, "unit": "GB/s", "ms": ms_spmv_csr, "frac_of_hbm": csr_gbs / hbm_peak,
                               "kernel": "spmv_pair_kernel", "bytes": "nnz*12 + (ne+1)*8 + 2*n*8"}},
             "reordered": reordered,
@@ -977,7 +998,7 @@ def main():
                     "bound": "not HBM: candidate selection (distance keys and the sorted k+8 list) on the "
                              "SM pipes; the HBM fraction shows how far it is from the traffic bound"},
             "kernels_ms": {"knn": ms_knn_kernel, "knn_per_call_api": ms_knn, "build_headline": ms_kernel,
-                           "build_fp64": float(st64.ms_build), "spmv": ms_spmv},
+                           "build_fp64": float(st64.ms_build), "spmv": ms_spmv, "spmv_ordered": ms_spmv_ord},
             "peaks": {"fp64_tflops_measured": fp64_peak.value, "fp32_tflops_measured": fp32_peak.value,
                       "hbm_gbs": hbm_peak},
             "roofline": roof,

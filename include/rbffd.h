@@ -272,6 +272,28 @@ int rbf_sell_from_csr(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, const in
 int rbf_spmv_sell(rbf_ctx *ctx, int64_t ne, const int64_t *slice_off, const int32_t *sell_col,
                   const double *sell_val, const double *x, double alpha, double beta, double *y);
 
+/* The sliced copy in a locality order, for operators on unordered points applied many times
+ * (the same product as _eval_op / mul!, src/operators/operators.jl:217-218, 529-542).  The
+ * caller's point order stays the operator's interface; inside, the rows sit in the order
+ * row_at (slice s holds rows row_at[32 s .. 32 s + 31]) and each column is replaced by its
+ * position in the order col_at, so that rows applied together gather nearby x values.  The
+ * orders are permutations, e.g. the Morton orders rbf_reorder_points returns for the eval and
+ * the data points (the same array when eval == data).  Device pointers only.
+ *   rbf_sell_offsets_perm: slice_off[ceil(ne/32) + 1] over the rows in the order row_at.
+ *   rbf_sell_from_csr_perm: fill sell_col / sell_val from the CSR (each row's entries in CSR
+ *     order; row_at and col_at are range-checked).
+ *   rbf_spmv_sell_perm: y = alpha * W x + beta * y with x and y in the caller's order; x_work
+ *     (ns doubles, not aliasing x) receives x in the order col_at; row_at and col_at must be the
+ *     arrays the copy was made with. */
+int rbf_sell_offsets_perm(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, const int32_t *row_at, int64_t *slice_off,
+                          int64_t *sell_nnz);
+int rbf_sell_from_csr_perm(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const int32_t *col,
+                           const double *val, const int32_t *row_at, const int32_t *col_at, const int64_t *slice_off,
+                           int32_t *sell_col, double *sell_val);
+int rbf_spmv_sell_perm(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *slice_off, const int32_t *sell_col,
+                       const double *sell_val, const int32_t *row_at, const int32_t *col_at, const double *x,
+                       double *x_work, double alpha, double beta, double *y);
+
 /* ---- learned stencil surrogate (no counterpart in the reference) ------------ */
 /* Kernels of the MLP that predicts stencil weights (training and inference run on
  * them).  All arrays are device pointers; bf16 matrices are row-major with leading

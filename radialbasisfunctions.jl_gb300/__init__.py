@@ -452,6 +452,69 @@ class WeightsCSR:
                                                       _ptr(self.val), _ptr(off), _ptr(c), _ptr(v)))
         return WeightsSELL(off, c, v, self.shape, self.ctx)
 
+    def to_sell_ordered(self, data, eval_points=None, row_at=None, col_at=None):
+        """The sliced copy in a locality order (rbf_sell_offsets_perm + rbf_sell_from_csr_perm):
+        rows in the Morton order of the eval points and columns in that of the data points
+        (rbf_reorder_points; one order when the eval points are the data points), applied with
+        x and y in the caller's order.  For operators on unordered points applied many times."""
+        torch = _torch()
+        ne, ns = self.shape
+        dev = self.col.device
+        d = _points(data)
+        if col_at is None:
+            col_at, _ = reorder_points(d if _is_torch(d) else torch.from_numpy(d).to(dev), ctx=self.ctx)
+        if row_at is None:
+            if eval_points is None:
+                row_at = col_at
+            else:
+                q = _points(eval_points, "eval_points")
+                row_at, _ = reorder_points(q if _is_torch(q) else torch.from_numpy(q).to(dev), ctx=self.ctx)
+        row_at = torch.as_tensor(row_at).to(dev, torch.int32).contiguous()
+        col_at = torch.as_tensor(col_at).to(dev, torch.int32).contiguous()
+        if row_at.numel() != ne or col_at.numel() != ns:
+            raise DimensionMismatch("row_at / col_at must hold one entry per row / column")
+        off = torch.empty((ne + 31) // 32 + 1, dtype=torch.int64, device=dev)
+        tot = ctypes.c_int64(0)
+        self.ctx.check(self.ctx.lib.rbf_sell_offsets_perm(self.ctx.h, ne, _ptr(self.row_ptr), _ptr(row_at), _ptr(off),
+                                                          ctypes.byref(tot)))
+        c = torch.empty(max(tot.value, 1), dtype=torch.int32, device=dev)
+        v = torch.empty(max(tot.value, 1), dtype=torch.float64, device=dev)
+        self.ctx.check(self.ctx.lib.rbf_sell_from_csr_perm(self.ctx.h, ne, ns, _ptr(self.row_ptr), _ptr(self.col),
+                                                           _ptr(self.val), _ptr(row_at), _ptr(col_at), _ptr(off),
+                                                           _ptr(c), _ptr(v)))
+        return WeightsSELLOrdered(off, c, v, row_at, col_at, self.shape, self.ctx)
+
+    def __matmul__(self, x):
+        return self.apply(x)
+
+
+class WeightsSELLOrdered:
+    """An operator's sliced copy in a locality order of its rows and columns (see
+    WeightsCSR.to_sell_ordered): y = alpha W x + beta y for one field in the caller's order."""
+
+    def __init__(self, slice_off, col, val, row_at, col_at, shape, ctx: Context):
+        self.slice_off, self.col, self.val, self.row_at, self.col_at = slice_off, col, val, row_at, col_at
+        self.shape, self.ctx = shape, ctx
+        self._work = None
+
+    def apply(self, x, y=None, alpha=1.0, beta=0.0):
+        torch = _torch()
+        ne, ns = self.shape
+        dev = self.col.device
+        xt = torch.as_tensor(x, dtype=torch.float64).to(dev).contiguous()
+        if xt.ndim != 1 or xt.shape[0] != ns:
+            raise DimensionMismatch(f"the sliced apply takes one field of {ns} values")
+        out = y if y is not None else torch.zeros(ne, dtype=torch.float64, device=dev)
+        if out.dtype != torch.float64 or not out.is_cuda or not out.is_contiguous() or out.shape != (ne,):
+            raise DimensionMismatch("y must be a contiguous float64 CUDA vector of the operator's row count")
+        if self._work is None:
+            self._work = torch.empty(max(ns, 1), dtype=torch.float64, device=dev)
+        self.ctx.check(self.ctx.lib.rbf_spmv_sell_perm(self.ctx.h, ne, ns, _ptr(self.slice_off), _ptr(self.col),
+                                                       _ptr(self.val), _ptr(self.row_at), _ptr(self.col_at), _ptr(xt),
+                                                       _ptr(self._work), float(alpha),
+                                                       float(beta) if y is not None else 0.0, _ptr(out)))
+        return out
+
     def __matmul__(self, x):
         return self.apply(x)
 

@@ -128,6 +128,9 @@ SIGNATURES = {
     "rbf_sell_offsets": (_I, [_P, _I64, _P, _P, _P]),
     "rbf_sell_from_csr": (_I, [_P, _I64, _P, _P, _P, _P, _P, _P]),
     "rbf_spmv_sell": (_I, [_P, _I64, _P, _P, _P, _P, _D, _D, _P]),
+    "rbf_sell_offsets_perm": (_I, [_P, _I64, _P, _P, _P, _P]),
+    "rbf_sell_from_csr_perm": (_I, [_P, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "rbf_spmv_sell_perm": (_I, [_P, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _D, _D, _P]),
     "rbf_spmm_noalloc": (_I, [_P, _I64, _I64, _P, _P, _P, _I32, _I32, _P, _I64, _D, _D, _P, _I64]),
     "rbf_diag_fma_peak": (_I, [_P, _I32, ctypes.POINTER(_D)]),
     "rbf_ctx_kernel_launches": (_I64, [_P]),

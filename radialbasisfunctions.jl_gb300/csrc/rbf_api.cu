@@ -810,6 +810,69 @@ int rbf_spmv_sell(rbf_ctx *ctx, int64_t ne, const int64_t *slice_off, const int3
     return st;
 }
 
+int rbf_sell_offsets_perm(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, const int32_t *row_at, int64_t *slice_off,
+                          int64_t *sell_nnz) {
+    RBF_TRY(check_ctx(ctx));
+    if (ne < 0 || ne >= INT32_MAX) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid row count");
+    if (!sell_nnz) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null sell_nnz");
+    const void *ptrs[] = {row_ptr, row_at, slice_off};
+    for (const void *p : ptrs)
+        if (!rbf_is_device_ptr(p)) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the sliced layout takes device pointers only");
+    bool ok = true;
+    RBF_TRY(rbf_check_indices(ctx, row_at, ne, (int32_t)ne, &ok));
+    if (!ok) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "row_at holds a row index outside [0, ne)");
+    RBF_TRY(rbf_sell_offsets_perm_device(ctx, ne, row_ptr, row_at, slice_off, sell_nnz));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
+int rbf_sell_from_csr_perm(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const int32_t *col,
+                           const double *val, const int32_t *row_at, const int32_t *col_at, const int64_t *slice_off,
+                           int32_t *sell_col, double *sell_val) {
+    RBF_TRY(check_ctx(ctx));
+    if (ne < 0 || ne >= INT32_MAX || ns < 0 || ns >= INT32_MAX)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid row or column count");
+    const void *ptrs[] = {row_ptr, col, val, row_at, col_at, slice_off, sell_col, sell_val};
+    for (const void *p : ptrs)
+        if (!rbf_is_device_ptr(p)) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the sliced layout takes device pointers only");
+    bool ok = true;
+    RBF_TRY(rbf_check_indices(ctx, row_at, ne, (int32_t)ne, &ok));
+    if (!ok) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "row_at holds a row index outside [0, ne)");
+    RBF_TRY(rbf_check_indices(ctx, col_at, ns, (int32_t)ns, &ok));
+    if (!ok) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "col_at holds a column index outside [0, ns)");
+    RBF_TRY(rbf_sell_fill_perm_device(ctx, ne, ns, row_ptr, col, val, row_at, col_at, slice_off, sell_col, sell_val));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
+int rbf_spmv_sell_perm(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *slice_off, const int32_t *sell_col,
+                       const double *sell_val, const int32_t *row_at, const int32_t *col_at, const double *x,
+                       double *x_work, double alpha, double beta, double *y) {
+    RBF_TRY(check_ctx(ctx));
+    if (ne < 0 || ne >= INT32_MAX || ns < 0 || ns >= INT32_MAX)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid row or column count");
+    const void *ptrs[] = {slice_off, sell_col, sell_val, row_at, col_at, x, x_work, y};
+    for (const void *p : ptrs)
+        if (!rbf_is_device_ptr(p)) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "the sliced apply takes device pointers only");
+    if (x_work == x) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "x_work must not alias x");
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (ctx->timing) {
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, ctx->stream);
+    }
+    const int st = rbf_spmv_sell_perm_device(ctx, ne, ns, slice_off, sell_col, sell_val, row_at, col_at, x, x_work,
+                                             alpha, beta, y);
+    if (ctx->timing) {
+        cudaEventRecord(t1, ctx->stream);
+        cudaEventSynchronize(t1);
+        cudaEventElapsedTime(&ctx->last_ms, t0, t1);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
+    return st;
+}
+
 int rbf_build_count_ragged(rbf_ctx *ctx, int64_t ns, int64_t ne, const int64_t *adj_ptr, const rbf_hermite *herm,
                            int64_t *row_ptr_out, int64_t *nnz_out) {
     RBF_TRY(check_ctx(ctx));

@@ -142,6 +142,14 @@ int rbf_sell_fill_device(rbf_ctx *ctx, int64_t ne, const int64_t *d_rp, const in
                          const int64_t *d_off, int32_t *d_scol, double *d_sval);
 int rbf_spmv_sell_device(rbf_ctx *ctx, int64_t ne, const int64_t *d_off, const int32_t *d_scol, const double *d_sval,
                          const double *d_x, double alpha, double beta, double *d_y);
+int rbf_sell_offsets_perm_device(rbf_ctx *ctx, int64_t ne, const int64_t *d_rp, const int32_t *d_row_at,
+                                 int64_t *d_off, int64_t *sell_nnz);
+int rbf_sell_fill_perm_device(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *d_rp, const int32_t *d_col,
+                              const double *d_val, const int32_t *d_row_at, const int32_t *d_col_at,
+                              const int64_t *d_off, int32_t *d_scol, double *d_sval);
+int rbf_spmv_sell_perm_device(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *d_off, const int32_t *d_scol,
+                              const double *d_sval, const int32_t *d_row_at, const int32_t *d_col_at,
+                              const double *d_x, double *d_xwork, double alpha, double beta, double *d_y);
 int rbf_exclusive_scan_i32(rbf_ctx *ctx, const int32_t *d_in, int32_t *d_out, int64_t n,
                            int64_t *total);
 

@@ -113,3 +113,82 @@ def test_alpha_beta(pkg):
     assert (np.abs(y.cpu().numpy() - ref) <= 1e-14 * scale).all()
     with pytest.raises(pkg.DimensionMismatch):
         W.sell.apply(x[:100])
+
+
+def test_ordered_copy_on_unordered_points(pkg, orc):
+    """The copy in the Morton order of the points (to_sell_ordered): x and y stay in the caller's
+    order; the product equals the oracle's within 1e-10, and the plain sliced copy's bit for bit
+    (each row keeps its entries and their summation order, all rows have k entries)."""
+    rng = np.random.default_rng(31)
+    X = rng.uniform(0, 1, (40000, 3))
+    Xd = torch.from_numpy(X).cuda()
+    adjl = orc.knn(X, X, 30)
+    ref = orc.build(X, X, adjl, 3, 3, 2, [(orc.OP_LAP, 0)])
+    W = pkg.build_weights([(3, 0)], Xd, None, torch.from_numpy(adjl).cuda(), pkg.PHS(3, poly_deg=2), sell=True)[0]
+    S = W.to_sell_ordered(Xd)
+    # the ordered copy holds every row's entries, columns mapped to their Morton positions
+    pos = torch.empty_like(S.col_at)
+    pos[S.col_at.long()] = torch.arange(len(X), dtype=torch.int32, device="cuda")
+    rows = sell_to_rows(S, len(X))
+    ra = S.row_at.cpu().numpy()
+    posh = pos.cpu().numpy()
+    for r in range(0, len(X), 997):
+        c, v = rows[r]
+        cu, vu = csr_rows(W)[ra[r]]
+        assert np.array_equal(c, posh[cu]) and np.array_equal(v, vu)
+    f = np.sin(4 * X[:, 0]) * np.cos(3 * X[:, 1]) * np.exp(X[:, 2])
+    fd = torch.from_numpy(f).cuda()
+    y = S.apply(fd)
+    yr = orc.spmm(ref, f)
+    assert float(np.abs(y.cpu().numpy() - yr).max()) <= 1e-10 * np.abs(yr).max()
+    assert torch.equal(y, W.sell.apply(fd))
+    # beta != 0 accumulates into y in the caller's order
+    y0 = torch.from_numpy(rng.standard_normal(len(X))).cuda()
+    y1 = y0.clone()
+    S.apply(fd, y1, alpha=-0.5, beta=2.0)
+    assert torch.allclose(y1, -0.5 * y + 2.0 * y0, rtol=1e-14, atol=1e-12 * float(y.abs().max()))
+
+
+def test_ordered_copy_regrid_and_uneven_rows(pkg, orc):
+    """Eval points distinct from the data points (two orders) and rows of uneven length
+    (Dirichlet identity rows of one entry among k-entry rows): within 1e-10 of the oracle."""
+    rng = np.random.default_rng(32)
+    S_ = rng.uniform(0, 1, (20000, 2))
+    T_ = rng.uniform(0.05, 0.95, (15000, 2))
+    adjl = orc.knn(S_, T_, 12)
+    ref = orc.build(S_, T_, adjl, 2, 3, 1, [(orc.OP_IDENT, 0)])
+    W = pkg.build_weights([(0, 0)], torch.from_numpy(S_).cuda(), torch.from_numpy(T_).cuda(),
+                          torch.from_numpy(adjl).cuda(), pkg.PHS(3, poly_deg=1))[0]
+    So = W.to_sell_ordered(torch.from_numpy(S_).cuda(), torch.from_numpy(T_).cuda())
+    f = S_[:, 0] ** 2 - S_[:, 1]
+    y = So.apply(torch.from_numpy(f).cuda()).cpu().numpy()
+    yr = orc.spmm(ref, f)
+    assert np.abs(y - yr).max() <= 1e-10 * np.abs(yr).max()
+    # a square with Dirichlet boundary rows (identity rows hold one entry)
+    xs = np.linspace(0, 1, 61)
+    P = np.array([(x, yv) for x in xs for yv in xs])
+    isb = (P[:, 0] == 0) | (P[:, 0] == 1) | (P[:, 1] == 0) | (P[:, 1] == 1)
+    nrm = np.zeros((int(isb.sum()), 2))
+    nrm[:, 0] = 1.0
+    herm = dict(is_boundary=isb, bc=[pkg.BoundaryCondition(1.0, 0.0)] * int(isb.sum()), normals=nrm)
+    op = pkg.laplacian(P, basis=pkg.PHS(3, poly_deg=2), k=15, hermite=herm)
+    Wh = op.weights
+    Sh = Wh.to_sell_ordered(torch.from_numpy(P).cuda())
+    u = np.sin(P[:, 0]) * np.cos(2 * P[:, 1])
+    y0 = Wh.apply(torch.from_numpy(u).cuda()).cpu().numpy()
+    y1 = Sh.apply(torch.from_numpy(u).cuda()).cpu().numpy()
+    # rows of 1/h^2-sized weights cancel to O(1) results: two summation orders agree to the
+    # apply bar (1e-10 relative), not to the last bits
+    assert np.abs(y1 - y0).max() <= 1e-10 * np.abs(y0).max()
+
+
+def test_ordered_copy_rejects_bad_orders(pkg):
+    rng = np.random.default_rng(33)
+    X = torch.from_numpy(rng.uniform(0, 1, (3000, 2))).cuda()
+    W = pkg.build_weights([(3, 0)], X, None, pkg.find_neighbors(X, k=12), pkg.PHS(3, poly_deg=2))[0]
+    bad = torch.arange(3000, dtype=torch.int32, device="cuda")
+    bad[7] = 3000
+    with pytest.raises(ValueError):
+        W.to_sell_ordered(X, row_at=bad, col_at=torch.arange(3000, dtype=torch.int32, device="cuda"))
+    with pytest.raises(ValueError):
+        W.to_sell_ordered(X, row_at=torch.arange(3000, dtype=torch.int32, device="cuda"), col_at=bad)
