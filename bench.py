@@ -418,11 +418,17 @@ def fourier_fields(torch, X, nf, seed):
     return F
 
 
-def all_configs(pkg, torch, ctx, stream):
+def all_configs(pkg, torch, ctx, stream, cpu=True):
     """The other workloads of the benchmark's configuration list, each timed once on the GPU:
-    kNN, plain FP64 and FP32-refined builds (stencils/s, build only), the refined weights'
-    max row-relative difference to the FP64 ones, and the apply (algorithmic bytes over the
-    library's kernel time, fraction of the measured copy rate).  One JSON line per workload."""
+    kNN, plain FP64, FP32-refined and (3D regrid) learned + refined builds (stencils/s, build
+    only), every build's max / RMS row-relative weight error and operator-on-test-function error
+    against the oracle (the reference algorithm on the host, on a sample of the same stencils:
+    the whole cloud where it is small or has Hermite rows), and the apply (algorithmic bytes over
+    the library's kernel time, fraction of the measured copy rate or of the FP64 FMA rate).  One
+    JSON line per workload."""
+    from importlib import import_module
+    from oracle import oracle as O
+    L = import_module(pkg.__name__ + ".learned")
     hbm = PEAKS.get("hbm_gbs", 6800.0)
 
     def ev_ms(fn, reps=2):
@@ -445,27 +451,31 @@ def all_configs(pkg, torch, ctx, stream):
         ctx.lib.rbf_ctx_set_timing(ctx.h, 0)
         return float(v.value)
 
-    def row_diff(W, Wr):
-        rp = W.row_ptr
-        rows = torch.repeat_interleave(torch.arange(W.shape[0], device=rp.device), rp[1:] - rp[:-1])
-        num = torch.zeros(W.shape[0], dtype=torch.float64, device=rp.device)
-        den = torch.zeros_like(num)
-        num.scatter_reduce_(0, rows, (W.val - Wr.val).abs(), "amax")
-        den.scatter_reduce_(0, rows, Wr.val.abs(), "amax")
-        ok = den > 0
-        return float((num[ok] / den[ok]).max())
-
     fma64 = pkg.ctypes.c_double(0.0)
     ctx.check(ctx.lib.rbf_diag_fma_peak(ctx.h, 1, pkg.ctypes.byref(fma64)))
     fma_peak = fma64.value / 2.0  # FP64 FMA per second (the peak counts 2 flops per FMA), in T
 
-    def report(name, desc, ne, ms_knn, ms64, ms32, err, W, nf, ms_apply, extra=None):
+    def vs_oracle(Ws, ref, f):
+        """Worst over the operators of oracle_errors on the sampled rows."""
+        if ref is None:
+            return None
+        errs = [oracle_errors(torch, W, ref, f, q) for q, W in enumerate(Ws)]
+        if not all(e.get("structure_equal") for e in errs):
+            return {"structure_equal": False}
+        return {"structure_equal": True,
+                "max_row_rel_weight_err": max(e["max_row_rel_weight_err"] for e in errs),
+                "rms_row_rel_weight_err": max(e["rms_row_rel_weight_err"] for e in errs),
+                "operator_on_test_function_rel_err": max(e["operator_on_test_function_rel_err"] for e in errs)}
+
+    def report(name, desc, ne, ms_knn, builds, ref_info, W, nf, ms_apply, extra=None):
         by = W.nnz * 12 + (ne + 1) * 8 + nf * (W.shape[1] + ne) * 8
         fmas = W.nnz * nf / (ms_apply * 1e-3) / 1e12
-        line = {"workload": name, "desc": desc, "stencils": ne, "ms_knn": ms_knn,
-                "fp64": {"ms_build": ms64, "stencils_per_s": ne / (ms64 * 1e-3)},
-                "fp32_refined": {"ms_build": ms32, "stencils_per_s": ne / (ms32 * 1e-3), "speedup_vs_fp64": ms64 / ms32},
-                "max_row_rel_diff_refined_vs_fp64": err, "bar": 1e-8,
+        ms64 = builds["fp64"]["ms_build"]
+        for b in builds.values():
+            b["stencils_per_s"] = ne / (b["ms_build"] * 1e-3)
+            b["speedup_vs_fp64"] = ms64 / b["ms_build"]
+        line = {"workload": name, "desc": desc, "stencils": ne, "ms_knn": ms_knn, "builds": builds,
+                "oracle_sample": ref_info, "bar": 1e-8,
                 "apply": {"fields": nf, "nnz": W.nnz, "ms": ms_apply, "GB_s": by / (ms_apply * 1e-3) / 1e9,
                           "frac_of_hbm": by / (ms_apply * 1e-3) / 1e9 / hbm,
                           "fp64_fma_T_per_s": fmas, "frac_of_fp64_fma": fmas / fma_peak,
@@ -474,39 +484,53 @@ def all_configs(pkg, torch, ctx, stream):
             line.update(extra)
         print(json.dumps(line), flush=True)
 
+    def stats_of(st):
+        return {"fallback_stencils": int(st.n_fallback),
+                "residuals_per_stencil": float(st.n_residuals) / max(1, int(st.n_stencils))}
+
     dev = torch.device("cuda", ctx.device)
-    # C1: 2D Laplacian, 10,000 uniform points, PHS3 degree 2, k = 20
+    # ---- C1: 2D Laplacian, 10,000 uniform points, PHS3 degree 2, k = 20 (oracle: every stencil)
     rng = np.random.default_rng(101)
-    X = torch.from_numpy(rng.uniform(0, 1, (10_000, 2))).to(dev)
+    Xh = rng.uniform(0, 1, (10_000, 2))
+    X = torch.from_numpy(Xh).to(dev)
     ms_knn, a = ev_ms(lambda: pkg.find_neighbors(X, k=20, ctx=ctx))
     b = pkg.PHS(3, poly_deg=2)
     ms64, W64 = ev_ms(lambda: pkg.build_weights([(3, 0)], X, None, a, b, ctx=ctx)[0])
-    ms32, W32 = ev_ms(lambda: pkg.build_weights([(3, 0)], X, None, a, b, ctx=ctx, precision="fp32_refined")[0])
-    f = torch.sin(4 * X[:, 0]) * torch.cos(3 * X[:, 1])
-    lap = W32.apply(f)
+    st = pkg._native.BuildStats()
+    ms32, W32 = ev_ms(lambda: pkg.build_weights([(3, 0)], X, None, a, b, ctx=ctx, precision="fp32_refined",
+                                                stats=st)[0])
+    f = np.sin(4 * Xh[:, 0]) * np.cos(3 * Xh[:, 1])
+    ref = O.build(Xh, Xh, a.cpu().numpy(), 2, 3, 2, [(3, 0)]) if cpu else None
+    builds = {"fp64": {"ms_build": ms64, "vs_oracle": vs_oracle([W64], ref, f)},
+              "fp32_refined": {"ms_build": ms32, "vs_oracle": vs_oracle([W32], ref, f), **stats_of(st)}}
+    fd = torch.from_numpy(f).to(dev)
+    lap = W32.apply(fd)
     inner = ((X > 0.1) & (X < 0.9)).all(1)
-    err_f = float(((lap + 25 * f)[inner]).abs().max() / (25 * f[inner]).abs().max())
+    err_f = float(((lap + 25 * fd)[inner]).abs().max() / (25 * fd[inner]).abs().max())
     report("lap2d_10k", "2D Laplacian, 10,000 uniform points, PHS3 degree 2, k = 20 (26 x 26)", 10_000, ms_knn,
-           ms64, ms32, row_diff(W32, W64), W32, 1, kernel_ms(lambda: W32.apply(f)),
+           builds, "all 10,000 stencils", W32, 1, kernel_ms(lambda: W32.apply(fd)),
            {"laplacian_rel_err_vs_analytic_interior": err_f, "note": "L2-resident sizes: launch-bound, not a roofline case"})
-    # C2: 3D gradient + Laplacian, 100^3 jittered lattice, PHS5 degree 2, k = 40, 16 fields
+    # ---- C2: 3D gradient + Laplacian, 100^3 jittered lattice, PHS5 degree 2, k = 40, 16 fields
     cfg = CONFIGS["gradlap3d_1M"]
-    X = torch.from_numpy(make_points(cfg, 1_000_000, 102)).to(dev)
+    Xh = make_points(cfg, 1_000_000, 102)
+    X = torch.from_numpy(Xh).to(dev)
     ms_knn, a = ev_ms(lambda: pkg.find_neighbors(X, k=40, ctx=ctx))
     b = pkg.PHS(5, poly_deg=2)
     ms64, W64 = ev_ms(lambda: pkg.build_weights(cfg["ops"], X, None, a, b, ctx=ctx))
     st = pkg._native.BuildStats()
     ms32, W32 = ev_ms(lambda: pkg.build_weights(cfg["ops"], X, None, a, b, ctx=ctx, precision="fp32_refined",
                                                 stats=st))
-    err = max(row_diff(w, w0) for w, w0 in zip(W32, W64))
+    m = 100_000
+    f = np.sin(2 * Xh[:, 0]) * np.cos(3 * Xh[:, 1]) * np.exp(Xh[:, 2])
+    ref = O.build(Xh, Xh[:m], a[:m].cpu().numpy(), 3, 5, 2, cfg["ops"]) if cpu else None
+    builds = {"fp64": {"ms_build": ms64, "vs_oracle": vs_oracle(W64, ref, f)},
+              "fp32_refined": {"ms_build": ms32, "vs_oracle": vs_oracle(W32, ref, f), **stats_of(st)}}
     F = fourier_fields(torch, X, 16, 103)
-    stats = {"refined_fallback_stencils": int(st.n_fallback),
-             "refined_residuals_per_stencil": float(st.n_residuals) / max(1, int(st.n_stencils))}
     report("gradlap3d_1M", "3D gradient + Laplacian (4 operators, one factorisation), 100^3 jittered lattice, "
-           "PHS5 degree 2, k = 40 (50 x 50); 16 fields per operator", 1_000_000, ms_knn, ms64, ms32, err, W32[3], 16,
-           kernel_ms(lambda: W32[3].apply(F)), stats)
+           "PHS5 degree 2, k = 40 (50 x 50); 16 fields per operator", 1_000_000, ms_knn, builds,
+           f"first {m} stencils", W32[3], 16, kernel_ms(lambda: W32[3].apply(F)))
     del W64, W32, F, a, X
-    # C3: 2D unit disk, 2,000,000 interior + 5,000 boundary points, Dirichlet / Neumann, PHS3 degree 3, k = 30
+    # ---- C3: 2D unit disk, 2,000,000 interior + 5,000 boundary points, Dirichlet / Neumann, PHS3 degree 3, k = 30
     Xh, isb, nrm, al, be = unit_disk(2_000_000, 5_000, 104)
     X = torch.from_numpy(Xh).to(dev)
     ms_knn, a = ev_ms(lambda: pkg.find_neighbors(X, k=30, ctx=ctx))
@@ -517,25 +541,52 @@ def all_configs(pkg, torch, ctx, stream):
     run = lambda prec: pkg.build_weights_batched([(3, 0)], X, None, ap, ai, b, hermite=herm, precision=prec,
                                                  tune=1, ctx=ctx, stats=st)[0]
     ms64, W64 = ev_ms(lambda: run("fp64"))
+    s64 = stats_of(st)
     ms32, W32 = ev_ms(lambda: run("fp32_refined"))
-    stats = {"refined_fallback_stencils": int(st.n_fallback),
-             "refined_residuals_per_stencil": float(st.n_residuals) / max(1, int(st.n_stencils))}
-    u = X[:, 0] ** 2 + X[:, 1] ** 2 + 1.0
+    s32 = stats_of(st)
+    u = Xh[:, 0] ** 2 + Xh[:, 1] ** 2 + 1.0
+    ref = O.build(Xh, Xh, a.cpu().numpy(), 2, 3, 3, [(3, 0)], hermite=(isb.astype(np.uint8), al, be, nrm)) \
+        if cpu else None
+    builds = {"fp64": {"ms_build": ms64, "vs_oracle": vs_oracle([W64], ref, u)},
+              "fp32_refined": {"ms_build": ms32, "vs_oracle": vs_oracle([W32], ref, u), **s32}}
+    ud = torch.from_numpy(u).to(dev)
     report("disk_hermite_2M", f"2D unit disk, {len(Xh) - 5000} interior + 5,000 boundary points (Dirichlet upper, "
            "Neumann lower half-circle), PHS3 degree 3, k = 30 (40 x 40, Hermite rows on boundary stencils), one "
-           "persistent batched launch with autotuned tiles", len(Xh), ms_knn, ms64, ms32, row_diff(W32, W64), W32, 1,
-           kernel_ms(lambda: W32.apply(u)), stats)
+           "persistent batched launch with autotuned tiles", len(Xh), ms_knn, builds, "all stencils", W32, 1,
+           kernel_ms(lambda: W32.apply(ud)))
     del W64, W32, a, ap, ai, X
-    # C5: 3D regrid, 8,000,000 uniform sources onto 8,000,000 mixture targets, PHS3 degree 1, k = 20, 32 fields
+    # ---- C5: 3D regrid, 8,000,000 uniform sources onto 8,000,000 mixture targets, PHS3 degree 1, k = 20,
+    # 32 fields; the learned form with a surrogate trained on 2,000,000 regrid stencils
     rng = np.random.default_rng(105)
-    S = torch.from_numpy(rng.uniform(0, 1, (8_000_000, 3))).to(dev)
-    T = torch.from_numpy(mixture_targets(8_000_000, 106)).to(dev)
+    Sh = rng.uniform(0, 1, (8_000_000, 3))
+    Th = mixture_targets(8_000_000, 106)
+    S = torch.from_numpy(Sh).to(dev)
+    T = torch.from_numpy(Th).to(dev)
     ms_knn, a = ev_ms(lambda: pkg.find_neighbors(S, T, k=20, ctx=ctx), reps=1)
     b = pkg.PHS(3, poly_deg=1)
+    t0 = time.perf_counter()
+    Xb, Tt = L.training_set(1_000_000, 1_000_000, 20, 3, b, [(0, 0)], seed=6000, ctx=ctx, separate_eval=True)
+    model, hist = L.train_surrogate(Xb, Tt, 20, 3, epochs=8, batch=4096, lr=2e-3, ctx=ctx)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    del Xb, Tt
     ms64, W64 = ev_ms(lambda: pkg.build_weights([(0, 0)], S, T, a, b, ctx=ctx)[0], reps=1)
-    ms32, W32 = ev_ms(lambda: pkg.build_weights([(0, 0)], S, T, a, b, ctx=ctx, precision="fp32_refined")[0], reps=1)
-    err = row_diff(W32, W64)
-    del W64
+    st = pkg._native.BuildStats()
+    ms32, W32 = ev_ms(lambda: pkg.build_weights([(0, 0)], S, T, a, b, ctx=ctx, precision="fp32_refined",
+                                                stats=st)[0], reps=1)
+    s32 = stats_of(st)
+    stl = pkg._native.BuildStats()
+    msl, Wl = ev_ms(lambda: L.build_learned(model, [(0, 0)], S, a, b, ctx=ctx, stats=stl, eval_points=T)[0], reps=1)
+    sl = stats_of(stl)
+    sl["seed_rel_err_mean_judged_by_solve"] = float(stl.seed_rel_err_mean)
+    m = 200_000
+    f = np.sin(3 * Sh[:, 0]) * np.cos(2 * Sh[:, 1]) + Sh[:, 2] ** 2
+    ref = O.build(Sh, Th[:m], a[:m].cpu().numpy(), 3, 3, 1, [(0, 0)]) if cpu else None
+    builds = {"fp64": {"ms_build": ms64, "vs_oracle": vs_oracle([W64], ref, f)},
+              "fp32_refined": {"ms_build": ms32, "vs_oracle": vs_oracle([W32], ref, f), **s32},
+              "learned": {"ms_build": msl, "vs_oracle": vs_oracle([Wl], ref, f), **sl,
+                          "note": "features + tcgen05 inference + seeded refined build"}}
+    del W64, Wl
     F = fourier_fields(torch, S, 32, 107)
     ms_apply = kernel_ms(lambda: W32.apply(F))
     # the same operator on Morton-ordered sources and targets (reorder_points): the gathers of
@@ -549,9 +600,13 @@ def all_configs(pkg, torch, ctx, stream):
     ms_o = kernel_ms(lambda: Wo.apply(Fo))
     by = Wo.nnz * 12 + (8_000_001) * 8 + 32 * 16_000_000 * 8
     report("regrid3d_8M", "3D regrid, 8,000,000 uniform sources onto 8,000,000 targets (50 % uniform, 50 % from 8 "
-           "Gaussians), PHS3 degree 1, k = 20 (24 x 24); 32 fields", 8_000_000, ms_knn, ms64, ms32, err, Wo, 32,
-           ms_apply, {"apply_morton_order": {"ms": ms_o, "GB_s": by / (ms_o * 1e-3) / 1e9,
-                                             "frac_of_hbm": by / (ms_o * 1e-3) / 1e9 / hbm}})
+           "Gaussians), PHS3 degree 1, k = 20 (24 x 24); 32 fields", 8_000_000, ms_knn, builds,
+           f"first {m} stencils", Wo, 32, ms_apply,
+           {"surrogate": {"train_stencils": 2_000_000, "epochs": 8, "train_s": train_s, "loss_last_epoch": hist[-1],
+                          "training_clouds": "uniform and +/-20 % density-gradient sources, independent eval clouds "
+                                             "of the same distribution"},
+            "apply_morton_order": {"ms": ms_o, "GB_s": by / (ms_o * 1e-3) / 1e9,
+                                   "frac_of_hbm": by / (ms_o * 1e-3) / 1e9 / hbm}})
 
 
 def run_reference(args, cfg, n):
@@ -608,7 +663,7 @@ def main():
     stream = torch.cuda.current_stream()  # the package binds the library to this stream
     dev = torch.device("cuda", local)
     if args.all_configs:
-        all_configs(pkg, torch, ctx, stream)
+        all_configs(pkg, torch, ctx, stream, cpu=not args.no_cpu_baseline)
         return
     if args.case:
         run_case(args, pkg, ctx, torch, dev)

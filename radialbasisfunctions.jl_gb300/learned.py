@@ -227,10 +227,12 @@ def sample_cloud(n, dim, seed, gradient=0.0, device=None):
     return X.to(device) if device is not None else X
 
 
-def training_set(n_uniform, n_gradient, k, dim, basis, ops, seed=0, ctx=None, gradient=0.2):
+def training_set(n_uniform, n_gradient, k, dim, basis, ops, seed=0, ctx=None, gradient=0.2, separate_eval=False):
     """Features and local-unit target weights of the plain FP64 solve on seeded clouds:
     n_uniform stencils of a uniform cloud and n_gradient of a cloud with a linear density
-    gradient (every point of each cloud is an eval point)."""
+    gradient.  Every point of each cloud is an eval point, or, with separate_eval (regrid
+    stencils, whose weights are trivial at the data points), an independent cloud of the same
+    distribution and size holds the eval points."""
     torch = _torch()
     from . import Context, build_weights, find_neighbors
     ctx = ctx or Context.default(0)
@@ -241,10 +243,11 @@ def training_set(n_uniform, n_gradient, k, dim, basis, ops, seed=0, ctx=None, gr
         if n <= 0:
             continue
         X = sample_cloud(n, dim, sd, gr, dev)
-        adjl = find_neighbors(X, k=k, ctx=ctx)
-        W = build_weights(ops, X, None, adjl, basis, precision="fp64", ctx=ctx,
+        E = sample_cloud(n, dim, sd + 7919, gr, dev) if separate_eval else None
+        adjl = find_neighbors(X, E, k=k, ctx=ctx)
+        W = build_weights(ops, X, E, adjl, basis, precision="fp64", ctx=ctx,
                           flags=RBF_FLAG_STENCIL_ORDER | RBF_FLAG_LOCAL_UNITS)[0]
-        feats.append(mlp.features(X, None, adjl))
+        feats.append(mlp.features(X, E, adjl))
         targs.append(W.val.reshape(n, k).to(torch.float32))
     return torch.cat(feats), torch.cat(targs)
 
@@ -286,10 +289,11 @@ def surrogate_error(model, Xb, T):
     return float(err.max()), float(err.median())
 
 
-def build_learned(model, ops, data, adjl, basis, ctx=None, stats=None, return_status=False, sell=False):
+def build_learned(model, ops, data, adjl, basis, ctx=None, stats=None, return_status=False, sell=False,
+                  eval_points=None):
     """Learned + FP32-refined build: the surrogate's prediction seeds the refinement."""
     from . import build_weights
-    feats = model.features(data, None, adjl)
+    feats = model.features(data, eval_points, adjl)
     seed = model.predict(feats)
-    return build_weights(ops, data, None, adjl, basis, precision="learned", ctx=ctx or model.ctx, stats=stats,
+    return build_weights(ops, data, eval_points, adjl, basis, precision="learned", ctx=ctx or model.ctx, stats=stats,
                          seed=seed, return_status=return_status, sell=sell)
