@@ -106,6 +106,8 @@ CASES = {
     "spmm16": "16-field apply of the built operator, column-major fields (spmm_interleaved_kernel)",
     "spmv_ordered": "single-field apply, sliced copy in the points' Morton order, x and y in the caller's order "
                     "(gather_perm_kernel + spmv_sell_perm_kernel)",
+    "step": "one headline step: kNN + features + tcgen05 inference + seeded refined build (CSR + sliced copy) + "
+            "one apply (an untrained surrogate: the same kernels as a trained one)",
 }
 
 
@@ -123,12 +125,12 @@ def run_case(args, pkg, ctx, torch, dev):
     case = args.case
     from importlib import import_module
     L = import_module(pkg.__name__ + ".learned")
-    adjl = pkg.find_neighbors(Xd, k=k, ctx=ctx) if case != "knn" else None
+    adjl = pkg.find_neighbors(Xd, k=k, ctx=ctx) if case not in ("knn", "step") else None
     model = None
     if case == "build_learned":  # a trained surrogate: its seed decides the refinement's path
         Xb, T = L.training_set(100_000, 100_000, k, cfg["dim"], basis, cfg["ops"], seed=5000, ctx=ctx)
         model, _ = L.train_surrogate(Xb, T, k, cfg["dim"], epochs=3, batch=4096, ctx=ctx)
-    elif case in ("features", "mlp_infer", "mlp_train"):  # the kernels' work does not depend on the weights
+    elif case in ("features", "mlp_infer", "mlp_train", "step"):  # the kernels' work does not depend on the weights
         model = L.StencilMLP(k, cfg["dim"], ctx=ctx, seed=0)
     W = None
     if case.startswith("spm"):
@@ -159,6 +161,8 @@ def run_case(args, pkg, ctx, torch, dev):
         "spmv_csr": lambda: W.apply(f),
         "spmm16": lambda: W.apply(F16.T),
         "spmv_ordered": lambda: W.apply(f),
+        "step": lambda: L.build_learned(model, cfg["ops"], Xd, pkg.find_neighbors(Xd, k=k, ctx=ctx), basis, ctx=ctx,
+                                        sell=True)[-1].apply(f),
     }
     fn = fns[case]
     fn()
@@ -456,9 +460,12 @@ def all_configs(pkg, torch, ctx, stream, cpu=True):
     fma_peak = fma64.value / 2.0  # FP64 FMA per second (the peak counts 2 flops per FMA), in T
 
     def vs_oracle(Ws, ref, f):
-        """Worst over the operators of oracle_errors on the sampled rows."""
+        """Worst over the operators of oracle_errors on the sampled rows; ref is a pair (the
+        reference arithmetic's weights, the local-frame oracle's) or None."""
         if ref is None:
             return None
+        if isinstance(ref, tuple):
+            return {"reference_arithmetic": vs_oracle(Ws, ref[0], f), "local_frame": vs_oracle(Ws, ref[1], f)}
         errs = [oracle_errors(torch, W, ref, f, q) for q, W in enumerate(Ws)]
         if not all(e.get("structure_equal") for e in errs):
             return {"structure_equal": False}
@@ -476,6 +483,10 @@ def all_configs(pkg, torch, ctx, stream, cpu=True):
             b["speedup_vs_fp64"] = ms64 / b["ms_build"]
         line = {"workload": name, "desc": desc, "stencils": ne, "ms_knn": ms_knn, "builds": builds,
                 "oracle_sample": ref_info, "bar": 1e-8,
+                "oracle_frames": "reference_arithmetic: the reference's algorithm in its raw coordinates; "
+                                 "local_frame: the same formulation assembled per stencil centred at the eval "
+                                 "point and scaled by a power of two (pinned to 60-digit truth where the raw "
+                                 "systems are ill-conditioned)",
                 "apply": {"fields": nf, "nnz": W.nnz, "ms": ms_apply, "GB_s": by / (ms_apply * 1e-3) / 1e9,
                           "frac_of_hbm": by / (ms_apply * 1e-3) / 1e9 / hbm,
                           "fp64_fma_T_per_s": fmas, "frac_of_fp64_fma": fmas / fma_peak,
@@ -500,7 +511,8 @@ def all_configs(pkg, torch, ctx, stream, cpu=True):
     ms32, W32 = ev_ms(lambda: pkg.build_weights([(3, 0)], X, None, a, b, ctx=ctx, precision="fp32_refined",
                                                 stats=st)[0])
     f = np.sin(4 * Xh[:, 0]) * np.cos(3 * Xh[:, 1])
-    ref = O.build(Xh, Xh, a.cpu().numpy(), 2, 3, 2, [(3, 0)]) if cpu else None
+    ref = tuple(O.build(Xh, Xh, a.cpu().numpy(), 2, 3, 2, [(3, 0)], frame=fr) for fr in ("raw", "local")) \
+        if cpu else None
     builds = {"fp64": {"ms_build": ms64, "vs_oracle": vs_oracle([W64], ref, f)},
               "fp32_refined": {"ms_build": ms32, "vs_oracle": vs_oracle([W32], ref, f), **stats_of(st)}}
     fd = torch.from_numpy(f).to(dev)
@@ -522,7 +534,8 @@ def all_configs(pkg, torch, ctx, stream, cpu=True):
                                                 stats=st))
     m = 100_000
     f = np.sin(2 * Xh[:, 0]) * np.cos(3 * Xh[:, 1]) * np.exp(Xh[:, 2])
-    ref = O.build(Xh, Xh[:m], a[:m].cpu().numpy(), 3, 5, 2, cfg["ops"]) if cpu else None
+    ref = tuple(O.build(Xh, Xh[:m], a[:m].cpu().numpy(), 3, 5, 2, cfg["ops"], frame=fr) for fr in ("raw", "local")) \
+        if cpu else None
     builds = {"fp64": {"ms_build": ms64, "vs_oracle": vs_oracle(W64, ref, f)},
               "fp32_refined": {"ms_build": ms32, "vs_oracle": vs_oracle(W32, ref, f), **stats_of(st)}}
     F = fourier_fields(torch, X, 16, 103)
@@ -545,8 +558,8 @@ def all_configs(pkg, torch, ctx, stream, cpu=True):
     ms32, W32 = ev_ms(lambda: run("fp32_refined"))
     s32 = stats_of(st)
     u = Xh[:, 0] ** 2 + Xh[:, 1] ** 2 + 1.0
-    ref = O.build(Xh, Xh, a.cpu().numpy(), 2, 3, 3, [(3, 0)], hermite=(isb.astype(np.uint8), al, be, nrm)) \
-        if cpu else None
+    ref = tuple(O.build(Xh, Xh, a.cpu().numpy(), 2, 3, 3, [(3, 0)], hermite=(isb.astype(np.uint8), al, be, nrm),
+                        frame=fr) for fr in ("raw", "local")) if cpu else None
     builds = {"fp64": {"ms_build": ms64, "vs_oracle": vs_oracle([W64], ref, u)},
               "fp32_refined": {"ms_build": ms32, "vs_oracle": vs_oracle([W32], ref, u), **s32}}
     ud = torch.from_numpy(u).to(dev)
@@ -581,7 +594,8 @@ def all_configs(pkg, torch, ctx, stream, cpu=True):
     sl["seed_rel_err_mean_judged_by_solve"] = float(stl.seed_rel_err_mean)
     m = 200_000
     f = np.sin(3 * Sh[:, 0]) * np.cos(2 * Sh[:, 1]) + Sh[:, 2] ** 2
-    ref = O.build(Sh, Th[:m], a[:m].cpu().numpy(), 3, 3, 1, [(0, 0)]) if cpu else None
+    ref = tuple(O.build(Sh, Th[:m], a[:m].cpu().numpy(), 3, 3, 1, [(0, 0)], frame=fr) for fr in ("raw", "local")) \
+        if cpu else None
     builds = {"fp64": {"ms_build": ms64, "vs_oracle": vs_oracle([W64], ref, f)},
               "fp32_refined": {"ms_build": ms32, "vs_oracle": vs_oracle([W32], ref, f), **s32},
               "learned": {"ms_build": msl, "vs_oracle": vs_oracle([Wl], ref, f), **sl,
@@ -782,6 +796,9 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sample = args.cpu_sample or (200_000 if n >= 1_000_000 else n)
         cb = cpu_baseline(cfg, n, sample, X=X_h)
+        from oracle import oracle as O
+        cb["ref_local"] = O.build(X_h, X_h[:sample], cb["adjl"], cfg["dim"], cfg["phs"], cfg["deg"], cfg["ops"],
+                                  frame="local")
 
     # ---- equal-error check: every GPU build against the oracle's weights of the sampled
     # stencils, and over all stencils against the plain GPU build
@@ -808,9 +825,13 @@ def main():
         vs_oracle = {"sample_stencils": cb["sample"],
                      "neighbour_lists_equal": bool(np.array_equal(adjl[: cb["sample"]].cpu().numpy(), cb["adjl"])),
                      headline: oracle_errors(torch, W_h[-1], cb["ref"], f_h, ops_last),
-                     "fp64": oracle_errors(torch, W64[-1], cb["ref"], f_h, ops_last)}
+                     "fp64": oracle_errors(torch, W64[-1], cb["ref"], f_h, ops_last),
+                     "local_frame_oracle": {headline: oracle_errors(torch, W_h[-1], cb["ref_local"], f_h, ops_last),
+                                            "fp64": oracle_errors(torch, W64[-1], cb["ref_local"], f_h, ops_last)}}
         if learned_on:
             vs_oracle["fp32_refined"] = oracle_errors(torch, W32[-1], cb["ref"], f_h, ops_last)
+            vs_oracle["local_frame_oracle"]["fp32_refined"] = oracle_errors(torch, W32[-1], cb["ref_local"], f_h,
+                                                                            ops_last)
     del W64, W_h, W32
     # ---- per-stage timings (device-resident, events on the launching stream)
     ms_b_h = timed(lambda: build(headline, Xd, adjl), 3, 1)

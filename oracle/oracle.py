@@ -78,6 +78,8 @@ def lib():
         L.orc_count_rows.argtypes = [i64, ctypes.c_int, P, P, P, P, P]
         L.orc_build.restype = ctypes.c_int
         L.orc_build.argtypes = [P, P, i64, P, i64, P, ctypes.c_int, P, P, P, P, P, P, P, P, ctypes.c_int]
+        L.orc_build_local.restype = ctypes.c_int
+        L.orc_build_local.argtypes = L.orc_build.argtypes
         L.orc_spmm.argtypes = [i64, i64, P, P, P, ctypes.c_int, P, ctypes.c_double, ctypes.c_double, P,
                                ctypes.c_int]
         L.orc_knn_brute.argtypes = [P, i64, P, i64, ctypes.c_int, ctypes.c_int, P, ctypes.c_int]
@@ -250,10 +252,15 @@ class CSR:
     shape: tuple
 
 
-def build(data, eval_points, adjl, dim, phs, poly_deg, ops, hermite=None, nthreads=0):
+def build(data, eval_points, adjl, dim, phs, poly_deg, ops, hermite=None, nthreads=0, frame="raw"):
     """Weights of the operators `ops` on the stencils `adjl` (0-based), sorted rows.
 
     hermite: None or (is_boundary[uint8 per data point], alpha[nb], beta[nb], normals[nb x dim]).
+    frame: "raw" -- the reference's arithmetic (every stencil assembled in the given
+    coordinates, src/solve/assembly.jl:95-222); "local" -- the same formulation assembled per
+    stencil in its local frame (centred at the eval point, scaled by a power of two): the same
+    weights in exact arithmetic, accurate where the raw systems are ill-conditioned (stencils
+    small against their distance from the origin).
     """
     data, eval_points = _f64(data), _f64(eval_points)
     adjl = np.ascontiguousarray(adjl, dtype=np.int32)
@@ -274,8 +281,9 @@ def build(data, eval_points, adjl, dim, phs, poly_deg, ops, hermite=None, nthrea
     col = np.zeros(nnz, dtype=np.int32)
     val = np.zeros(len(ops) * nnz)
     status = np.zeros(ne, dtype=np.int8)
-    lib().orc_build(ctypes.byref(cfg), _p(data), ns, _p(eval_points), ne, _p(adjl), k, _p(isb), _p(al),
-                    _p(be), _p(nr), _p(row_ptr), _p(col), _p(val), _p(status), nthreads)
+    fn = lib().orc_build if frame == "raw" else lib().orc_build_local
+    fn(ctypes.byref(cfg), _p(data), ns, _p(eval_points), ne, _p(adjl), k, _p(isb), _p(al),
+       _p(be), _p(nr), _p(row_ptr), _p(col), _p(val), _p(status), nthreads)
     return CSR(row_ptr, col, val.reshape(len(ops), nnz), status, (ne, ns))
 
 

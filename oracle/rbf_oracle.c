@@ -38,6 +38,15 @@
 #endif
 
 #define AVOID_INF 1.0e-16 /* avoid_inf(Float64), src/RadialBasisFunctions.jl:111 */
+/* The guards of r^b denominators (r^b + avoid_inf).  They are avoid_inf itself in the
+ * reference's (raw) coordinates; the local-frame build (orc_build_local) sets them to
+ * avoid_inf / s^b per stencil, so that every entry of the local system is exactly s^p times
+ * the raw entry, the guards included. */
+static _Thread_local double orc_ai1 = AVOID_INF, orc_ai2 = AVOID_INF, orc_ai3 = AVOID_INF, orc_ai5 = AVOID_INF;
+#define AI_R1 orc_ai1
+#define AI_R2 orc_ai2
+#define AI_R3 orc_ai3
+#define AI_R5 orc_ai5
 #define MAXDIM 3
 #define MAXN 160
 
@@ -80,12 +89,12 @@ double orc_phs_op(int p, int op, int odim, const double *x, const double *xi, in
     double dd = x[odim] - xi[odim];
     switch (p) {
     case 1:
-        if (op == OP_D1) return dd / (r + AVOID_INF);
-        if (op == OP_D2) return (-(dd * dd) + r2) / (pw3(r) + AVOID_INF);
-        return 2.0 / (r + AVOID_INF);
+        if (op == OP_D1) return dd / (r + AI_R1);
+        if (op == OP_D2) return (-(dd * dd) + r2) / (pw3(r) + AI_R3);
+        return 2.0 / (r + AI_R1);
     case 3:
         if (op == OP_D1) return 3.0 * dd * r;
-        if (op == OP_D2) return 3.0 * (r + (dd * dd) / (r + AVOID_INF));
+        if (op == OP_D2) return 3.0 * (r + (dd * dd) / (r + AI_R1));
         return 12.0 * r;
     case 5:
         if (op == OP_D1) return 5.0 * dd * pw3(r);
@@ -112,21 +121,21 @@ double orc_phs_op_normal(int p, int op, int odim, const double *x, const double 
     for (int d = 0; d < dim; d++) dn = dn + n[d] * (x[d] - xi[d]);
     switch (p) {
     case 1:
-        if (op == OP_D1) return -nd / (r + AVOID_INF) + dn * dd / (pw3(r) + AVOID_INF);
+        if (op == OP_D1) return -nd / (r + AI_R1) + dn * dd / (pw3(r) + AI_R3);
         if (op == OP_D2)
-            return (2.0 * nd * dd + dn) / (pw3(r) + AVOID_INF) -
-                   3.0 * (dd * dd) * dn / (pw5(r) + AVOID_INF);
-        return 2.0 * dn / (pw3(r) + AVOID_INF);
+            return (2.0 * nd * dd + dn) / (pw3(r) + AI_R3) -
+                   3.0 * (dd * dd) * dn / (pw5(r) + AI_R5);
+        return 2.0 * dn / (pw3(r) + AI_R3);
     case 3:
-        if (op == OP_D1) return -3.0 * (nd * r + dn * dd / (r + AVOID_INF));
+        if (op == OP_D1) return -3.0 * (nd * r + dn * dd / (r + AI_R1));
         if (op == OP_D2)
-            return -3.0 * (2.0 * dd * nd + dn - dn * (dd * dd) / (r2 + AVOID_INF)) /
-                   (r + AVOID_INF);
-        return -12.0 * dn / (r + AVOID_INF);
+            return -3.0 * (2.0 * dd * nd + dn - dn * (dd * dd) / (r2 + AI_R2)) /
+                   (r + AI_R1);
+        return -12.0 * dn / (r + AI_R1);
     case 5:
         if (op == OP_D1) return -5.0 * (nd * pw3(r) + 3.0 * dn * dd * r);
         if (op == OP_D2)
-            return -5.0 * (6.0 * nd * dd * r + 3.0 * dn * (r + (dd * dd) / (r + AVOID_INF)));
+            return -5.0 * (6.0 * nd * dd * r + 3.0 * dn * (r + (dd * dd) / (r + AI_R1)));
         return -90.0 * dn * r;
     default:
         if (op == OP_D1) return -7.0 * (nd * pw5(r) + 5.0 * pw3(r) * dd * dn);
@@ -142,7 +151,7 @@ void orc_phs_grad(int p, const double *x, const double *xi, int dim, double *g) 
     for (int d = 0; d < dim; d++) {
         double dd = x[d] - xi[d];
         switch (p) {
-        case 1: g[d] = dd / (r + AVOID_INF); break;
+        case 1: g[d] = dd / (r + AI_R1); break;
         case 3: g[d] = 3.0 * dd * r; break;
         case 5: g[d] = 5.0 * dd * pw3(r); break;
         default: g[d] = 7.0 * dd * pw5(r); break;
@@ -159,8 +168,8 @@ void orc_phs_hess(int p, const double *x, const double *xi, int dim, double *h) 
             double delta = (i == j) ? 1.0 : 0.0;
             double v;
             switch (p) {
-            case 1: v = delta / (r + AVOID_INF) - di * dj / (pw3(r) + AVOID_INF); break;
-            case 3: v = 3.0 * (delta * r + di * dj / (r + AVOID_INF)); break;
+            case 1: v = delta / (r + AI_R1) - di * dj / (pw3(r) + AI_R3); break;
+            case 3: v = 3.0 * (delta * r + di * dj / (r + AI_R1)); break;
             case 5: v = 5.0 * (delta * pw3(r) + 3.0 * di * dj * r); break;
             default: v = 7.0 * (delta * pw5(r) + 5.0 * di * dj * pw3(r)); break;
             }
@@ -665,11 +674,49 @@ int64_t orc_count_rows(int64_t ne, int k, const uint8_t *is_boundary, const int3
     return tot;
 }
 
-/* status per eval row: 0 ok, 1 singular, 2 Dirichlet identity row, <0 error (see orc_assemble) */
-int orc_build(const orc_cfg *c, const double *data, int64_t ns, const double *eval, int64_t ne,
-              const int32_t *adjl, int k, const uint8_t *is_boundary, const double *bc_alpha,
-              const double *bc_beta, const double *normals, const int64_t *row_ptr,
-              int32_t *col, double *val, int8_t *status, int nthreads) {
+static int op_order(int op) { return op == OP_IDENT ? 0 : (op == OP_D1 ? 1 : 2); }
+
+/* One stencil in its local frame: X (k points) and x0 already centred at the eval point and
+ * scaled by 2^-es, Neumann/Robin beta by 2^-es, the avoid_inf guards set to avoid_inf / s^b.
+ * The reference formulation is affine invariant except for the eval-node polynomial
+ * right-hand side of a Neumann/Robin eval node (alpha P(x0) + beta dP/dn(x0), not an
+ * operator applied), scaled here by s^q; the weights come back as w_local / s^q (q the
+ * operator's differential order). */
+static int orc_stencil_weights_local(const orc_cfg *c, const double *X, int k, const double *x0,
+                                     const herm_local *h, int es, double *w) {
+    int exps[64 * MAXDIM];
+    int nmon = orc_monomial_exponents(c->dim, c->poly_deg, exps);
+    int n = k + nmon;
+    double *A = (double *)malloc(sizeof(double) * n * n);
+    double *B = (double *)malloc(sizeof(double) * n * c->nops);
+    int ipiv[MAXN];
+    int st = orc_assemble(c, X, k, x0, h, A, B);
+    if (st == 0 && h && h->eval_local >= 0 && h->ptype[h->eval_local] == PT_NR)
+        for (int r = 0; r < c->nops; r++)
+            for (int m = 0; m < nmon; m++) B[r * n + k + m] = ldexp(B[r * n + k + m], es * op_order(c->op_code[r]));
+    if (st == 0) {
+        int info = orc_sytrf_rook_u(n, A, n, ipiv);
+        if (info != 0) st = 1;
+        else {
+            orc_sytrs_rook_u(n, c->nops, A, n, ipiv, B, n);
+            for (int r = 0; r < c->nops; r++)
+                for (int i = 0; i < k; i++) w[r * k + i] = ldexp(B[r * n + i], -es * op_order(c->op_code[r]));
+        }
+    }
+    free(A);
+    free(B);
+    return st;
+}
+
+/* status per eval row: 0 ok, 1 singular, 2 Dirichlet identity row, <0 error (see orc_assemble).
+ * local = 0: the reference's arithmetic (raw coordinates); local = 1: the same formulation
+ * assembled per stencil in its local frame (centred at the eval point, scaled by the power of
+ * two s >= the stencil radius): equal weights in exact arithmetic, far better conditioned
+ * systems where the stencil is small against its distance from the origin. */
+static int orc_build_impl(const orc_cfg *c, const double *data, int64_t ns, const double *eval, int64_t ne,
+                          const int32_t *adjl, int k, const uint8_t *is_boundary, const double *bc_alpha,
+                          const double *bc_beta, const double *normals, const int64_t *row_ptr,
+                          int32_t *col, double *val, int8_t *status, int nthreads, int local) {
     int dim = c->dim;
     int32_t *g2b = NULL;
     if (is_boundary) {
@@ -724,7 +771,31 @@ int orc_build(const orc_cfg *c, const double *data, int64_t ns, const double *ev
             }
             hp = &hl;
         }
-        int st = orc_stencil_weights(c, X, k, x0, hp, w);
+        int st;
+        if (local) {
+            double r2max = 0.0;
+            for (int i = 0; i < k; i++) {
+                double r2 = 0.0;
+                for (int d = 0; d < dim; d++) r2 = r2 + (X[i * dim + d] - x0[d]) * (X[i * dim + d] - x0[d]);
+                if (r2 > r2max) r2max = r2;
+            }
+            int es = 0;
+            if (r2max > 0.0) frexp(sqrt(r2max), &es);
+            for (int i = 0; i < k; i++)
+                for (int d = 0; d < dim; d++) X[i * dim + d] = ldexp(X[i * dim + d] - x0[d], -es);
+            if (hp)
+                for (int i = 0; i < k; i++)
+                    if (hl.ptype[i] == PT_NR) hl.beta[i] = ldexp(hl.beta[i], -es);
+            const double zero[MAXDIM] = {0.0, 0.0, 0.0};
+            orc_ai1 = ldexp(AVOID_INF, -es);
+            orc_ai2 = ldexp(AVOID_INF, -2 * es);
+            orc_ai3 = ldexp(AVOID_INF, -3 * es);
+            orc_ai5 = ldexp(AVOID_INF, -5 * es);
+            st = orc_stencil_weights_local(c, X, k, zero, hp, es, w);
+            orc_ai1 = orc_ai2 = orc_ai3 = orc_ai5 = AVOID_INF;
+        } else {
+            st = orc_stencil_weights(c, X, k, x0, hp, w);
+        }
         status[e] = (int8_t)st;
         if (st != 0) { bad = 1; continue; }
         /* scatter the row sorted by column (sparse() keeps columns sorted) */
@@ -743,6 +814,22 @@ int orc_build(const orc_cfg *c, const double *data, int64_t ns, const double *ev
     }
     free(g2b);
     return bad;
+}
+
+int orc_build(const orc_cfg *c, const double *data, int64_t ns, const double *eval, int64_t ne,
+              const int32_t *adjl, int k, const uint8_t *is_boundary, const double *bc_alpha,
+              const double *bc_beta, const double *normals, const int64_t *row_ptr,
+              int32_t *col, double *val, int8_t *status, int nthreads) {
+    return orc_build_impl(c, data, ns, eval, ne, adjl, k, is_boundary, bc_alpha, bc_beta, normals, row_ptr, col,
+                          val, status, nthreads, 0);
+}
+
+int orc_build_local(const orc_cfg *c, const double *data, int64_t ns, const double *eval, int64_t ne,
+                    const int32_t *adjl, int k, const uint8_t *is_boundary, const double *bc_alpha,
+                    const double *bc_beta, const double *normals, const int64_t *row_ptr,
+                    int32_t *col, double *val, int8_t *status, int nthreads) {
+    return orc_build_impl(c, data, ns, eval, ne, adjl, k, is_boundary, bc_alpha, bc_beta, normals, row_ptr, col,
+                          val, status, nthreads, 1);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -980,7 +1067,7 @@ static void grad_applied(int p, int op, int od, const double *D, int dim, double
     for (int d = 0; d < dim; d++) r2 = r2 + D[d] * D[d];
     const double r = sqrt(r2);
     if (op == OP_IDENT) {
-        const double c = p == 1 ? 1.0 / (r + AVOID_INF) : (p == 3 ? 3.0 * r : (p == 5 ? 5.0 * pw3(r) : 7.0 * pw5(r)));
+        const double c = p == 1 ? 1.0 / (r + AI_R1) : (p == 3 ? 3.0 * r : (p == 5 ? 5.0 * pw3(r) : 7.0 * pw5(r)));
         for (int d = 0; d < dim; d++) g[d] = c * D[d];
         return;
     }
@@ -989,14 +1076,14 @@ static void grad_applied(int p, int op, int od, const double *D, int dim, double
         return;
     }
     if (op == OP_LAP) {
-        const double c = p == 1 ? -2.0 / pw3(r) : (p == 3 ? 12.0 / (r + AVOID_INF) : (p == 5 ? 90.0 * r : 280.0 * pw3(r)));
+        const double c = p == 1 ? -2.0 / pw3(r) : (p == 3 ? 12.0 / (r + AI_R1) : (p == 5 ? 90.0 * r : 280.0 * pw3(r)));
         for (int d = 0; d < dim; d++) g[d] = c * D[d];
         return;
     }
     const double dd = D[od];
     double a, b;
     if (p == 1) { a = -1.0 / pw3(r); b = 1.0 / r; }
-    else if (p == 3) { a = 3.0 / (r + AVOID_INF); b = 3.0 * r; }
+    else if (p == 3) { a = 3.0 / (r + AI_R1); b = 3.0 * r; }
     else if (p == 5) { a = 15.0 * r; b = 5.0 * pw3(r); }
     else { a = 35.0 * pw3(r); b = 7.0 * pw5(r); }
     for (int d = 0; d < dim; d++) g[d] = a * dd * D[d] + (d == od ? b : 0.0);

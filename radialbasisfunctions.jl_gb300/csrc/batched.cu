@@ -12,12 +12,16 @@
 // uses is decided by an autotuner that times both tiles on a sample of the class and
 // caches the choice in the context (rbf_tuning_report prints the table).
 //
-// The per-stencil work is the same as in the one-size kernels (stencil_solve.cuh); the
-// block tile's factorisations are bit-identical to the warp ones.
+// The per-stencil work is that of the one-size kernels: FP64 warp tiles run the
+// Bunch-Kaufman solve of the default plain build (stencil_bk.cuh); FP64 block tiles run a
+// block-cooperative LU, bit-identical to the one-warp LU that the one-size build uses under
+// RBF_FLAG_FP64_LU; the refined tiles' FP32 factorisations are bit-identical between the two
+// tile shapes (stencil_solve.cuh).
 #include <algorithm>
 #include <cstring>
 #include <vector>
 
+#include "stencil_bk.cuh"
 #include "stencil_solve.cuh"
 
 namespace {
@@ -190,7 +194,7 @@ __global__ void __launch_bounds__(kBatchedThreads) build_batched_kernel(const Bi
                 const WarpSmem w = carve(base, P.n, P.k, P.nops);
                 const int64_t e = s_bin.slots[slot];
                 if (s_bin.precision == RBF_PREC_FP64)
-                    solve_fp64_warp(P, e, w, lane);
+                    solve_fp64_bk_warp(P, e, carve_bk(base, P.n, P.k, P.nops), lane);
                 else
                     solve_fp32r_warp(P, e, w, carve32(base, P.n, P.k, P.nops), lane);
             }
@@ -212,8 +216,19 @@ int grid_for(rbf_ctx *ctx, int64_t n) {
 
 }  // namespace
 
+int rbf_build_fp32_launch(rbf_ctx *ctx, const StencilParams &P);
+
+// Classes the split tile serves: FP32-refined 40-row systems with one operator, the sizes of
+// the split-row register kernel (stencil_refined_c.cu).
+static bool split_tile_serves(const BinDesc &b) {
+    return b.precision == RBF_PREC_FP32_REFINED && b.P.n == 40 && b.P.nops == 1;
+}
+
 size_t rbf_batched_region(int n, int k, int nops, int precision) {
-    const size_t b = precision == RBF_PREC_FP64 ? warp_smem_bytes(n, k, nops) : warp_smem_bytes32(n, k, nops);
+    // FP64 warp tiles solve by Bunch-Kaufman on the packed system, block tiles by the LU on the
+    // full one: room for either
+    const size_t b = precision == RBF_PREC_FP64 ? std::max(warp_smem_bytes(n, k, nops), bk_warp_bytes(n, k, nops))
+                                                : warp_smem_bytes32(n, k, nops);
     return (b + 15) & ~(size_t)15;
 }
 
@@ -257,14 +272,29 @@ int rbf_batched_scatter(rbf_ctx *ctx, int64_t ne, const int16_t *d_key, const st
 }
 
 // Runs the persistent kernel over the classes (their item_start fields are filled here).
-int rbf_batched_run(rbf_ctx *ctx, std::vector<BinDesc> &bins) {
+// Runs the persistent kernel over the classes with warp or block tiles (their item_start
+// fields are filled here), then each class with the split tile: the split-row register kernel
+// on the class's stencils and the general refined kernel on the ones it hands over (defer:
+// room for the largest such class's stencil count).
+int rbf_batched_run(rbf_ctx *ctx, std::vector<BinDesc> &bins, int32_t *defer) {
     if (bins.empty()) return RBF_OK;
     int64_t items = 0;
     size_t region = 16;
     for (auto &b : bins) {
         b.item_start = items;
+        if (b.tile == kTileSplit) continue;
         items += b.tile == 0 ? (b.count + 3) / 4 : b.count;
         region = std::max(region, rbf_batched_region(b.P.n, b.P.k, b.P.nops, b.precision));
+    }
+    for (const auto &b : bins) {
+        if (b.tile != kTileSplit || b.count == 0) continue;
+        if (!defer) return rbf_fail(ctx, RBF_ERR_INTERNAL, "split tile without a deferred list");
+        StencilParams Ps = b.P;
+        Ps.slots = b.slots;
+        Ps.nslots = b.count;
+        Ps.defer = defer;
+        RBF_CUDA(ctx, cudaMemsetAsync(&Ps.counters[7], 0, sizeof(unsigned long long), ctx->stream));
+        RBF_TRY(rbf_build_fp32_launch(ctx, Ps));
     }
     if (items == 0) return RBF_OK;
     const size_t smem = 4 * region;
@@ -302,7 +332,7 @@ unsigned long long rbf_tune_key(const BinDesc &b, bool boundary) {
 // trial runs write the real outputs of the sampled stencils (the final run rewrites
 // them) and count into scratch counters.  Classes too small to time get the warp tile
 // below n = 64 and the block tile above.
-int rbf_batched_tune(rbf_ctx *ctx, std::vector<BinDesc> &bins, bool boundary, int tune) {
+int rbf_batched_tune(rbf_ctx *ctx, std::vector<BinDesc> &bins, bool boundary, int tune, int32_t *defer) {
     DevBuf scratch;
     RBF_TRY(scratch.alloc(ctx, sizeof(unsigned long long) * 8 + sizeof(double)));
     for (auto &b : bins) {
@@ -312,25 +342,26 @@ int rbf_batched_tune(rbf_ctx *ctx, std::vector<BinDesc> &bins, bool boundary, in
             b.tile = it->second.tile;
             continue;
         }
+        const bool split_ok = split_tile_serves(b) && defer;
         if (tune == 0 || b.count < 1024) {
-            b.tile = b.P.n > 64 ? 1 : 0;
+            b.tile = split_ok ? kTileSplit : (b.P.n > 64 ? 1 : 0);
             continue;
         }
         rbf_tune_entry ent;
         ent.sample = std::min<int64_t>(b.count, 16384);
-        float ms[2] = {0.f, 0.f};
-        for (int tile = 0; tile < 2; tile++) {
+        float ms[3] = {0.f, 0.f, 0.f};
+        for (int tile = 0; tile < (split_ok ? 3 : 2); tile++) {
             std::vector<BinDesc> one(1, b);
             one[0].count = ent.sample;
             one[0].tile = tile;
             one[0].P.counters = scratch.as<unsigned long long>();
             one[0].P.max_resid = reinterpret_cast<double *>(scratch.as<unsigned long long>() + 8);
-            RBF_TRY(rbf_batched_run(ctx, one));  // warm-up (module load, caches)
+            RBF_TRY(rbf_batched_run(ctx, one, defer));  // warm-up (module load, caches)
             cudaEvent_t e0, e1;
             RBF_CUDA(ctx, cudaEventCreate(&e0));
             RBF_CUDA(ctx, cudaEventCreate(&e1));
             cudaEventRecord(e0, ctx->stream);
-            int st = rbf_batched_run(ctx, one);
+            int st = rbf_batched_run(ctx, one, defer);
             cudaEventRecord(e1, ctx->stream);
             cudaEventSynchronize(e1);
             cudaEventElapsedTime(&ms[tile], e0, e1);
@@ -340,7 +371,9 @@ int rbf_batched_tune(rbf_ctx *ctx, std::vector<BinDesc> &bins, bool boundary, in
         }
         ent.ms_warp = ms[0];
         ent.ms_block = ms[1];
+        ent.ms_split = split_ok ? ms[2] : 0.f;
         ent.tile = ms[1] < ms[0] ? 1 : 0;
+        if (split_ok && ms[2] < ms[ent.tile]) ent.tile = kTileSplit;
         ctx->tune[key] = ent;
         b.tile = ent.tile;
     }

@@ -14,8 +14,8 @@ int rbf_batched_classify(rbf_ctx *ctx, int64_t ne, int dim, const int64_t *d_adj
                          int def_deg, int16_t *d_key, std::vector<unsigned long long> &hist, int *err);
 int rbf_batched_scatter(rbf_ctx *ctx, int64_t ne, const int16_t *d_key, const std::vector<int> &class_of_key,
                         const std::vector<unsigned long long> &class_start, int32_t *d_slots);
-int rbf_batched_tune(rbf_ctx *ctx, std::vector<BinDesc> &bins, bool boundary, int tune);
-int rbf_batched_run(rbf_ctx *ctx, std::vector<BinDesc> &bins);
+int rbf_batched_tune(rbf_ctx *ctx, std::vector<BinDesc> &bins, bool boundary, int tune, int32_t *defer);
+int rbf_batched_run(rbf_ctx *ctx, std::vector<BinDesc> &bins, int32_t *defer);
 
 int rbf_fail(rbf_ctx *ctx, int code, const char *fmt, ...) {
     char buf[1024];
@@ -1016,12 +1016,18 @@ int rbf_build_batched(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data
     RBF_TRY(slots.alloc(ctx, sizeof(int32_t) * (size_t)std::max<int64_t>(ne, 1)));
     RBF_TRY(rbf_batched_scatter(ctx, ne, keys.as<int16_t>(), class_of_key, class_start, slots.as<int32_t>()));
     for (size_t c = 0; c < bins.size(); c++) bins[c].slots = slots.as<int32_t>() + class_start[c];
-    RBF_TRY(rbf_batched_tune(ctx, bins, b.any, tune));
+    // the split tile's deferred list (refined builds): room for the largest class
+    DevBuf defer;
+    int64_t max_class = 0;
+    for (const auto &bn : bins) max_class = std::max<int64_t>(max_class, bn.count);
+    if (cfg->precision == RBF_PREC_FP32_REFINED)
+        RBF_TRY(defer.alloc(ctx, sizeof(int32_t) * (size_t)std::max<int64_t>(max_class, 1)));
+    RBF_TRY(rbf_batched_tune(ctx, bins, b.any, tune, defer.as<int32_t>()));
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
     cudaEventRecord(ev0, ctx->stream);
-    const int st = rbf_batched_run(ctx, bins);
+    const int st = rbf_batched_run(ctx, bins, defer.as<int32_t>());
     cudaEventRecord(ev1, ctx->stream);
     if (st != RBF_OK) {
         cudaEventDestroy(ev0);
@@ -1066,10 +1072,11 @@ int rbf_tuning_report(rbf_ctx *ctx, char *buf, int64_t len) {
         const rbf_tune_entry &t = kv.second;
         snprintf(line, sizeof line,
                  "precision=%s dim=%llu phs=%llu nops=%llu k=%llu degree=%lld boundary=%llu op=%llu: tile=%s "
-                 "(warp %.3f ms, block %.3f ms, sample %lld)\n",
+                 "(warp %.3f ms, block %.3f ms, split %.3f ms, sample %lld)\n",
                  (k & 15) == RBF_PREC_FP64 ? "fp64" : "fp32_refined", (k >> 4) & 15, (k >> 8) & 15, (k >> 12) & 15,
                  (k >> 16) & 255, (long long)((k >> 24) & 15) - 1, (k >> 28) & 1, (k >> 32) & 15,
-                 t.tile ? "block" : "warp", t.ms_warp, t.ms_block, t.sample);
+                 t.tile == kTileSplit ? "split" : (t.tile ? "block" : "warp"), t.ms_warp, t.ms_block, t.ms_split,
+                 t.sample);
         out += line;
     }
     const size_t m = std::min<size_t>(out.size(), (size_t)len - 1);

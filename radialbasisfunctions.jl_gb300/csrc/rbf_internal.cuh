@@ -14,9 +14,12 @@
 constexpr int kRbfBatchKeys = 65 * 8;
 
 // One tuned size class of the batched build: the tile shape chosen and the trial timings.
+// tile 2 of a batched class: the split-row register kernel on the class's stencils (its own launch)
+constexpr int kTileSplit = 2;
+
 struct rbf_tune_entry {
-    int tile = 0;  // 0: one warp per stencil, 1: the whole block on one stencil
-    float ms_warp = 0.f, ms_block = 0.f;
+    int tile = 0;  // 0: one warp per stencil, 1: the whole block on one stencil, 2: split-row kernel
+    float ms_warp = 0.f, ms_block = 0.f, ms_split = 0.f;
     long long sample = 0;
 };
 

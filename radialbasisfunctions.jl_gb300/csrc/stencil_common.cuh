@@ -54,6 +54,8 @@ struct StencilParams {
     const int64_t *adj_ptr;  // ragged adjacency: neighbours of e at adjl[adj_ptr[e] ..], or nullptr
     int32_t *defer;          // FP32 paths: room for ne stencil indices that the split-row kernel
                              // hands to the general kernel (count in counters[7]), or nullptr
+    const int32_t *slots;    // split-row kernel: the stencils to build (nslots of them; a size class
+    int64_t nslots;          // of a batched build), or nullptr: stencils 0 .. ne-1
     // optional sliced-ELL copy of the rows (slices of 32 rows, entry j of row r at
     // sell_off[r / 32] + 32 j + r % 32; operator q's values at sell_val + q * sell_nnz)
     const int64_t *sell_off;

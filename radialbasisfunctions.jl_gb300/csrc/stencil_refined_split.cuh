@@ -192,7 +192,9 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
     const bool xvalid = g < NX;
     const int gx = 32 + (xvalid ? g : 0);  // extra row of this lane's group
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
-    for (int64_t e = (int64_t)blockIdx.x * wpb + wib; e < P.ne; e += nwarps) {
+    const int64_t count = P.slots ? P.nslots : P.ne;
+    for (int64_t t = (int64_t)blockIdx.x * wpb + wib; t < count; t += nwarps) {
+        const int64_t e = P.slots ? (int64_t)P.slots[t] : t;
         // a learned seed is read first so that its latency hides behind the load and assembly
         const float seed_main = (P.seed && lane < P.k) ? __ldg(&P.seed[e * P.k + lane]) : 0.0f;
         const float seed_x = (P.seed && lane < NX && 32 + lane < P.k) ? __ldg(&P.seed[e * P.k + 32 + lane]) : 0.0f;
@@ -449,7 +451,9 @@ int launch_refined_split(rbf_ctx *ctx, const StencilParams &P) {
     RBF_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, build_refined_split_kernel<N>, wpb * 32,
                                                                 smem));
     if (per_sm < 1) per_sm = 1;
-    const int64_t blocks = std::min<int64_t>((P.ne + wpb - 1) / wpb, (int64_t)ctx->num_sms * per_sm);
+    const int64_t count = P.slots ? P.nslots : P.ne;
+    if (count == 0) return RBF_OK;
+    const int64_t blocks = std::min<int64_t>((count + wpb - 1) / wpb, (int64_t)ctx->num_sms * per_sm);
     build_refined_split_kernel<N><<<(unsigned)blocks, wpb * 32, smem, ctx->stream>>>(P, wpb, wb);
     RBF_CHECK_LAUNCH(ctx);
     return RBF_OK;

@@ -193,9 +193,129 @@ def illcond_fixtures():
                         **{f"{nm}__{key}": v for nm, d in out.items() for key, v in d.items()})
 
 
+def _truth_hermite_lap_phs3_2d(P, x0, ptype, alpha, beta, normal, exps):
+    """60-digit weights of the reference's Hermite formulation (src/solve/assembly.jl:251-468)
+    for PHS3 in 2D with the Laplacian, the reference's Laplacian coefficient 12 r: basis
+    columns alpha phi - beta dphi/dn_j at Neumann/Robin points, the symmetric rules of
+    herm_entry for the rows, alpha P + beta dP/dn in the polynomial block, the normal form
+    -12 (n . (x0 - x_i)) / (r + avoid_inf) in the right-hand side."""
+    import mpmath
+    mpmath.mp.dps = 60
+    k = len(P)
+    n = k + len(exps)
+    ai = mpmath.mpf(1e-16)
+    Pm = [[mpmath.mpf(float(v)) for v in p] for p in P]
+    x0m = [mpmath.mpf(float(v)) for v in x0]
+    al = [mpmath.mpf(float(v)) for v in alpha]
+    be = [mpmath.mpf(float(v)) for v in beta]
+    nr = [[mpmath.mpf(float(v)) for v in q] for q in normal]
+    A = mpmath.zeros(n, n)
+    B = mpmath.zeros(n, 1)
+    for i in range(k):
+        for j in range(k):
+            D = [Pm[i][0] - Pm[j][0], Pm[i][1] - Pm[j][1]]
+            r = mpmath.sqrt(D[0] ** 2 + D[1] ** 2)
+            phi = r ** 3
+            g = [3 * r * D[0], 3 * r * D[1]]
+            ti, tj = ptype[i], ptype[j]
+            if ti != 2 and tj != 2:
+                v = phi
+            else:
+                di = nr[i][0] * g[0] + nr[i][1] * g[1]
+                dj = nr[j][0] * g[0] + nr[j][1] * g[1]
+                if ti != 2:
+                    v = al[j] * phi - be[j] * dj
+                elif tj != 2:
+                    v = al[i] * phi + be[i] * di
+                else:
+                    H = [[3 * ((1 if a == b else 0) * r + D[a] * D[b] / (r + ai)) for b in range(2)] for a in range(2)]
+                    d2 = sum(nr[i][a] * sum(H[a][b] * nr[j][b] for b in range(2)) for a in range(2))
+                    v = al[i] * al[j] * phi - al[i] * be[j] * dj + be[i] * al[j] * di + be[i] * be[j] * d2
+            A[i, j] = v
+    for i in range(k):
+        x, y = Pm[i]
+        for m, (ex, ey) in enumerate(exps):
+            pv = x ** ex * y ** ey
+            if ptype[i] == 2:
+                dx = ex * x ** (ex - 1) * y ** ey if ex > 0 else 0
+                dy = ey * x ** ex * y ** (ey - 1) if ey > 0 else 0
+                pv = al[i] * pv + be[i] * (nr[i][0] * dx + nr[i][1] * dy)
+            A[i, k + m] = pv
+            A[k + m, i] = pv
+        D = [x0m[0] - x, x0m[1] - y]
+        r = mpmath.sqrt(D[0] ** 2 + D[1] ** 2)
+        b = 12 * r
+        if ptype[i] == 2:
+            b = al[i] * b + be[i] * (-12 * (nr[i][0] * D[0] + nr[i][1] * D[1]) / (r + ai))
+        B[i] = b
+    x, y = x0m
+    for m, (ex, ey) in enumerate(exps):
+        v = 0
+        if ex >= 2:
+            v += ex * (ex - 1) * x ** (ex - 2) * y ** ey
+        if ey >= 2:
+            v += ey * (ey - 1) * x ** ex * y ** (ey - 2)
+        B[k + m] = v
+    w = mpmath.lu_solve(A, B)
+    return np.array([float(w[i]) for i in range(k)])
+
+
+def disk_hermite_fixtures():
+    """The 2D unit-disk workload at full size (bench.unit_disk: 2M jittered interior points, 5,000
+    boundary points, Dirichlet upper / Neumann lower half-circle; PHS3 degree 3, k = 30): its
+    interior stencils near the circle are small against their distance from the origin, so the
+    reference's raw-coordinate systems are ill-conditioned (condition numbers ~1e13).  The six
+    stencils where the raw-frame oracle and the local-frame oracle differ most, each stored
+    self-contained (points in stencil order, Hermite data), with 60-digit truth weights and the
+    raw-frame oracle's weights (stencil order)."""
+    from oracle import oracle as O
+    import bench
+    X, isb, nrm, al, be = bench.unit_disk(2_000_000, 5_000, 104)
+    adjl = O.knn(X, X, 30)
+    g2b = -np.ones(len(X), dtype=np.int64)
+    g2b[np.nonzero(isb)[0]] = np.arange(int(isb.sum()))
+    cand = np.nonzero((np.sqrt((X ** 2).sum(1)) > 0.985) & ~isb)[0]
+    h = (isb.astype(np.uint8), al, be, nrm)
+    raw = O.build(X, X[cand], adjl[cand], 2, 3, 3, [(O.OP_LAP, 0)], hermite=h)
+    loc = O.build(X, X[cand], adjl[cand], 2, 3, 3, [(O.OP_LAP, 0)], hermite=h, frame="local")
+    rows = np.repeat(np.arange(len(cand)), np.diff(raw.row_ptr))
+    num = np.zeros(len(cand))
+    den = np.zeros(len(cand))
+    np.maximum.at(num, rows, np.abs(raw.val[0] - loc.val[0]))
+    np.maximum.at(den, rows, np.abs(loc.val[0]))
+    pick = cand[np.argsort(-(num / den))[:6]]
+    exps = O.monomial_exponents(2, 3)
+    out = dict(points=[], eval_index=[], ptype=[], alpha=[], beta=[], normal=[], truth=[], oracle_raw=[])
+    for e in pick:
+        ids = adjl[e]
+        assert ids[0] == e  # interior eval point: itself first
+        pt = np.zeros(30, dtype=np.int8)
+        a = np.zeros(30)
+        b = np.zeros(30)
+        nv = np.zeros((30, 2))
+        for i, g in enumerate(ids):
+            if isb[g]:
+                q = g2b[g]
+                pt[i] = 1 if (al[q] == 1 and be[q] == 0) else 2
+                a[i], b[i], nv[i] = al[q], be[q], nrm[q]
+        tw = _truth_hermite_lap_phs3_2d(X[ids], X[e], pt, a, b, nv, exps)
+        r1 = O.build(X, X[e:e + 1], adjl[e:e + 1], 2, 3, 3, [(O.OP_LAP, 0)], hermite=h)
+        inv = np.argsort(np.argsort(ids, kind="stable"), kind="stable")  # column-sorted -> stencil order
+        out["points"].append(X[ids])
+        out["eval_index"].append(e)
+        out["ptype"].append(pt)
+        out["alpha"].append(a)
+        out["beta"].append(b)
+        out["normal"].append(nv)
+        out["truth"].append(tw)
+        out["oracle_raw"].append(r1.val[0][inv])
+    np.savez_compressed(os.path.join(HERE, "disk_hermite_truth.npz"), **{k: np.array(v) for k, v in out.items()})
+
+
 if __name__ == "__main__":
     with open(os.path.join(HERE, "reference_known_answers.json"), "w") as f:
         json.dump(known_answers(), f, indent=1)
     oracle_fixtures()
     illcond_fixtures()
+    disk_hermite_fixtures()
     print("golden fixtures written")

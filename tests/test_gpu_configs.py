@@ -122,3 +122,35 @@ def test_regrid_mixture_32_fields(pkg, orc, precision):
     # degree-1 regrid reproduces a linear field
     lin = 1.0 + src @ np.array([0.3, -1.2, 2.0])
     assert np.abs(W.apply(lin) - (1.0 + tgt @ np.array([0.3, -1.2, 2.0]))).max() < 1e-8
+
+
+@pytest.mark.parametrize("path", ["fp64", "fp64_lu", "fp32_refined", "batched_fp64", "batched_fp32_refined"])
+def test_disk_stencils_where_the_reference_arithmetic_loses_digits(pkg, path):
+    """Six interior stencils of the full-size unit disk (2M points) next to the Neumann half of
+    the circle, where the reference's raw-coordinate systems are ill-conditioned (the raw-frame
+    oracle is 2e-6 .. 1e-5 off the 60-digit truth, tests/golden/disk_hermite_truth.npz).  Each
+    is rebuilt as a 30-point cloud; every GPU path (one-size FP64 by symmetric indefinite and by
+    LU, FP32-refined, the batched launch in both precisions) is within 1e-8 of the truth."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "disk_hermite_truth.npz"))
+    basis = pkg.PHS(3, poly_deg=3)
+    for t in range(len(z["truth"])):
+        P = torch.from_numpy(z["points"][t]).cuda()
+        pt = z["ptype"][t]
+        b = pt > 0
+        herm = dict(is_boundary=b, bc=[pkg.BoundaryCondition(x, y) for x, y in zip(z["alpha"][t][b], z["beta"][t][b])],
+                    normals=z["normal"][t][b])
+        adjl = torch.arange(30, dtype=torch.int32, device="cuda").repeat(30, 1)
+        if path.startswith("batched"):
+            ap, ai = pkg.ragged_stencils(adjl, torch.full((30,), 30, device="cuda"))
+            W = pkg.build_weights_batched([(3, 0)], P, None, ap, ai, basis, hermite=herm,
+                                          precision=path.split("_", 1)[1], tune=0)[0]
+        else:
+            W = pkg.build_weights([(3, 0)], P, None, adjl, basis, hermite=herm,
+                                  precision="fp64" if path.startswith("fp64") else path,
+                                  flags=4 if path == "fp64_lu" else 0)[0]
+        w = W.val[:30].cpu().numpy()  # row 0: the stencil's eval point; columns 0..29 in stencil order
+        assert np.array_equal(W.col[:30].cpu().numpy(), np.arange(30))
+        truth = z["truth"][t]
+        err = np.abs(w - truth).max() / np.abs(truth).max()
+        assert err <= W_TOL, (path, t, err)
