@@ -6,7 +6,9 @@
 // mma.sync m16n8k16.  One 64x64 tile per block of 4 warps (each warp 32x32 = 2 x 4
 // fragments), K staged through shared memory 32 at a time.  Epilogues: + bias, GELU (tanh form, mlp_common.cuh),
 // or multiplication by GELU'(aux) for the backward pass; outputs FP32 and/or bf16.
-// K must be a multiple of 32 and leading dimensions multiples of 8 (inputs are padded).
+// K must be a multiple of 32 and leading dimensions multiples of 8 (inputs are padded).  A
+// GEMM with few output tiles and a long K (the weight gradients, K = batch) splits K over the
+// blocks and sums the slices' tiles in a second, deterministic pass.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -34,7 +36,10 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K, con
                                                         const float *__restrict__ bias, int epi,
                                                         const float *__restrict__ aux, int ldaux,
                                                         float *__restrict__ Cf, int ldcf, __nv_bfloat16 *__restrict__ Cb,
-                                                        int ldcb, float *__restrict__ Zf, int ldz) {
+                                                        int ldcb, float *__restrict__ Zf, int ldz, int kchunk,
+                                                        float *__restrict__ part) {
+    // split K (gridDim.z > 1): this block sums K slice blockIdx.z (kchunk elements) and writes
+    // its raw tile to part[blockIdx.z][M][N]; splitk_reduce_kernel applies the epilogue
     __shared__ __align__(16) __nv_bfloat16 As[BM][BK + SPAD];
     __shared__ __align__(16) __nv_bfloat16 Bs[BN][BK + SPAD];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -49,7 +54,8 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K, con
 #pragma unroll
             for (int t = 0; t < 4; t++) acc[i][j][t] = 0.0f;
 
-    for (int k0 = 0; k0 < K; k0 += BK) {
+    const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+    for (int k0 = kb; k0 < ke; k0 += BK) {
         // 64 rows x 32 bf16 = 256 chunks of 16 B per operand; 2 per thread
 #pragma unroll
         for (int it = 0; it < 2; it++) {
@@ -97,6 +103,10 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K, con
                 const int col = n0 + wn * 32 + ni * 8 + 2 * tig + (t & 1);
                 if (row >= M || col >= N) continue;
                 float z = acc[mi][ni][t];
+                if (part) {
+                    part[((size_t)blockIdx.z * M + row) * N + col] = z;
+                    continue;
+                }
                 if (bias) z += bias[col];
                 if (Zf) Zf[(size_t)row * ldz + col] = z;
                 float o = z;
@@ -105,6 +115,27 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K, con
                 if (Cf) Cf[(size_t)row * ldcf + col] = o;
                 if (Cb) Cb[(size_t)row * ldcb + col] = __float2bfloat16_rn(o);
             }
+}
+
+// Sum of the split-K partial tiles in slice order (deterministic), then the epilogue of
+// gemm_bf16_kernel.
+__global__ void splitk_reduce_kernel(int M, int N, int nsplit, const float *__restrict__ part,
+                                     const float *__restrict__ bias, int epi, const float *__restrict__ aux, int ldaux,
+                                     float *__restrict__ Cf, int ldcf, __nv_bfloat16 *__restrict__ Cb, int ldcb,
+                                     float *__restrict__ Zf, int ldz) {
+    const int64_t total = (int64_t)M * N;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int row = (int)(t / N), col = (int)(t % N);
+        float z = 0.0f;
+        for (int sp = 0; sp < nsplit; sp++) z += part[(size_t)sp * total + t];
+        if (bias) z += bias[col];
+        if (Zf) Zf[(size_t)row * ldz + col] = z;
+        float o = z;
+        if (epi == EPI_GELU) o = gelu(z);
+        else if (epi == EPI_GELU_GRAD) o = z * gelu_grad(aux[(size_t)row * ldaux + col]);
+        if (Cf) Cf[(size_t)row * ldcf + col] = o;
+        if (Cb) Cb[(size_t)row * ldcb + col] = __float2bfloat16_rn(o);
+    }
 }
 
 __global__ void transpose_bf16_kernel(int rows, int cols, const __nv_bfloat16 *__restrict__ in, int ldi,
@@ -197,8 +228,31 @@ int rbf_mlp_gemm(rbf_ctx *ctx, int32_t M, int32_t N, int32_t K, const void *A, i
     if (epi == EPI_GELU_GRAD && !aux) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "gemm: GELU-gradient epilogue needs aux");
     if (M == 0 || N == 0) return RBF_OK;
     dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+    // few output tiles over a long K (the weight gradients: K = batch): split K so that the
+    // GEMM fills the GPU (about two blocks per SM), slices of at least 128
+    const int tiles = (int)(grid.x * grid.y);
+    int nsplit = 1, kchunk = K;
+    if (2 * tiles < ctx->num_sms && K >= 256) {
+        nsplit = std::min(K / 128, (2 * ctx->num_sms + tiles - 1) / tiles);
+        kchunk = ((K + nsplit - 1) / nsplit + BK - 1) / BK * BK;
+        nsplit = (K + kchunk - 1) / kchunk;
+    }
+    if (nsplit <= 1) {
+        gemm_bf16_kernel<<<grid, 128, 0, ctx->stream>>>(M, N, K, (const __nv_bfloat16 *)A, lda, (const __nv_bfloat16 *)B,
+                                                         ldb, bias, epi, aux, ldaux, Cf, ldcf, (__nv_bfloat16 *)Cb, ldcb,
+                                                         Zf, ldz, K, nullptr);
+        RBF_CHECK_LAUNCH(ctx);
+        return RBF_OK;
+    }
+    DevBuf part;
+    RBF_TRY(part.alloc(ctx, sizeof(float) * (size_t)nsplit * M * N));
+    grid.z = nsplit;
     gemm_bf16_kernel<<<grid, 128, 0, ctx->stream>>>(M, N, K, (const __nv_bfloat16 *)A, lda, (const __nv_bfloat16 *)B, ldb,
-                                                     bias, epi, aux, ldaux, Cf, ldcf, (__nv_bfloat16 *)Cb, ldcb, Zf, ldz);
+                                                     nullptr, 0, nullptr, 0, nullptr, 0, nullptr, 0, nullptr, 0, kchunk,
+                                                     part.as<float>());
+    RBF_CHECK_LAUNCH(ctx);
+    splitk_reduce_kernel<<<grid1d(ctx, (int64_t)M * N), 256, 0, ctx->stream>>>(
+        M, N, nsplit, part.as<float>(), bias, epi, aux, ldaux, Cf, ldcf, (__nv_bfloat16 *)Cb, ldcb, Zf, ldz);
     RBF_CHECK_LAUNCH(ctx);
     return RBF_OK;
 }
