@@ -55,9 +55,10 @@ PEAKS = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.ex
 
 # DRAM bytes (read + write) per stencil of the headline build kernel: constants from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on a 1,000,000-point
-# case of this workload (`python bench.py --case build_learned --n 1000000` under ncu), scaled by
-# the stencil count (the kernel's traffic grows in proportion).  None: not captured.
-KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": None, "learned": None}
+# case of this workload (`python bench.py --case build_refined --n 1000000` and `--case
+# build_learned` under ncu), scaled by the stencil count (the kernel's traffic grows in
+# proportion).  None: not captured.
+KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": 479.6, "learned": None}
 
 
 def peaks_bf16():
