@@ -496,6 +496,24 @@ def all_configs(pkg, torch, ctx, stream, cpu=True):
             line.update(extra)
         print(json.dumps(line), flush=True)
 
+    def aug_errors(W, rows, rp, col, val, f):
+        """GPU rows `rows` of a normal-derivative build against the oracle's (rp, col, val):
+        structure, max / RMS row-relative weight error, and the rows applied to f = [u; du/dn]."""
+        grp, gcol, gval = W.row_ptr.cpu().numpy(), W.col.cpu().numpy(), W.val.cpu().numpy()
+        rel, y, yr = [], [], []
+        for t, e in enumerate(rows):
+            c, v = gcol[grp[e]:grp[e + 1]], gval[grp[e]:grp[e + 1]]
+            cr, vr = col[rp[t]:rp[t + 1]], val[rp[t]:rp[t + 1]]
+            if not np.array_equal(c, cr):
+                return {"structure_equal": False}
+            rel.append(np.abs(v - vr).max() / np.abs(vr).max())
+            y.append(v @ f[c])
+            yr.append(vr @ f[cr])
+        rel, y, yr = np.array(rel), np.array(y), np.array(yr)
+        return {"structure_equal": True, "max_row_rel_weight_err": float(rel.max()),
+                "rms_row_rel_weight_err": float(np.sqrt((rel ** 2).mean())),
+                "operator_on_test_function_rel_err": float(np.abs(y - yr).max() / np.abs(yr).max())}
+
     def stats_of(st):
         return {"fallback_stencils": int(st.n_fallback),
                 "residuals_per_stencil": float(st.n_residuals) / max(1, int(st.n_stencils))}
@@ -568,6 +586,36 @@ def all_configs(pkg, torch, ctx, stream, cpu=True):
            "Neumann lower half-circle), PHS3 degree 3, k = 30 (40 x 40, Hermite rows on boundary stencils), one "
            "persistent batched launch with autotuned tiles", len(Xh), ms_knn, builds, "all stencils", W32, 1,
            kernel_ms(lambda: W32.apply(ud)))
+    # the same disk with du/dn unknowns at the Neumann points (RBF_FLAG_NORMAL_DOF): boundary-
+    # adjacent stencils solve 40 + m systems, m their Neumann neighbours, all in one launch
+    nd_run = lambda prec: pkg.build_weights_batched([(3, 0)], X, None, ap, ai, b, hermite=herm, precision=prec,
+                                                    tune=1, ctx=ctx, stats=st, normal_dof=True)[0]
+    ms64, W64 = ev_ms(lambda: nd_run("fp64"))
+    ms32, W32 = ev_ms(lambda: nd_run("fp32_refined"))
+    s32 = stats_of(st)
+    ah = a.cpu().numpy()
+    bidx = np.nonzero(isb)[0]
+    nr_pt = np.zeros(len(Xh), bool)
+    nr_pt[bidx[be != 0.0]] = True
+    dir_pt = np.zeros(len(Xh), bool)
+    dir_pt[bidx[be == 0.0]] = True
+    m_of = np.where(dir_pt, 0, nr_pt[ah].sum(1))
+    sizes = np.bincount(30 + 10 + m_of[~dir_pt])
+    builds = {"fp64": {"ms_build": ms64}, "fp32_refined": {"ms_build": ms32, **s32}}
+    if cpu:
+        from oracle import augmented_oracle as A
+        rows = np.concatenate([np.nonzero(m_of > 0)[0][::3][:1500], np.nonzero((m_of == 0) & ~dir_pt)[0][:500]])
+        rp, col, val = A.build_augmented(Xh, ah, 2, 3, 3, [(3, 0)], (isb, al, be, nrm), rows=rows)
+        dudn = (2.0 * Xh[bidx] * nrm).sum(1)
+        fa = np.concatenate([u, dudn])
+        for nm, Wx in (("fp64", W64), ("fp32_refined", W32)):
+            builds[nm]["vs_oracle"] = {"normal_dof_oracle": aug_errors(Wx, rows, rp, col, val[0], fa)}
+    report("disk_hermite_normal_dof_2M", f"the 2D unit disk above with u and du/dn unknowns at the Neumann points "
+           "(Hermite-Birkhoff stencils, RBF_FLAG_NORMAL_DOF): boundary-adjacent systems of 40 + m, m the stencil's "
+           "Neumann neighbours, all sizes in one persistent launch", len(Xh), ms_knn, builds,
+           "1,500 stencils with Neumann neighbours and 500 interior ones (oracle/augmented_oracle.py)", W32, 1,
+           kernel_ms(lambda: W32.apply(torch.from_numpy(np.concatenate([u, np.zeros(len(bidx))])).to(dev))),
+           {"system_sizes": {int(n): int(c) for n, c in enumerate(sizes) if c}})
     del W64, W32, a, ap, ai, X
     # ---- C5: 3D regrid, 8,000,000 uniform sources onto 8,000,000 mixture targets, PHS3 degree 1, k = 20,
     # 32 fields; the learned form with a surrogate trained on 2,000,000 regrid stencils

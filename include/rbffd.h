@@ -92,6 +92,21 @@ typedef struct rbf_build_cfg {
 #define RBF_FLAG_FP64_LU 4        /* RBF_PREC_FP64 in rbf_build: solve by LU with partial pivoting
                                      (the batched build's solver, bit-identical to it) instead of
                                      the default symmetric indefinite (Bunch-Kaufman) LDL^T */
+#define RBF_FLAG_NORMAL_DOF 8     /* rbf_build_batched with a Hermite boundary: the augmented
+                                     (Hermite-Birkhoff) formulation, no counterpart in the
+                                     reference.  Every Neumann/Robin stencil point carries two
+                                     unknowns, u and du/dn (outward normal): the system of a
+                                     stencil with m such neighbours is k + m + nmon.  Rows: a
+                                     Dirichlet eval point keeps its identity row; every other row
+                                     holds the operator's weights on u at its k points (columns =
+                                     data indices) and on du/dn at its m Neumann/Robin points
+                                     (column ns + b, b the point's boundary ordinal), k + m
+                                     entries, columns ascending.  The operator has ns + nb
+                                     columns: apply it to [u; du/dn at the boundary points].
+                                     Neumann/Robin eval points take the operator itself (not the
+                                     boundary condition).  PHS 3, 5 and 7 (r has no normal
+                                     derivative at r = 0).  Row layout from
+                                     rbf_build_count_normal_dof. */
 
 /* Hermite boundary description (src/solve/types.jl:18-42,178-182).  Boundary
  * conditions are B u = alpha*u + beta*du/dn; Dirichlet is (1,0), Neumann (0,1).
@@ -353,6 +368,12 @@ int rbf_reorder_points(rbf_ctx *ctx, const double *data, int64_t n, int32_t dim,
  * them (Dirichlet eval rows hold 1 entry, every other row its stencil's length). */
 int rbf_build_count_ragged(rbf_ctx *ctx, int64_t ns, int64_t ne, const int64_t *adj_ptr,
                            const rbf_hermite *herm, int64_t *row_ptr_out, int64_t *nnz_out);
+/* Row layout of a RBF_FLAG_NORMAL_DOF build of ragged stencils: a Dirichlet eval row holds
+ * 1 entry, every other row its stencil's length plus the number of its Neumann/Robin
+ * neighbours (their du/dn columns). */
+int rbf_build_count_normal_dof(rbf_ctx *ctx, int64_t ns, int64_t ne, const int64_t *adj_ptr,
+                               const int32_t *adj_idx, const rbf_hermite *herm, int64_t *row_ptr_out,
+                               int64_t *nnz_out);
 /* Builds every stencil of a ragged batch in one persistent launch.  Stencils are binned
  * by size class (stencil length k, polynomial degree: system size n = k + nmon) and each
  * class runs with the tile shape the autotuner chose for it: one warp per stencil, or the

@@ -922,12 +922,18 @@ def ragged_stencils(adjl, k_per):
 
 def build_weights_batched(ops, data, eval_points, adj_ptr, adj_idx, basis, hermite=None, precision="fp64", *,
                           poly_deg=None, tune=1, ctx=None, refine_steps=0, tol=0.0, return_status=False,
-                          stats=None, flags=0):
+                          stats=None, flags=0, normal_dof=False):
     """Weights of `ops` on ragged stencils (the neighbours of eval point e are
     adj_idx[adj_ptr[e]:adj_ptr[e+1]]), with an optional polynomial degree per stencil
     (poly_deg, int8 array; basis.poly_deg otherwise), all in one persistent launch binned by
     system size with autotuned tile shapes (tune: 0 cached/heuristic, 1 tune new classes,
-    2 re-tune).  Returns a list of WeightsCSR like build_weights."""
+    2 re-tune).  Returns a list of WeightsCSR like build_weights.
+
+    normal_dof (with a Hermite boundary; no counterpart in the reference): every
+    Neumann/Robin stencil point carries u and du/dn as unknowns, so a stencil with m such
+    neighbours solves a (k + m + nmon) system (binned by that size).  The operators then
+    have ns + nb columns, applied to [u; du/dn at the boundary points in boundary order];
+    Dirichlet eval rows stay identity rows and every other row takes the operator itself."""
     torch = _torch()
     d = _points(data)
     q = d if eval_points is None else _points(eval_points, "eval_points")
@@ -956,16 +962,23 @@ def build_weights_batched(ops, data, eval_points, adj_ptr, adj_idx, basis, hermi
     cfg.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     cfg.refine_steps = refine_steps
     cfg.tol = tol
-    cfg.flags = flags
+    cfg.flags = flags | (_native.FLAG_NORMAL_DOF if normal_dof else 0)
     herm = _hermite_arrays(hermite, ns, dim)
     hs = None
+    nb = 0
     if herm is not None:
         isb, al, be, nr = herm
         hs = _native.Hermite(isb.ctypes.data, al.ctypes.data, be.ctypes.data, nr.ctypes.data, len(al))
+        nb = len(al)
     row_ptr = torch.empty(ne + 1, dtype=torch.int64, device=dev)
     nnz = ctypes.c_int64(0)
-    ctx.check(ctx.lib.rbf_build_count_ragged(ctx.h, ns, ne, _ptr(ap), ctypes.byref(hs) if hs else None,
-                                             _ptr(row_ptr), ctypes.byref(nnz)))
+    if normal_dof:
+        ctx.check(ctx.lib.rbf_build_count_normal_dof(ctx.h, ns, ne, _ptr(ap), _ptr(ai),
+                                                     ctypes.byref(hs) if hs else None, _ptr(row_ptr),
+                                                     ctypes.byref(nnz)))
+    else:
+        ctx.check(ctx.lib.rbf_build_count_ragged(ctx.h, ns, ne, _ptr(ap), ctypes.byref(hs) if hs else None,
+                                                 _ptr(row_ptr), ctypes.byref(nnz)))
     col = torch.empty(nnz.value, dtype=torch.int32, device=dev)
     val = torch.empty((len(ops), nnz.value), dtype=torch.float64, device=dev)
     status = torch.empty(ne, dtype=torch.int8, device=dev) if return_status else None
@@ -973,7 +986,8 @@ def build_weights_batched(ops, data, eval_points, adj_ptr, adj_idx, basis, hermi
     ctx.check(ctx.lib.rbf_build_batched(ctx.h, ctypes.byref(cfg), _ptr(d), ns, _ptr(q), ne, _ptr(ap), _ptr(ai),
                                         _ptr(pd), ctypes.byref(hs) if hs else None, _ptr(row_ptr), _ptr(col),
                                         _ptr(val), _ptr(status), ctypes.byref(st), int(tune)))
-    Ws = [WeightsCSR(row_ptr, col, val[i], (ne, ns), ctx) for i in range(len(ops))]
+    ncols = ns + nb if normal_dof else ns
+    Ws = [WeightsCSR(row_ptr, col, val[i], (ne, ncols), ctx) for i in range(len(ops))]
     if return_status:
         return Ws, status
     return Ws

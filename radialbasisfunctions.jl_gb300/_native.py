@@ -77,6 +77,11 @@ def build_library(force: bool = False, verbose: bool = False, extra_flags=()) ->
 
 # ---------------------------------------------------------------------- C structs
 RBF_MAX_OPS = 8
+# rbf_build_cfg.flags bits (include/rbffd.h)
+FLAG_STENCIL_ORDER = 1
+FLAG_LOCAL_UNITS = 2
+FLAG_FP64_LU = 4
+FLAG_NORMAL_DOF = 8
 
 
 class BuildCfg(ctypes.Structure):
@@ -137,6 +142,7 @@ SIGNATURES = {
     "rbf_mlp_gemm": (_I, [_P, _I32, _I32, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32, _P, _I32]),
     "rbf_mlp_transpose": (_I, [_P, _I32, _I32, _P, _I32, _P, _I32]),
     "rbf_build_count_ragged": (_I, [_P, _I64, _I64, _P, _P, _P, _P]),
+    "rbf_build_count_normal_dof": (_I, [_P, _I64, _I64, _P, _P, _P, _P, _P]),
     "rbf_build_batched": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I32]),
     "rbf_tuning_report": (_I, [_P, ctypes.c_char_p, _I64]),
     "rbf_plan_create": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _I32, _P, _P, _P, _I32, _P, _P, _P]),

@@ -26,9 +26,9 @@
 
 namespace {
 
-constexpr int kKeys = kRbfBatchKeys;  // class key = k * 8 + (degree + 1), k <= 64, degree <= 6
+constexpr int kKeys = kRbfBatchKeys;  // (m * 65 + k) * 8 + (degree + 1)
 
-__device__ __forceinline__ int nmon_of(int dim, int deg) {
+__device__ int nmon_of(int dim, int deg) {
     if (deg < 0) return 0;
     // binomial(dim + deg, dim)
     int r = 1;
@@ -38,9 +38,19 @@ __device__ __forceinline__ int nmon_of(int dim, int deg) {
 
 // Class key of every stencil and the class histogram; err: bit 0 stencil size out of
 // range, bit 1 system too large, bit 2 degree out of range, bit 3 adj_ptr not monotone.
+// nd (RBF_FLAG_NORMAL_DOF builds, else null adj_idx): m, the stencil's Neumann/Robin
+// neighbours, enters the key; Dirichlet eval stencils (identity rows) count none.
+struct NormalDofView {
+    const int32_t *adj_idx;
+    const uint8_t *isb;
+    const int32_t *g2b;
+    const double *alpha, *beta;
+};
+
 __global__ void classify_kernel(int64_t ne, int dim, const int64_t *__restrict__ adj_ptr,
-                                const int8_t *__restrict__ degs, int def_deg, int16_t *__restrict__ key,
-                                unsigned long long *__restrict__ hist, int *__restrict__ err) {
+                                const int8_t *__restrict__ degs, int def_deg, NormalDofView nd,
+                                int32_t *__restrict__ key, unsigned long long *__restrict__ hist,
+                                int *__restrict__ err) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t len = adj_ptr[e + 1] - adj_ptr[e];
         const int deg = degs ? (int)degs[e] : def_deg;
@@ -48,20 +58,28 @@ __global__ void classify_kernel(int64_t ne, int dim, const int64_t *__restrict__
         if (len < 0) bad |= 8;
         if (len < 1 || len > RBF_MAX_STENCIL) bad |= 1;
         if (deg < -1 || deg > 6) bad |= 4;
-        if (!bad && len + nmon_of(dim, deg) > RBF_MAX_SYSTEM) bad |= 2;
+        int m = 0;
+        if (!bad && nd.adj_idx && nd.isb &&
+            !(nd.isb[e] && nd.alpha[nd.g2b[e]] == 1.0 && nd.beta[nd.g2b[e]] == 0.0)) {
+            for (int64_t t = adj_ptr[e]; t < adj_ptr[e + 1]; t++) {
+                const int32_t g = nd.adj_idx[t];
+                if (nd.isb[g]) m += !(nd.alpha[nd.g2b[g]] == 1.0 && nd.beta[nd.g2b[g]] == 0.0);
+            }
+        }
+        if (!bad && len + m + nmon_of(dim, deg) > RBF_MAX_SYSTEM) bad |= 2;
         if (bad) {
             atomicOr(err, bad);
             key[e] = -1;
             continue;
         }
-        const int kk = (int)len * 8 + deg + 1;
-        key[e] = (int16_t)kk;
+        const int kk = (m * 65 + (int)len) * 8 + deg + 1;
+        key[e] = kk;
         atomicAdd(&hist[kk], 1ull);
     }
 }
 
 // Counting-sort scatter of the stencils into their class's slot range.
-__global__ void scatter_slots_kernel(int64_t ne, const int16_t *__restrict__ key, const int *__restrict__ class_of_key,
+__global__ void scatter_slots_kernel(int64_t ne, const int32_t *__restrict__ key, const int *__restrict__ class_of_key,
                                      unsigned long long *__restrict__ cursor, int32_t *__restrict__ slots) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
         const int kk = key[e];
@@ -218,10 +236,10 @@ int grid_for(rbf_ctx *ctx, int64_t n) {
 
 int rbf_build_fp32_launch(rbf_ctx *ctx, const StencilParams &P);
 
-// Classes the split tile serves: FP32-refined 40-row systems with one operator, the sizes of
-// the split-row register kernel (stencil_refined_c.cu).
+// Classes the split tile serves: FP32-refined 40-row systems with one operator and no
+// normal-derivative unknowns, the sizes of the split-row register kernel (stencil_refined_c.cu).
 static bool split_tile_serves(const BinDesc &b) {
-    return b.precision == RBF_PREC_FP32_REFINED && b.P.n == 40 && b.P.nops == 1;
+    return b.precision == RBF_PREC_FP32_REFINED && b.P.n == 40 && b.P.nops == 1 && b.P.nnr == 0;
 }
 
 size_t rbf_batched_region(int n, int k, int nops, int precision) {
@@ -233,7 +251,10 @@ size_t rbf_batched_region(int n, int k, int nops, int precision) {
 }
 
 int rbf_batched_classify(rbf_ctx *ctx, int64_t ne, int dim, const int64_t *d_adj_ptr, const int8_t *d_degs,
-                         int def_deg, int16_t *d_key, std::vector<unsigned long long> &hist, int *err) {
+                         int def_deg, const StencilParams *nd, int32_t *d_key, std::vector<unsigned long long> &hist,
+                         int *err) {
+    NormalDofView v{nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (nd && nd->isb) v = NormalDofView{nd->adjl, nd->isb, nd->g2b, nd->alpha, nd->beta};
     hist.assign(kKeys, 0ull);
     DevBuf dh, de;
     RBF_TRY(dh.alloc(ctx, sizeof(unsigned long long) * kKeys));
@@ -241,7 +262,7 @@ int rbf_batched_classify(rbf_ctx *ctx, int64_t ne, int dim, const int64_t *d_adj
     RBF_CUDA(ctx, cudaMemsetAsync(dh.ptr, 0, sizeof(unsigned long long) * kKeys, ctx->stream));
     RBF_CUDA(ctx, cudaMemsetAsync(de.ptr, 0, sizeof(int), ctx->stream));
     if (ne > 0) {
-        classify_kernel<<<grid_for(ctx, ne), 256, 0, ctx->stream>>>(ne, dim, d_adj_ptr, d_degs, def_deg, d_key,
+        classify_kernel<<<grid_for(ctx, ne), 256, 0, ctx->stream>>>(ne, dim, d_adj_ptr, d_degs, def_deg, v, d_key,
                                                                     dh.as<unsigned long long>(), de.as<int>());
         RBF_CHECK_LAUNCH(ctx);
     }
@@ -252,7 +273,7 @@ int rbf_batched_classify(rbf_ctx *ctx, int64_t ne, int dim, const int64_t *d_adj
     return RBF_OK;
 }
 
-int rbf_batched_scatter(rbf_ctx *ctx, int64_t ne, const int16_t *d_key, const std::vector<int> &class_of_key,
+int rbf_batched_scatter(rbf_ctx *ctx, int64_t ne, const int32_t *d_key, const std::vector<int> &class_of_key,
                         const std::vector<unsigned long long> &class_start, int32_t *d_slots) {
     DevBuf dmap, dcur;
     RBF_TRY(dmap.alloc(ctx, sizeof(int) * kKeys));
@@ -324,7 +345,7 @@ unsigned long long rbf_tune_key(const BinDesc &b, bool boundary) {
     return (unsigned long long)b.precision | ((unsigned long long)P.dim << 4) | ((unsigned long long)P.phs << 8) |
            ((unsigned long long)P.nops << 12) | ((unsigned long long)P.k << 16) |
            ((unsigned long long)(P.poly_deg + 1) << 24) | ((unsigned long long)boundary << 28) |
-           ((unsigned long long)P.op_code[0] << 32);
+           ((unsigned long long)P.op_code[0] << 32) | ((unsigned long long)P.nnr << 40);
 }
 
 // Chooses each class's tile: a cached choice, or (tune >= 1) the faster of the two tiles

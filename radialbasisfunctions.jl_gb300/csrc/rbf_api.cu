@@ -11,8 +11,9 @@
 int rbf_build_fp64_launch(rbf_ctx *ctx, const StencilParams &P);
 int rbf_build_fp32_launch(rbf_ctx *ctx, const StencilParams &P);
 int rbf_batched_classify(rbf_ctx *ctx, int64_t ne, int dim, const int64_t *d_adj_ptr, const int8_t *d_degs,
-                         int def_deg, int16_t *d_key, std::vector<unsigned long long> &hist, int *err);
-int rbf_batched_scatter(rbf_ctx *ctx, int64_t ne, const int16_t *d_key, const std::vector<int> &class_of_key,
+                         int def_deg, const StencilParams *nd, int32_t *d_key, std::vector<unsigned long long> &hist,
+                         int *err);
+int rbf_batched_scatter(rbf_ctx *ctx, int64_t ne, const int32_t *d_key, const std::vector<int> &class_of_key,
                         const std::vector<unsigned long long> &class_start, int32_t *d_slots);
 int rbf_batched_tune(rbf_ctx *ctx, std::vector<BinDesc> &bins, bool boundary, int tune, int32_t *defer);
 int rbf_batched_run(rbf_ctx *ctx, std::vector<BinDesc> &bins, int32_t *defer);
@@ -201,6 +202,8 @@ int bind_boundary(rbf_ctx *ctx, const rbf_hermite *h, int64_t ns, int dim, Bound
 // Basis, operator and precision fields of P for a plan (P.k set by the caller).
 int rbf_plan_params(rbf_ctx *ctx, const rbf_build_cfg *cfg, StencilParams &P) {
     const int dim = cfg->dim;
+    if (cfg->flags & RBF_FLAG_NORMAL_DOF)
+        return rbf_fail(ctx, RBF_ERR_UNSUPPORTED, "normal-derivative unknowns are built by rbf_build_batched");
     if (dim < 1 || dim > 3) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "dim must be 1, 2 or 3 (got %d)", dim);
     if (!(cfg->phs == 1 || cfg->phs == 3 || cfg->phs == 5 || cfg->phs == 7))
         return rbf_fail(ctx, RBF_ERR_ARGUMENT, "n must be 1, 3, 5, or 7 (got n=%d)", cfg->phs);
@@ -333,6 +336,8 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
               int32_t *col, double *val, int8_t *status_out, rbf_build_stats *stats) {
     RBF_TRY(check_ctx(ctx));
     if (!cfg) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null configuration");
+    if (cfg->flags & RBF_FLAG_NORMAL_DOF)
+        return rbf_fail(ctx, RBF_ERR_UNSUPPORTED, "normal-derivative unknowns are built by rbf_build_batched");
     const int dim = cfg->dim;
     if (dim < 1 || dim > 3) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "dim must be 1, 2 or 3 (got %d)", dim);
     if (!(cfg->phs == 1 || cfg->phs == 3 || cfg->phs == 5 || cfg->phs == 7))
@@ -895,6 +900,40 @@ int rbf_build_count_ragged(rbf_ctx *ctx, int64_t ns, int64_t ne, const int64_t *
     return RBF_OK;
 }
 
+int rbf_build_count_normal_dof(rbf_ctx *ctx, int64_t ns, int64_t ne, const int64_t *adj_ptr, const int32_t *adj_idx,
+                               const rbf_hermite *herm, int64_t *row_ptr_out, int64_t *nnz_out) {
+    RBF_TRY(check_ctx(ctx));
+    if (ne < 0 || ns < 1 || !adj_ptr || !adj_idx)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid sizes or null adjacency");
+    if (herm && herm->is_boundary && ne > ns)
+        return rbf_fail(ctx, RBF_ERR_DIMENSION, "Hermite builds evaluate at the data points (ne <= ns)");
+    BoundaryDev b;
+    RBF_TRY(bind_boundary(ctx, herm, ns, 1, b));
+    InArray ap, ai;
+    RBF_TRY(ap.bind(ctx, adj_ptr, sizeof(int64_t) * (ne + 1)));
+    int64_t ends[2] = {0, 0};
+    RBF_CUDA(ctx, cudaMemcpyAsync(&ends[0], ap.as<int64_t>(), sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaMemcpyAsync(&ends[1], ap.as<int64_t>() + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ends[0] != 0 || ends[1] < 0 || ends[1] > (int64_t)RBF_MAX_STENCIL * ne)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "adj_ptr must start at 0 and hold at most %d neighbours per stencil",
+                        RBF_MAX_STENCIL);
+    RBF_TRY(ai.bind(ctx, adj_idx, sizeof(int32_t) * ends[1]));
+    bool idx_ok = true;
+    RBF_TRY(rbf_check_indices(ctx, ai.as<int32_t>(), ends[1], (int32_t)ns, &idx_ok));
+    if (!idx_ok) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "adj_idx holds indices outside [0, %lld)", (long long)ns);
+    OutArray rp;
+    RBF_TRY(rp.bind(ctx, row_ptr_out, sizeof(int64_t) * (ne + 1)));
+    int64_t nnz = 0;
+    RBF_TRY(rbf_count_rows_device(ctx, ne, 0, b.any ? b.isb.as<uint8_t>() : nullptr, b.any ? b.g2b.as<int32_t>() : nullptr,
+                                  b.any ? b.alpha.as<double>() : nullptr, b.any ? b.beta.as<double>() : nullptr,
+                                  rp.as<int64_t>(), &nnz, ap.as<int64_t>(), ai.as<int32_t>()));
+    RBF_TRY(rp.finish(ctx));
+    RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (nnz_out) *nnz_out = nnz;
+    return RBF_OK;
+}
+
 int rbf_build_batched(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns, const double *eval,
                       int64_t ne, const int64_t *adj_ptr, const int32_t *adj_idx, const int8_t *poly_deg_per,
                       const rbf_hermite *herm, const int64_t *row_ptr, int32_t *col, double *val, int8_t *status_out,
@@ -942,22 +981,37 @@ int rbf_build_batched(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data
     bool idx_ok = true;
     RBF_TRY(rbf_check_indices(ctx, ai.as<int32_t>(), ends[1], (int32_t)ns, &idx_ok));
     if (!idx_ok) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "adj_idx holds indices outside [0, %lld)", (long long)ns);
-    // size classes
+    const bool normal_dof = (cfg->flags & RBF_FLAG_NORMAL_DOF) != 0;
+    if (normal_dof && ns + b.nb >= INT32_MAX)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "data points + boundary points must be < 2^31");
+    if (normal_dof && b.any_nr && cfg->phs == 1)
+        return rbf_fail(ctx, RBF_ERR_UNSUPPORTED,
+                        "normal-derivative unknowns need PHS 3, 5 or 7 (r has no normal derivative at r = 0)");
+    // size classes (with normal-derivative unknowns: their number m is part of the class)
+    StencilParams nd;
+    memset(&nd, 0, sizeof nd);
+    nd.adjl = ai.as<int32_t>();
+    nd.isb = b.any ? b.isb.as<uint8_t>() : nullptr;
+    nd.g2b = b.any ? b.g2b.as<int32_t>() : nullptr;
+    nd.alpha = b.any ? b.alpha.as<double>() : nullptr;
+    nd.beta = b.any ? b.beta.as<double>() : nullptr;
     DevBuf keys;
-    RBF_TRY(keys.alloc(ctx, sizeof(int16_t) * (size_t)std::max<int64_t>(ne, 1)));
+    RBF_TRY(keys.alloc(ctx, sizeof(int32_t) * (size_t)std::max<int64_t>(ne, 1)));
     std::vector<unsigned long long> hist;
     int err = 0;
     RBF_TRY(rbf_batched_classify(ctx, ne, dim, ap.as<int64_t>(), poly_deg_per ? dg.as<int8_t>() : nullptr,
-                                 cfg->poly_deg, keys.as<int16_t>(), hist, &err));
+                                 cfg->poly_deg, normal_dof ? &nd : nullptr, keys.as<int32_t>(), hist, &err));
     if (err & 8) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "adj_ptr must be non-decreasing");
     if (err & 1) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "stencil sizes must be in 1..%d", RBF_MAX_STENCIL);
     if (err & 4) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "polynomial degrees must be in -1..6");
     if (err & 2)
-        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "a stencil's k + number of monomials exceeds %d", RBF_MAX_SYSTEM);
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "a stencil's k + %snumber of monomials exceeds %d",
+                        normal_dof ? "Neumann/Robin neighbours + " : "", RBF_MAX_SYSTEM);
     int64_t nnz = 0;
     RBF_CUDA(ctx, cudaMemcpyAsync(&nnz, rp.as<int64_t>() + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
     RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (nnz < 0 || nnz > ends[1]) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "row_ptr is not the layout of this build");
+    if (nnz < 0 || nnz > (normal_dof ? 2 : 1) * ends[1])
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "row_ptr is not the layout of this build");
     OutArray oc, ov, os;
     RBF_TRY(oc.bind(ctx, col, sizeof(int32_t) * nnz));
     RBF_TRY(ov.bind(ctx, val, sizeof(double) * nnz * cfg->nops));
@@ -997,10 +1051,11 @@ int rbf_build_batched(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data
         BinDesc B;
         memset(&B, 0, sizeof B);
         B.P = P;
-        B.P.k = key / 8;
+        B.P.nnr = key / (65 * 8);
+        B.P.k = (key % (65 * 8)) / 8;
         B.P.poly_deg = key % 8 - 1;
         B.P.nmon = monomial_exponents(dim, B.P.poly_deg, B.P.exps);
-        B.P.n = B.P.k + B.P.nmon;
+        B.P.n = B.P.k + B.P.nnr + B.P.nmon;
         B.count = (int64_t)hist[key];
         B.precision = cfg->precision;
         bins.push_back(B);
@@ -1009,12 +1064,12 @@ int rbf_build_batched(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data
     std::vector<int> class_of_key(kRbfBatchKeys, -1);
     std::vector<unsigned long long> class_start(bins.size() + 1, 0ull);
     for (size_t c = 0; c < bins.size(); c++) {
-        class_of_key[bins[c].P.k * 8 + bins[c].P.poly_deg + 1] = (int)c;
+        class_of_key[(bins[c].P.nnr * 65 + bins[c].P.k) * 8 + bins[c].P.poly_deg + 1] = (int)c;
         class_start[c + 1] = class_start[c] + (unsigned long long)bins[c].count;
     }
     DevBuf slots;
     RBF_TRY(slots.alloc(ctx, sizeof(int32_t) * (size_t)std::max<int64_t>(ne, 1)));
-    RBF_TRY(rbf_batched_scatter(ctx, ne, keys.as<int16_t>(), class_of_key, class_start, slots.as<int32_t>()));
+    RBF_TRY(rbf_batched_scatter(ctx, ne, keys.as<int32_t>(), class_of_key, class_start, slots.as<int32_t>()));
     for (size_t c = 0; c < bins.size(); c++) bins[c].slots = slots.as<int32_t>() + class_start[c];
     // the split tile's deferred list (refined builds): room for the largest class
     DevBuf defer;
@@ -1071,10 +1126,10 @@ int rbf_tuning_report(rbf_ctx *ctx, char *buf, int64_t len) {
         const unsigned long long k = kv.first;
         const rbf_tune_entry &t = kv.second;
         snprintf(line, sizeof line,
-                 "precision=%s dim=%llu phs=%llu nops=%llu k=%llu degree=%lld boundary=%llu op=%llu: tile=%s "
-                 "(warp %.3f ms, block %.3f ms, split %.3f ms, sample %lld)\n",
+                 "precision=%s dim=%llu phs=%llu nops=%llu k=%llu degree=%lld boundary=%llu op=%llu dudn=%llu: "
+                 "tile=%s (warp %.3f ms, block %.3f ms, split %.3f ms, sample %lld)\n",
                  (k & 15) == RBF_PREC_FP64 ? "fp64" : "fp32_refined", (k >> 4) & 15, (k >> 8) & 15, (k >> 12) & 15,
-                 (k >> 16) & 255, (long long)((k >> 24) & 15) - 1, (k >> 28) & 1, (k >> 32) & 15,
+                 (k >> 16) & 255, (long long)((k >> 24) & 15) - 1, (k >> 28) & 1, (k >> 32) & 255, (k >> 40) & 255,
                  t.tile == kTileSplit ? "split" : (t.tile ? "block" : "warp"), t.ms_warp, t.ms_block, t.ms_split,
                  t.sample);
         out += line;

@@ -10,8 +10,9 @@
 
 #include "rbffd.h"
 
-// Size-class keys of the batched build: k * 8 + (polynomial degree + 1), k <= 64.
-constexpr int kRbfBatchKeys = 65 * 8;
+// Size-class keys of the batched build: (m * 65 + k) * 8 + (polynomial degree + 1), k <= 64
+// the stencil length, m <= 64 the normal-derivative unknowns (RBF_FLAG_NORMAL_DOF).
+constexpr int kRbfBatchKeys = 65 * 65 * 8;
 
 // One tuned size class of the batched build: the tile shape chosen and the trial timings.
 // tile 2 of a batched class: the split-row register kernel on the class's stencils (its own launch)
@@ -115,7 +116,8 @@ struct StencilParams;  // stencil.cuh
 
 int rbf_count_rows_device(rbf_ctx *ctx, int64_t ne, int k, const uint8_t *d_isb,
                           const int32_t *d_g2b, const double *d_alpha, const double *d_beta,
-                          int64_t *d_row_ptr, int64_t *nnz, const int64_t *d_adj_ptr = nullptr);
+                          int64_t *d_row_ptr, int64_t *nnz, const int64_t *d_adj_ptr = nullptr,
+                          const int32_t *d_adj_idx = nullptr);
 
 int rbf_boundary_map_device(rbf_ctx *ctx, int64_t n, const uint8_t *d_isb, int32_t *d_g2b,
                             int64_t *n_boundary);

@@ -108,17 +108,30 @@ int exclusive_scan(rbf_ctx *ctx, const T *d_in, T *d_out, int64_t n, T *d_total_
 }
 
 // rows: Dirichlet eval rows (boundary point with alpha == 1, beta == 0) hold one entry,
-// every other row holds k (src/solve/execution.jl:39-69).
+// every other row holds k (src/solve/execution.jl:39-69); with adj_idx (the normal-derivative
+// formulation) k plus one du/dn entry per Neumann/Robin neighbour.
 __global__ void row_counts_kernel(int64_t ne, int k, const uint8_t *__restrict__ isb,
                                   const int32_t *__restrict__ g2b, const double *__restrict__ alpha,
                                   const double *__restrict__ beta, int64_t *__restrict__ cnt,
-                                  const int64_t *__restrict__ adj_ptr) {
+                                  const int64_t *__restrict__ adj_ptr, const int32_t *__restrict__ adj_idx) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne;
          e += (int64_t)gridDim.x * blockDim.x) {
         int64_t c = adj_ptr ? adj_ptr[e + 1] - adj_ptr[e] : k;
+        bool dirichlet_eval = false;
         if (isb && isb[e]) {
             int32_t b = g2b[e];
-            if (alpha[b] == 1.0 && beta[b] == 0.0) c = 1;
+            dirichlet_eval = alpha[b] == 1.0 && beta[b] == 0.0;
+        }
+        if (dirichlet_eval) {
+            c = 1;
+        } else if (adj_idx && isb) {
+            for (int64_t t = adj_ptr[e]; t < adj_ptr[e + 1]; t++) {
+                const int32_t g = adj_idx[t];
+                if (isb[g]) {
+                    const int32_t b = g2b[g];
+                    c += !(alpha[b] == 1.0 && beta[b] == 0.0);
+                }
+            }
         }
         cnt[e] = c;
     }
@@ -184,13 +197,13 @@ int rbf_boundary_map_device(rbf_ctx *ctx, int64_t n, const uint8_t *d_isb, int32
 
 int rbf_count_rows_device(rbf_ctx *ctx, int64_t ne, int k, const uint8_t *d_isb, const int32_t *d_g2b,
                           const double *d_alpha, const double *d_beta, int64_t *d_row_ptr, int64_t *nnz,
-                          const int64_t *d_adj_ptr) {
+                          const int64_t *d_adj_ptr, const int32_t *d_adj_idx) {
     DevBuf cnt;
     RBF_TRY(cnt.alloc(ctx, sizeof(int64_t) * (ne + 1)));
     int blocks = (int)std::min<int64_t>((ne + 255) / 256, (int64_t)ctx->num_sms * 8);
     if (blocks < 1) blocks = 1;
     row_counts_kernel<<<blocks, 256, 0, ctx->stream>>>(ne, k, d_isb, d_g2b, d_alpha, d_beta, cnt.as<int64_t>(),
-                                                     d_adj_ptr);
+                                                     d_adj_ptr, d_adj_idx);
     RBF_CHECK_LAUNCH(ctx);
     RBF_CUDA(ctx, cudaMemsetAsync(cnt.as<int64_t>() + ne, 0, sizeof(int64_t), ctx->stream));
     // scan over ne+1 entries so that row_ptr[ne] is the total

@@ -326,7 +326,7 @@ __device__ void solve_fp64_bk_warp(const StencilParams &P, int64_t e, const BKSm
         __syncwarp();
         return;
     }
-    assemble_fp64_into(P, s.w, lane, es, eval_local, PackedStore{s.P, s.B, P.n, P.k, P.nops});
+    assemble_fp64_into(P, s.w, lane, es, eval_local, PackedStore{s.P, s.B, P.n, P.k + P.nnr, P.nops});
     if (!bk_solve(s, P.n, P.nops, lane)) {
         if (lane == 0) {
             if (P.status) P.status[e] = 1;

@@ -25,6 +25,7 @@ enum { PT_INTERIOR = 0, PT_DIRICHLET = 1, PT_NR = 2 };
 // Launch parameters of one build (passed by value, read from the constant bank).
 struct StencilParams {
     int dim, phs, poly_deg, nmon, k, n, nops;
+    int nnr;  // RBF_FLAG_NORMAL_DOF: the du/dn unknowns of the size class (n = k + nnr + nmon)
     int op_code[RBF_MAX_OPS];
     int op_dim[RBF_MAX_OPS];
     int op_order[RBF_MAX_OPS];

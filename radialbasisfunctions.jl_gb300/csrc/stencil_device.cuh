@@ -9,6 +9,9 @@
 
 namespace {
 
+// Per-warp staging of one stencil.  ptype: the points' Hermite types; in a normal-derivative
+// build (RBF_FLAG_NORMAL_DOF) ptype[a] is instead the stencil position of du/dn unknown a and
+// HN[3a..3a+2] its normal.
 struct WarpSmem {
     double *M, *X, *HA, *HB, *HN;
     int *cols, *ptype;
@@ -40,7 +43,10 @@ __device__ inline WarpSmem carve(char *base, int n, int k, int nops) {
 }
 
 // Loads the stencil, classifies it and fills X/cols/Hermite data.  Returns
-//  0: solve needed, 2: Dirichlet identity row written, -1: eval point not in stencil.
+//  0: solve needed, 2: Dirichlet identity row written, -1: eval point not in stencil,
+//  1: the stencil's du/dn unknowns differ from its size class's (normal-derivative builds).
+// *eval_local_out: -2 interior stencil (plain collocation), -3 stencil with du/dn unknowns,
+// else the reference's Hermite stencil (the eval point's stencil position, -1 if absent).
 __device__ int load_stencil(const StencilParams &P, int64_t e, const WarpSmem &w, int lane, int *es_out,
                             int *eval_local_out) {
     const int k = P.k, dim = P.dim;
@@ -91,6 +97,37 @@ __device__ int load_stencil(const StencilParams &P, int64_t e, const WarpSmem &w
                 }
                 return 2;
             }
+        }
+        if (P.flags & RBF_FLAG_NORMAL_DOF) {
+            // every point is a value point; the Neumann/Robin ones also carry du/dn, numbered
+            // in stencil order (the Dirichlet ones are plain value points)
+            int m = 0;
+            for (int i0 = 0; i0 < k; i0 += 32) {
+                const int i = i0 + lane;
+                bool nr = false;
+                int32_t b = 0;
+                if (i < k && P.isb[w.cols[i]]) {
+                    b = P.g2b[w.cols[i]];
+                    nr = !(P.alpha[b] == 1.0 && P.beta[b] == 0.0);
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, nr);
+                const int a = m + __popc(bal & ((1u << lane) - 1u));
+                if (nr && a < P.nnr) {
+                    w.ptype[a] = i;
+                    for (int d = 0; d < 3; d++) w.HN[a * 3 + d] = d < dim ? P.normals[(int64_t)b * dim + d] : 0.0;
+                }
+                m += __popc(bal);
+            }
+            if (m != P.nnr) {
+                if (lane == 0) {
+                    if (P.status) P.status[e] = 1;
+                    atomicAdd(&P.counters[0], 1ull);
+                }
+                return 1;
+            }
+            *eval_local_out = m > 0 ? -3 : -2;
+            __syncwarp();
+            return 0;
         }
         const double sinv = scale2(1.0, -es);
         bool found = false;
@@ -172,7 +209,9 @@ template <class S>
 __device__ void assemble_fp64_into(const StencilParams &P, const WarpSmem &w, int lane, int es, int eval_local,
                                    const S &st) {
     const int k = P.k, nops = P.nops, dim = P.dim, nmon = P.nmon;
-    const bool herm = eval_local != -2;
+    const bool aug = eval_local == -3;           // du/dn unknowns: plain value-value block
+    const bool herm = eval_local != -2 && !aug;  // the reference's Hermite stencil
+    const int kv = aug ? k + P.nnr : k;          // unknowns before the polynomial multipliers
     const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
     st.zero(lane);
     __syncwarp();
@@ -232,7 +271,7 @@ __device__ void assemble_fp64_into(const StencilParams &P, const WarpSmem &w, in
                     if (w.HN[i * 3 + d] != 0.0) dn += w.HN[i * 3 + d] * mono_d1<double>(P, m, d, xi);
                 v = w.HA[i] * v + w.HB[i] * dn;
             }
-            st.sym(i, k + m, v);
+            st.sym(i, kv + m, v);
         }
         double D[3];
         for (int d = 0; d < dim; d++) D[d] = -xi[d];  // x0 - xi in local coordinates
@@ -257,7 +296,63 @@ __device__ void assemble_fp64_into(const StencilParams &P, const WarpSmem &w, in
         } else {
             v = mono_op_at_origin(P, m, P.op_code[r], P.op_dim[r]);
         }
-        st.rhs(k + m, r, v);
+        st.rhs(kv + m, r, v);
+    }
+    if (aug) {
+        // du/dn unknowns a, b (stencil positions ptype[a], normals n_a): the functionals
+        // u(x_i) and du/dn(x_a) applied to the kernel, in local units --
+        //   value row i, column k + a:  -n_a . grad phi(x_i - x_a)
+        //   rows/columns k + a, k + b:  -n_a^T Hess phi(x_a - x_b) n_b
+        //   polynomial columns:          n_a . grad p(x_a)
+        //   right-hand sides:            L applied to -n_a . grad phi(x - x_a) at the eval point
+        const int m = P.nnr;
+        const int nvd = k * m, ndd = m * (m + 1) / 2;
+        for (int t = lane; t < nvd + ndd; t += 32) {
+            int i, a;
+            const bool dd = t >= nvd;
+            if (!dd) {
+                i = t / m;
+                a = t - i * m;
+            } else {
+                const int p = t - nvd;  // pair (i, a), i >= a, in row order
+                i = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+                while (i * (i + 1) / 2 > p) i--;
+                while ((i + 1) * (i + 2) / 2 <= p) i++;
+                a = p - i * (i + 1) / 2;
+            }
+            const double *xi = dd ? &w.X[w.ptype[i] * 3] : &w.X[i * 3];
+            const double *xa = &w.X[w.ptype[a] * 3];
+            const double *na = &w.HN[a * 3];
+            double D[3], g[3], H[9];
+            for (int d = 0; d < dim; d++) D[d] = xi[d] - xa[d];
+            phs_grad_hess<double>(P.phs, D, dim, g, H, dd, AI);
+            double v = 0.0;
+            if (!dd) {
+                for (int d = 0; d < dim; d++) v = fma(-na[d], g[d], v);
+                st.sym(i, k + a, v);
+            } else {
+                const double *ni = &w.HN[i * 3];
+                for (int c = 0; c < dim; c++) {
+                    double hn = 0.0;
+                    for (int d = 0; d < dim; d++) hn = fma(H[c * 3 + d], na[d], hn);
+                    v = fma(-ni[c], hn, v);
+                }
+                st.sym(k + i, k + a, v);
+            }
+        }
+        for (int a = lane; a < m; a += 32) {
+            const double *xa = &w.X[w.ptype[a] * 3];
+            const double *na = &w.HN[a * 3];
+            for (int mm = 0; mm < nmon; mm++) {
+                double dn = 0.0;
+                for (int d = 0; d < dim; d++) dn = fma(na[d], mono_d1<double>(P, mm, d, xa), dn);
+                st.sym(k + a, kv + mm, dn);
+            }
+            double D[3];
+            for (int d = 0; d < dim; d++) D[d] = -xa[d];
+            for (int r = 0; r < nops; r++)
+                st.rhs(k + a, r, phs_op_normal<double>(P.phs, P.op_code[r], P.op_dim[r], D, na, dim, AI));
+        }
     }
     __syncwarp();
 }
@@ -336,10 +431,30 @@ __device__ bool lu_solve_fp64(double *M, int n, int nops, int lane) {
 // Writes the solved weights of stencil e into its CSR row, columns ascending.
 __device__ void scatter_row(const StencilParams &P, int64_t e, const WarpSmem &w, int lane, int es,
                             const double *sol, int sol_ld, int sol_stride) {
-    const int k = P.k;
+    const int k = P.k, m = P.nnr;
     const int64_t base = P.row_ptr[e];
     const bool sorted = !(P.flags & RBF_FLAG_STENCIL_ORDER);
     const bool local = (P.flags & RBF_FLAG_LOCAL_UNITS) != 0;
+    // du/dn unknowns (normal-derivative builds): columns ns + boundary ordinal after the value
+    // columns; their weights scale by s^(1 - q) (one derivative in the unknown)
+    for (int a = lane; a < m; a += 32) {
+        const int32_t ca = (int32_t)P.ns + P.g2b[w.cols[w.ptype[a]]];
+        int rank = k + a;
+        if (sorted) {
+            rank = k;
+            for (int b = 0; b < m; b++) {
+                const int32_t cb = (int32_t)P.ns + P.g2b[w.cols[w.ptype[b]]];
+                rank += (cb < ca) || (cb == ca && b < a);
+            }
+        }
+        P.col[base + rank] = ca;
+        for (int r = 0; r < P.nops; r++) {
+            const double v = sol[(k + a) * sol_ld + r * sol_stride];
+            const double vo = local ? v : scale2(v, es * (1 - P.op_order[r]));
+            P.val[r * P.nnz + base + rank] = vo;
+            if (P.sell_col) sell_put(P, e, rank, ca, r, vo);
+        }
+    }
     for (int i = lane; i < k; i += 32) {
         const int ci = w.cols[i];
         int rank = i;

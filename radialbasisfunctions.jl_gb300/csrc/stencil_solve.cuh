@@ -55,7 +55,7 @@ __device__ bool refine_fp32_warp(const StencilParams &P, const WarpSmem &w, cons
         for (int t = lane; t < n * nops; t += 32) {
             const float df = u.v[t];
             u.x[t] += widen(df);
-            if (t / nops < P.k) {
+            if (t / nops < P.k + P.nnr) {  // the weights (value and du/dn unknowns)
                 dmaxf = fmaxf(dmaxf, fabsf(df));
                 xmaxf = fmaxf(xmaxf, fabsf(__double2float_rn(u.x[t])));
             }

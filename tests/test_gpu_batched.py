@@ -189,7 +189,7 @@ def test_split_tile_for_40_row_classes(pkg):
     st = pkg._native.BuildStats()
     W = pkg.build_weights_batched([(3, 0)], X, None, ap, ai, basis, precision="fp32_refined", tune=2, stats=st)[0]
     rep = pkg.tuning_report()
-    line = [ln for ln in rep.splitlines() if "precision=fp32_refined dim=3" in ln and "k=30 degree=2" in ln]
+    line = [ln for ln in rep.splitlines() if "precision=fp32_refined dim=3 phs=3 nops=1 k=30 degree=2 boundary=0" in ln]
     assert line and "split " in line[0] and "split 0.000 ms" not in line[0], rep
     assert int(st.n_stencils) == n
     for k in (20, 30):
