@@ -58,7 +58,7 @@ PEAKS = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.ex
 # case of this workload (`python bench.py --case build_refined --n 1000000` and `--case
 # build_learned` under ncu), scaled by the stencil count (the kernel's traffic grows in
 # proportion).  None: not captured.
-KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": 479.6, "learned": None}
+KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": 479.6, "learned": 610.3}
 
 
 def peaks_bf16():
@@ -944,11 +944,15 @@ def main():
     # one entry-wise pass over the value arrays, 24 bytes per entry (two reads, one write)
     alg_out = torch.empty_like(W.val)
     alg_b = W.val.clone()  # a second operand in its own memory
-    ms_axpby = timed(lambda: ctx.check(ctx.lib.rbf_weights_axpby(ctx.h, nnz, 1.0, pkg._ptr(W.val), 2.0,
-                                                                  pkg._ptr(alg_b), pkg._ptr(alg_out))), 5, 2)
+    ms_axpby = kernel_ms(lambda: ctx.check(ctx.lib.rbf_weights_axpby(ctx.h, nnz, 1.0, pkg._ptr(W.val), 2.0,
+                                                                      pkg._ptr(alg_b), pkg._ptr(alg_out))))
+    ms_axpby_api = timed(lambda: ctx.check(ctx.lib.rbf_weights_axpby(ctx.h, nnz, 1.0, pkg._ptr(W.val), 2.0,
+                                                                      pkg._ptr(alg_b), pkg._ptr(alg_out))), 5, 2)
     alg_gbs = 24 * nnz / (ms_axpby * 1e-3) / 1e9
-    algebra = {"kernel": "axpby_kernel (rbf_weights_axpby: out = a + 2 b over the values)", "nnz": nnz,
-               "ms": ms_axpby, "GB_s": alg_gbs, "frac_of_hbm": alg_gbs / PEAKS.get("hbm_gbs", 6800.0)}
+    algebra = {"kernel": "axpby_kernel (rbf_weights_axpby: out = a + 2 b over the values; the scalings are "
+                         "powers of two, applied on the integer pipe, so one DADD per entry)", "nnz": nnz,
+               "ms": ms_axpby, "ms_per_call_api": ms_axpby_api, "GB_s": alg_gbs,
+               "frac_of_hbm": alg_gbs / PEAKS.get("hbm_gbs", 6800.0)}
     del W, W_sell, W_ord, alg_out, alg_b
     hbm_peak = PEAKS.get("hbm_gbs", 6800.0)
     hbm_src = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in PEAKS else "fallback"
@@ -956,6 +960,10 @@ def main():
     ctx.check(ctx.lib.rbf_diag_fma_peak(ctx.h, 1, pkg.ctypes.byref(fp64_peak)))
     fp32_peak = pkg.ctypes.c_double(0.0)
     ctx.check(ctx.lib.rbf_diag_fma_peak(ctx.h, 0, pkg.ctypes.byref(fp32_peak)))
+    # the algebra's other bound: one FP64 add per entry at the FP64 pipe's rate (the FMA loop's
+    # rate; the peak counts two flops per FMA)
+    algebra["fp64_issue_bound_ms"] = nnz / (fp64_peak.value * 0.5e12) * 1e3
+    algebra["hbm_bound_ms"] = 24 * nnz / (hbm_peak * 1e9) * 1e3
     nsys = k + math.comb(cfg["deg"] + cfg["dim"], cfg["dim"])
     R = len(cfg["ops"])
     # algorithmic FLOPs of the reference algorithm per stencil: symmetric factor n^3/3,

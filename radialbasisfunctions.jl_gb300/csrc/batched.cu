@@ -99,13 +99,14 @@ struct BlockScratch {
 
 // One stencil on the whole block, plain FP64: warp 0 loads, assembles and scatters, every
 // thread factorises.
+template <bool ND>
 __device__ void solve_fp64_block(const StencilParams &P, int64_t e, const WarpSmem &w, int tid, int G,
                                  BlockScratch &bs) {
     const int lane = tid & 31;
     if (tid < 32) {
         int es = 0, eval_local = -2;
         const int st = load_stencil(P, e, w, lane, &es, &eval_local);
-        if (st == 0) assemble_fp64(P, w, lane, es, eval_local);
+        if (st == 0) assemble_fp64<ND>(P, w, lane, es, eval_local);
         if (lane == 0) {
             bs.flag = st;
             bs.es = es;
@@ -129,13 +130,14 @@ __device__ void solve_fp64_block(const StencilParams &P, int64_t e, const WarpSm
 
 // One stencil on the whole block, FP32 factor + FP64 refinement: every thread factorises,
 // warp 0 refines (O(n^2) per step); the FP64 fallback is factorised by the block again.
+template <bool ND>
 __device__ void solve_fp32r_block(const StencilParams &P, int64_t e, const WarpSmem &w, const Warp32 &u, int tid,
                                   int G, BlockScratch &bs) {
     const int lane = tid & 31;
     int es = 0, eval_local = -2;
     if (tid < 32) {
         const int st = load_stencil(P, e, w, lane, &es, &eval_local);
-        if (st == 0) assemble_refined(P, w, u, lane, es, eval_local);
+        if (st == 0) assemble_refined<ND>(P, w, u, lane, es, eval_local);
         if (lane == 0) {
             bs.flag = st;
             bs.es = es;
@@ -205,24 +207,42 @@ __global__ void __launch_bounds__(kBatchedThreads) build_batched_kernel(const Bi
             __syncthreads();
         }
         const StencilParams &P = s_bin.P;
+        const bool nd = P.nnr > 0;  // classes with du/dn unknowns take the ND instantiations
         if (s_bin.tile == 0) {
             const int64_t slot = (item - s_bin.item_start) * 4 + wib;
             if (slot < s_bin.count) {
                 char *base = smem + wib * region;
                 const WarpSmem w = carve(base, P.n, P.k, P.nops);
                 const int64_t e = s_bin.slots[slot];
-                if (s_bin.precision == RBF_PREC_FP64)
-                    solve_fp64_bk_warp(P, e, carve_bk(base, P.n, P.k, P.nops), lane);
-                else
-                    solve_fp32r_warp(P, e, w, carve32(base, P.n, P.k, P.nops), lane);
+                if (s_bin.precision == RBF_PREC_FP64) {
+                    const BKSmem bk = carve_bk(base, P.n, P.k, P.nops);
+                    if (nd)
+                        solve_fp64_bk_warp<true>(P, e, bk, lane);
+                    else
+                        solve_fp64_bk_warp<false>(P, e, bk, lane);
+                } else {
+                    const Warp32 u = carve32(base, P.n, P.k, P.nops);
+                    if (nd)
+                        solve_fp32r_warp<true>(P, e, w, u, lane);
+                    else
+                        solve_fp32r_warp<false>(P, e, w, u, lane);
+                }
             }
         } else {
             const int64_t e = s_bin.slots[item - s_bin.item_start];
             const WarpSmem w = carve(smem, P.n, P.k, P.nops);
-            if (s_bin.precision == RBF_PREC_FP64)
-                solve_fp64_block(P, e, w, tid, blockDim.x, bs);
-            else
-                solve_fp32r_block(P, e, w, carve32(smem, P.n, P.k, P.nops), tid, blockDim.x, bs);
+            if (s_bin.precision == RBF_PREC_FP64) {
+                if (nd)
+                    solve_fp64_block<true>(P, e, w, tid, blockDim.x, bs);
+                else
+                    solve_fp64_block<false>(P, e, w, tid, blockDim.x, bs);
+            } else {
+                const Warp32 u = carve32(smem, P.n, P.k, P.nops);
+                if (nd)
+                    solve_fp32r_block<true>(P, e, w, u, tid, blockDim.x, bs);
+                else
+                    solve_fp32r_block<false>(P, e, w, u, tid, blockDim.x, bs);
+            }
         }
         __syncthreads();
     }
@@ -292,30 +312,15 @@ int rbf_batched_scatter(rbf_ctx *ctx, int64_t ne, const int32_t *d_key, const st
     return RBF_OK;
 }
 
-// Runs the persistent kernel over the classes (their item_start fields are filled here).
-// Runs the persistent kernel over the classes with warp or block tiles (their item_start
-// fields are filled here), then each class with the split tile: the split-row register kernel
-// on the class's stencils and the general refined kernel on the ones it hands over (defer:
-// room for the largest such class's stencil count).
-int rbf_batched_run(rbf_ctx *ctx, std::vector<BinDesc> &bins, int32_t *defer) {
-    if (bins.empty()) return RBF_OK;
+// One persistent launch over the warp- and block-tile classes in `bins` (their item_start
+// fields are filled here), with room for the largest of their systems.
+static int run_persistent(rbf_ctx *ctx, std::vector<BinDesc> &bins) {
     int64_t items = 0;
     size_t region = 16;
     for (auto &b : bins) {
         b.item_start = items;
-        if (b.tile == kTileSplit) continue;
         items += b.tile == 0 ? (b.count + 3) / 4 : b.count;
         region = std::max(region, rbf_batched_region(b.P.n, b.P.k, b.P.nops, b.precision));
-    }
-    for (const auto &b : bins) {
-        if (b.tile != kTileSplit || b.count == 0) continue;
-        if (!defer) return rbf_fail(ctx, RBF_ERR_INTERNAL, "split tile without a deferred list");
-        StencilParams Ps = b.P;
-        Ps.slots = b.slots;
-        Ps.nslots = b.count;
-        Ps.defer = defer;
-        RBF_CUDA(ctx, cudaMemsetAsync(&Ps.counters[7], 0, sizeof(unsigned long long), ctx->stream));
-        RBF_TRY(rbf_build_fp32_launch(ctx, Ps));
     }
     if (items == 0) return RBF_OK;
     const size_t smem = 4 * region;
@@ -336,6 +341,52 @@ int rbf_batched_run(rbf_ctx *ctx, std::vector<BinDesc> &bins, int32_t *defer) {
     RBF_CHECK_LAUNCH(ctx);
     // the descriptor copy reads host memory: complete it before the vector can change
     RBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return RBF_OK;
+}
+
+// Runs each split-tile class on the split-row register kernel (the general refined kernel
+// finishing what it hands over; defer: room for the largest such class's stencil count),
+// then the warp- and block-tile classes in persistent launches grouped by occupancy: the
+// shared memory of a launch is set by its largest system, so classes whose systems allow
+// more resident blocks per SM (the common interior class beside a few larger boundary
+// classes) get a launch of their own instead of running at the larger classes' occupancy.
+int rbf_batched_run(rbf_ctx *ctx, std::vector<BinDesc> &bins, int32_t *defer) {
+    if (bins.empty()) return RBF_OK;
+    for (auto &b : bins) b.item_start = 0;
+    for (const auto &b : bins) {
+        if (b.tile != kTileSplit || b.count == 0) continue;
+        if (!defer) return rbf_fail(ctx, RBF_ERR_INTERNAL, "split tile without a deferred list");
+        StencilParams Ps = b.P;
+        Ps.slots = b.slots;
+        Ps.nslots = b.count;
+        Ps.defer = defer;
+        RBF_CUDA(ctx, cudaMemsetAsync(&Ps.counters[7], 0, sizeof(unsigned long long), ctx->stream));
+        RBF_TRY(rbf_build_fp32_launch(ctx, Ps));
+    }
+    // resident blocks per SM of each remaining class at its own shared memory
+    std::vector<std::pair<int, size_t>> occ;  // (blocks per SM, index into bins)
+    for (size_t i = 0; i < bins.size(); i++) {
+        const BinDesc &b = bins[i];
+        if (b.tile == kTileSplit || b.count == 0) continue;
+        const size_t smem = 4 * rbf_batched_region(b.P.n, b.P.k, b.P.nops, b.precision);
+        if (smem > 227 * 1024) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "batched build: system too large for shared memory");
+        RBF_CUDA(ctx, cudaFuncSetAttribute(build_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        RBF_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, build_batched_kernel, kBatchedThreads, smem));
+        occ.push_back({per_sm, i});
+    }
+    // one launch per occupancy level, the highest first (classes keep their largest-system-
+    // first order within a launch)
+    std::stable_sort(occ.begin(), occ.end(), [](const std::pair<int, size_t> &a, const std::pair<int, size_t> &c) {
+        return a.first > c.first;
+    });
+    for (size_t g = 0; g < occ.size();) {
+        size_t h = g;
+        std::vector<BinDesc> group;
+        while (h < occ.size() && occ[h].first == occ[g].first) group.push_back(bins[occ[h++].second]);
+        RBF_TRY(run_persistent(ctx, group));
+        g = h;
+    }
     return RBF_OK;
 }
 

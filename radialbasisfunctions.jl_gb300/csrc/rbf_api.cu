@@ -757,7 +757,21 @@ int rbf_weights_axpby(rbf_ctx *ctx, int64_t nnz, double alpha, const double *a, 
     if (nnz < 0) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid entry count");
     if (!rbf_is_device_ptr(a) || !rbf_is_device_ptr(out) || (b && !rbf_is_device_ptr(b)))
         return rbf_fail(ctx, RBF_ERR_ARGUMENT, "operator algebra takes device pointers only");
-    return rbf_weights_axpby_device(ctx, nnz, alpha, a, beta, b, out);
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (ctx->timing) {
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        cudaEventRecord(t0, ctx->stream);
+    }
+    const int st = rbf_weights_axpby_device(ctx, nnz, alpha, a, beta, b, out);
+    if (ctx->timing) {
+        cudaEventRecord(t1, ctx->stream);
+        cudaEventSynchronize(t1);
+        cudaEventElapsedTime(&ctx->last_ms, t0, t1);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
+    return st;
 }
 
 int rbf_weights_directional(rbf_ctx *ctx, int64_t ne, const int64_t *row_ptr, int32_t nd, const double *val,

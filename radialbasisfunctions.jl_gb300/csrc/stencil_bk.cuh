@@ -23,7 +23,7 @@ namespace {
 
 // Per-warp workspace: the packed system and the step vectors beside WarpSmem's stencil data.
 struct BKSmem {
-    WarpSmem w;        // X, HA, HB, HN, cols, ptype (w.M unused)
+    WarpSmem w;        // X, HA, HB, HN (in the work area), cols, ptype (w.M unused)
     double *P;         // lower triangle, packed by rows: (i, j), i >= j, at pidx(i, j)
     double *B;         // right-hand sides, n x nops; on return the solution in pivot order
     double *l1, *l2;   // multipliers of the current step's pivot column(s), indexed by row
@@ -34,8 +34,17 @@ struct BKSmem {
     int *blk;          // 1: 1x1 pivot at this position, 2: first row of a 2x2 block, 0: second row
 };
 
+// Work area shared by the phases: the stencil data (X, HA, HB, HN: 8k doubles) is read only by
+// the assembly, the step vectors (l1, l2, w1, w2, dinv: 7n) only by the factorisation and
+// the D solve, and the solution in the original order (n x nops) is written after both.
+__host__ __device__ inline size_t bk_work_doubles(int n, int k, int nops) {
+    size_t m = 8 * (size_t)k;
+    m = m > 7 * (size_t)n ? m : 7 * (size_t)n;
+    return m > (size_t)n * nops ? m : (size_t)n * nops;
+}
+
 __host__ __device__ inline size_t bk_warp_bytes(int n, int k, int nops) {
-    const size_t d = (size_t)n * (n + 1) / 2 + 2 * (size_t)n * nops + 4 * (size_t)n + 3 * (size_t)n + 8 * (size_t)k;
+    const size_t d = (size_t)n * (n + 1) / 2 + (size_t)n * nops + bk_work_doubles(n, k, nops);
     const size_t i = 2 * (size_t)k + 2 * (size_t)n;
     return ((d * sizeof(double) + i * sizeof(int)) + 15) & ~(size_t)15;
 }
@@ -47,25 +56,19 @@ __device__ inline BKSmem carve_bk(char *base, int n, int k, int nops) {
     p += (size_t)n * (n + 1) / 2;
     s.B = p;
     p += (size_t)n * nops;
-    s.sol = p;
-    p += (size_t)n * nops;
-    s.l1 = p;
-    s.l2 = p + n;
-    s.w1 = p + 2 * n;
-    s.w2 = p + 3 * n;
-    p += 4 * (size_t)n;
-    s.dinv = p;
-    p += 3 * (size_t)n;
+    double *work = p;
+    s.l1 = work;
+    s.l2 = work + n;
+    s.w1 = work + 2 * n;
+    s.w2 = work + 3 * n;
+    s.dinv = work + 4 * n;
+    s.sol = work;
     s.w.M = nullptr;
-    s.w.X = p;
-    p += 3 * k;
-    s.w.HA = p;
-    p += k;
-    s.w.HB = p;
-    p += k;
-    s.w.HN = p;
-    p += 3 * k;
-    int *ip = reinterpret_cast<int *>(p);
+    s.w.X = work;
+    s.w.HA = work + 3 * k;
+    s.w.HB = work + 4 * k;
+    s.w.HN = work + 5 * k;
+    int *ip = reinterpret_cast<int *>(work + bk_work_doubles(n, k, nops));
     s.w.cols = ip;
     s.w.ptype = ip + k;
     s.orig = ip + 2 * k;
@@ -318,7 +321,8 @@ __device__ bool bk_solve(const BKSmem &s, int n, int nops, int lane) {
 }
 
 // One stencil e on one warp, plain FP64 by Bunch-Kaufman: load, assemble (packed), factorise,
-// solve, scatter.
+// solve, scatter (ND: the normal-derivative builds' instantiation).
+template <bool ND = false>
 __device__ void solve_fp64_bk_warp(const StencilParams &P, int64_t e, const BKSmem &s, int lane) {
     int es = 0, eval_local = -2;
     const int st = load_stencil(P, e, s.w, lane, &es, &eval_local);
@@ -326,7 +330,7 @@ __device__ void solve_fp64_bk_warp(const StencilParams &P, int64_t e, const BKSm
         __syncwarp();
         return;
     }
-    assemble_fp64_into(P, s.w, lane, es, eval_local, PackedStore{s.P, s.B, P.n, P.k + P.nnr, P.nops});
+    assemble_fp64_into<PackedStore, ND>(P, s.w, lane, es, eval_local, PackedStore{s.P, s.B, P.n, P.k + P.nnr, P.nops});
     if (!bk_solve(s, P.n, P.nops, lane)) {
         if (lane == 0) {
             if (P.status) P.status[e] = 1;

@@ -131,13 +131,15 @@ int rbf_build_fp32_launch(rbf_ctx *ctx, const StencilParams &P) {
             return launch_deferred(ctx, P);
         }
     }
-    // register-resident kernels for the standard system sizes (they need 3k >= n for the
-    // reciprocal-pivot buffer that reuses the split-coordinate space)
-    if (3 * P.k >= P.n) {
+    // register-resident kernels for the standard system sizes on the interior stencils, then
+    // the general kernel on the ones they deferred
+    if (P.defer) {
         int st = rbf_launch_refined_reg_a(ctx, P);
-        if (st != RBF_LAUNCH_NO_VARIANT) return st;
-        st = rbf_launch_refined_reg_b(ctx, P);
-        if (st != RBF_LAUNCH_NO_VARIANT) return st;
+        if (st == RBF_LAUNCH_NO_VARIANT) st = rbf_launch_refined_reg_b(ctx, P);
+        if (st != RBF_LAUNCH_NO_VARIANT) {
+            if (st != RBF_OK) return st;
+            return launch_deferred(ctx, P);
+        }
     }
     const size_t wb = warp_smem_bytes32(P.n, P.k, P.nops);
     int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (100 * 1024) / wb));

@@ -204,8 +204,74 @@ struct PackedStore {
     __device__ void rhs(int i, int r, double v) const { B[i * nops + r] = v; }
 };
 
-// Assemble [Phi P; P^T 0 | B] into the storage S.
+// The du/dn unknowns of a normal-derivative stencil (RBF_FLAG_NORMAL_DOF).  Only the
+// normal-derivative instantiations of the assembly (ND = true) include it, so the kernels of
+// the other builds keep their register budget.
 template <class S>
+__device__ __forceinline__ void assemble_normal_dof(const StencilParams &P, const WarpSmem &w, int lane, int es,
+                                                 const S &st) {
+    const int k = P.k, nops = P.nops, dim = P.dim, nmon = P.nmon;
+    const int kv = k + P.nnr;
+    const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
+    // du/dn unknowns a, b (stencil positions ptype[a], normals n_a): the functionals
+    // u(x_i) and du/dn(x_a) applied to the kernel, in local units --
+    //   value row i, column k + a:  -n_a . grad phi(x_i - x_a)
+    //   rows/columns k + a, k + b:  -n_a^T Hess phi(x_a - x_b) n_b
+    //   polynomial columns:          n_a . grad p(x_a)
+    //   right-hand sides:            L applied to -n_a . grad phi(x - x_a) at the eval point
+    const int m = P.nnr;
+    const int nvd = k * m, ndd = m * (m + 1) / 2;
+    for (int t = lane; t < nvd + ndd; t += 32) {
+        int i, a;
+        const bool dd = t >= nvd;
+        if (!dd) {
+            i = t / m;
+            a = t - i * m;
+        } else {
+            const int p = t - nvd;  // pair (i, a), i >= a, in row order
+            i = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+            while (i * (i + 1) / 2 > p) i--;
+            while ((i + 1) * (i + 2) / 2 <= p) i++;
+            a = p - i * (i + 1) / 2;
+        }
+        const double *xi = dd ? &w.X[w.ptype[i] * 3] : &w.X[i * 3];
+        const double *xa = &w.X[w.ptype[a] * 3];
+        const double *na = &w.HN[a * 3];
+        double D[3], g[3], H[9];
+        for (int d = 0; d < dim; d++) D[d] = xi[d] - xa[d];
+        phs_grad_hess<double>(P.phs, D, dim, g, H, dd, AI);
+        double v = 0.0;
+        if (!dd) {
+            for (int d = 0; d < dim; d++) v = fma(-na[d], g[d], v);
+            st.sym(i, k + a, v);
+        } else {
+            const double *ni = &w.HN[i * 3];
+            for (int c = 0; c < dim; c++) {
+                double hn = 0.0;
+                for (int d = 0; d < dim; d++) hn = fma(H[c * 3 + d], na[d], hn);
+                v = fma(-ni[c], hn, v);
+            }
+            st.sym(k + i, k + a, v);
+        }
+    }
+    for (int a = lane; a < m; a += 32) {
+        const double *xa = &w.X[w.ptype[a] * 3];
+        const double *na = &w.HN[a * 3];
+        for (int mm = 0; mm < nmon; mm++) {
+            double dn = 0.0;
+            for (int d = 0; d < dim; d++) dn = fma(na[d], mono_d1<double>(P, mm, d, xa), dn);
+            st.sym(k + a, kv + mm, dn);
+        }
+        double D[3];
+        for (int d = 0; d < dim; d++) D[d] = -xa[d];
+        for (int r = 0; r < nops; r++)
+            st.rhs(k + a, r, phs_op_normal<double>(P.phs, P.op_code[r], P.op_dim[r], D, na, dim, AI));
+    }
+}
+
+// Assemble [Phi P; P^T 0 | B] into the storage S (ND: the instantiation of the
+// normal-derivative builds, which also assembles their du/dn unknowns).
+template <class S, bool ND = false>
 __device__ void assemble_fp64_into(const StencilParams &P, const WarpSmem &w, int lane, int es, int eval_local,
                                    const S &st) {
     const int k = P.k, nops = P.nops, dim = P.dim, nmon = P.nmon;
@@ -298,68 +364,15 @@ __device__ void assemble_fp64_into(const StencilParams &P, const WarpSmem &w, in
         }
         st.rhs(kv + m, r, v);
     }
-    if (aug) {
-        // du/dn unknowns a, b (stencil positions ptype[a], normals n_a): the functionals
-        // u(x_i) and du/dn(x_a) applied to the kernel, in local units --
-        //   value row i, column k + a:  -n_a . grad phi(x_i - x_a)
-        //   rows/columns k + a, k + b:  -n_a^T Hess phi(x_a - x_b) n_b
-        //   polynomial columns:          n_a . grad p(x_a)
-        //   right-hand sides:            L applied to -n_a . grad phi(x - x_a) at the eval point
-        const int m = P.nnr;
-        const int nvd = k * m, ndd = m * (m + 1) / 2;
-        for (int t = lane; t < nvd + ndd; t += 32) {
-            int i, a;
-            const bool dd = t >= nvd;
-            if (!dd) {
-                i = t / m;
-                a = t - i * m;
-            } else {
-                const int p = t - nvd;  // pair (i, a), i >= a, in row order
-                i = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
-                while (i * (i + 1) / 2 > p) i--;
-                while ((i + 1) * (i + 2) / 2 <= p) i++;
-                a = p - i * (i + 1) / 2;
-            }
-            const double *xi = dd ? &w.X[w.ptype[i] * 3] : &w.X[i * 3];
-            const double *xa = &w.X[w.ptype[a] * 3];
-            const double *na = &w.HN[a * 3];
-            double D[3], g[3], H[9];
-            for (int d = 0; d < dim; d++) D[d] = xi[d] - xa[d];
-            phs_grad_hess<double>(P.phs, D, dim, g, H, dd, AI);
-            double v = 0.0;
-            if (!dd) {
-                for (int d = 0; d < dim; d++) v = fma(-na[d], g[d], v);
-                st.sym(i, k + a, v);
-            } else {
-                const double *ni = &w.HN[i * 3];
-                for (int c = 0; c < dim; c++) {
-                    double hn = 0.0;
-                    for (int d = 0; d < dim; d++) hn = fma(H[c * 3 + d], na[d], hn);
-                    v = fma(-ni[c], hn, v);
-                }
-                st.sym(k + i, k + a, v);
-            }
-        }
-        for (int a = lane; a < m; a += 32) {
-            const double *xa = &w.X[w.ptype[a] * 3];
-            const double *na = &w.HN[a * 3];
-            for (int mm = 0; mm < nmon; mm++) {
-                double dn = 0.0;
-                for (int d = 0; d < dim; d++) dn = fma(na[d], mono_d1<double>(P, mm, d, xa), dn);
-                st.sym(k + a, kv + mm, dn);
-            }
-            double D[3];
-            for (int d = 0; d < dim; d++) D[d] = -xa[d];
-            for (int r = 0; r < nops; r++)
-                st.rhs(k + a, r, phs_op_normal<double>(P.phs, P.op_code[r], P.op_dim[r], D, na, dim, AI));
-        }
-    }
+    if constexpr (ND)
+        if (aug) assemble_normal_dof(P, w, lane, es, st);
     __syncwarp();
 }
 
 // Assemble [Phi P; P^T 0 | B] into M (full symmetric storage).
+template <bool ND = false>
 __device__ void assemble_fp64(const StencilParams &P, const WarpSmem &w, int lane, int es, int eval_local) {
-    assemble_fp64_into(P, w, lane, es, eval_local, FullStore{w.M, P.n, mat_ld(P.n, P.nops)});
+    assemble_fp64_into<FullStore, ND>(P, w, lane, es, eval_local, FullStore{w.M, P.n, mat_ld(P.n, P.nops)});
 }
 
 // In-place LU with partial pivoting of M[:, 0:n] applied to the right-hand sides, then
@@ -557,12 +570,13 @@ __device__ __forceinline__ double df_to_double(dfl a) { return widen(a.hi) + wid
 // residual and the fallback), F the FP32 factor matrix (hi).  Right-hand sides in FP64.
 // Hermite stencils (a small minority) take the FP64 assembly and are rounded to F.
 // pairs (optional): the upper-triangle pairs (i <= j) in order, packed as i | j << 8.
+template <bool ND = false>
 __device__ void assemble_refined(const StencilParams &P, const WarpSmem &w, const Warp32 &u, int lane, int es,
                                  int eval_local, const uint16_t *pairs = nullptr) {
     // u.F == nullptr: only the FP64 system is needed (the register kernels narrow it)
     const int k = P.k, n = P.n, nops = P.nops, ld = mat_ld(n, nops), fld = f32_ld(n), dim = P.dim, nmon = P.nmon;
     if (eval_local != -2) {  // Hermite stencil
-        assemble_fp64(P, w, lane, es, eval_local);
+        assemble_fp64<ND>(P, w, lane, es, eval_local);
         if (u.F) {
             for (int t = lane; t < n * n; t += 32) {
                 int i = t / n, j = t - (t / n) * n;

@@ -28,42 +28,6 @@ __host__ __device__ constexpr int residual_blocks(int n) {
     return best;
 }
 
-// Shared memory of one warp in the register kernels: the FP64 system (WarpSmem), then the
-// FP64 solution, the FP32 increments, the split coordinates, pivots, reciprocal pivots and
-// the pivot-row broadcast buffer (16-byte aligned, rounded up to whole float4s).
-__host__ __device__ inline size_t reg_smem_bytes(int n, int k, int nops) {
-    size_t b = (warp_smem_bytes(n, k, nops) + 15) & ~(size_t)15;
-    b += sizeof(double) * (size_t)n * nops;                  // x
-    b += sizeof(float) * (size_t)n * nops;                   // xs
-    b += sizeof(float) * 6 * (size_t)k;                      // XH, XL
-    b += sizeof(int) * (size_t)n + sizeof(float) * (size_t)n;  // piv, rcp
-    b = (b + 15) & ~(size_t)15;
-    b += sizeof(float) * (((size_t)n + 3) & ~(size_t)3);     // rowbuf
-    return (b + 15) & ~(size_t)15;
-}
-
-struct RegSmem {
-    Warp32 u;  // u.F is unused (nullptr)
-    float *rcp, *rowbuf;
-};
-
-__device__ inline RegSmem carve_reg(char *base, int n, int k, int nops) {
-    RegSmem r;
-    size_t off = (warp_smem_bytes(n, k, nops) + 15) & ~(size_t)15;
-    r.u.x = reinterpret_cast<double *>(base + off);
-    r.u.r = nullptr;
-    r.u.F = nullptr;
-    r.u.v = reinterpret_cast<float *>(r.u.x + (size_t)n * nops);
-    r.u.XH = r.u.v + (size_t)n * nops;
-    r.u.XL = r.u.XH + 3 * (size_t)k;
-    r.u.piv = reinterpret_cast<int *>(r.u.XL + 3 * (size_t)k);
-    r.rcp = reinterpret_cast<float *>(r.u.piv + n);
-    size_t o2 = (size_t)(reinterpret_cast<char *>(r.rcp + n) - base);
-    o2 = (o2 + 15) & ~(size_t)15;
-    r.rowbuf = reinterpret_cast<float *>(base + o2);
-    return r;
-}
-
 // double -> float on the integer pipe, mantissa truncated (the FP32 factor only needs
 // FP32 accuracy): the exponent is rebased and the top 23 mantissa bits taken in one funnel
 // shift; magnitudes below FLT_MIN map to a signed zero (the entries here are bounded, so
@@ -73,6 +37,150 @@ __device__ __forceinline__ float narrow(double d) {
     const unsigned sign = hi & 0x80000000u;
     const unsigned mag = __funnelshift_l(lo, hi - 0x38000000u, 3);
     return __uint_as_float((hi & 0x7fffffffu) < 0x38100000u ? sign : (sign | mag));
+}
+
+// lower triangle by rows: A(i, j), j <= i, at tri(i) + j
+__host__ __device__ constexpr int tri(int i) { return (i * (i + 1)) >> 1; }
+
+// Shared memory of one warp of the register kernels: packed FP64 system (lower triangle by
+// rows) and its nops right-hand sides (n x nops), local coordinates and column indices, FP64
+// solution (n x nops), FP32 increments (n x nops), split coordinates, pivots, reciprocal
+// pivots and two pivot-row buffers (16-byte aligned, 4 * ceil(n/4) floats each).
+struct SplitSmem {
+    double *Mp, *bv, *X, *x;
+    int *cols, *piv;
+    float *xs, *XH, *XL, *rcp, *rowbuf;
+};
+
+__host__ __device__ inline size_t split_smem_bytes(int n, int k, int nops = 1) {
+    size_t b = sizeof(double) * ((size_t)tri(n) + 2 * (size_t)n * nops + 3 * (size_t)k);
+    b += sizeof(int) * ((size_t)k + n) + sizeof(float) * ((size_t)n * nops + 6 * (size_t)k + n);
+    b = (b + 15) & ~(size_t)15;
+    b += sizeof(float) * 8 * (((size_t)n + 3) / 4);  // two buffers, alternating by step
+    return (b + 15) & ~(size_t)15;
+}
+
+__device__ inline SplitSmem carve_split(char *base, int n, int k, int nops = 1) {
+    SplitSmem s;
+    double *d = reinterpret_cast<double *>(base);
+    s.Mp = d;
+    s.bv = s.Mp + tri(n);
+    s.X = s.bv + (size_t)n * nops;
+    s.x = s.X + 3 * k;
+    s.cols = reinterpret_cast<int *>(s.x + (size_t)n * nops);
+    s.piv = s.cols + k;
+    s.xs = reinterpret_cast<float *>(s.piv + n);
+    s.XH = s.xs + (size_t)n * nops;
+    s.XL = s.XH + 3 * k;
+    s.rcp = s.XL + 3 * k;
+    size_t o = (size_t)(reinterpret_cast<char *>(s.rcp + n) - base);
+    s.rowbuf = reinterpret_cast<float *>(base + ((o + 15) & ~(size_t)15));
+    return s;
+}
+
+// Column indices and local coordinates (scaled by 2^-es, as load_stencil) of stencil e.
+// Returns 1 without scaling when a boundary point is in the stencil: such stencils are
+// deferred to the general kernel.
+__device__ int load_interior(const StencilParams &P, int64_t e, const SplitSmem &s, int lane, int *es_out) {
+    const int k = P.k, dim = P.dim;
+    double x0[3] = {0, 0, 0};
+    for (int d = 0; d < dim; d++) x0[d] = P.eval[e * dim + d];
+    double r2max = 0.0;
+    bool anyb = false;
+    const int32_t *nbr = P.adj_ptr ? P.adjl + P.adj_ptr[e] : P.adjl + e * k;
+    for (int i = lane; i < k; i += 32) {
+        const int g = nbr[i];
+        s.cols[i] = g;
+        double r2 = 0.0;
+        for (int d = 0; d < 3; d++) {
+            const double dd = d < dim ? P.data[(int64_t)g * dim + d] - x0[d] : 0.0;
+            s.X[i * 3 + d] = dd;
+            r2 += dd * dd;
+        }
+        r2max = fmax(r2max, r2);
+        if (P.isb) anyb |= (P.isb[g] != 0);
+    }
+    if (__any_sync(0xffffffffu, anyb)) return 1;
+    {  // r2max >= 0: an integer max of its bit pattern
+        long long m = __double_as_longlong(r2max);
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        r2max = __longlong_as_double(m);
+    }
+    int es = 0;
+    if (r2max > 0.0) frexp(sqrt(r2max), &es);
+    *es_out = es;
+    __syncwarp();
+    for (int i = lane; i < k; i += 32)
+        for (int d = 0; d < dim; d++) s.X[i * 3 + d] = scale2(s.X[i * 3 + d], -es);
+    __syncwarp();
+    return 0;
+}
+
+// [Phi P; P^T 0] of an interior stencil in double-float (the arithmetic of
+// assemble_refined), stored as the packed lower triangle, and the right-hand sides.
+__device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int lane, int es, const uint16_t *pairs) {
+    const int k = P.k, n = P.n, dim = P.dim, nmon = P.nmon, nops = P.nops;
+    for (int i = lane; i < k; i += 32)
+        for (int d = 0; d < 3; d++) {
+            const double xv = d < dim ? s.X[i * 3 + d] : 0.0;
+            const float hi = __double2float_rn(xv);
+            s.XH[i * 3 + d] = hi;
+            s.XL[i * 3 + d] = __double2float_rn(xv - widen(hi));
+        }
+    for (int t = lane; t < tri(n) - tri(k); t += 32) s.Mp[tri(k) + t] = 0.0;  // rows k..n-1; the
+    __syncwarp();                                                           // P^T part is set below
+    const int npairs = k * (k + 1) / 2;
+    for (int p = lane; p < npairs; p += 32) {
+        const unsigned pk = pairs[p];
+        const int i = (int)(pk & 0xffu), j = (int)(pk >> 8);  // i <= j
+        dfl r2 = {0.0f, 0.0f};
+        for (int d = 0; d < dim; d++) {
+            dfl dd = ts(s.XH[i * 3 + d], -s.XH[j * 3 + d]);
+            dd = qts(dd.hi, dd.lo + (s.XL[i * 3 + d] - s.XL[j * 3 + d]));
+            r2 = df_add(r2, df_sqr(dd));
+        }
+        const dfl r = df_sqrt(r2);
+        dfl phi;
+        switch (P.phs) {
+        case 1: phi = r; break;
+        case 3: phi = df_mul(r2, r); break;
+        case 5: phi = df_mul(df_sqr(r2), r); break;
+        default: phi = df_mul(df_mul(df_sqr(r2), r2), r); break;
+        }
+        s.Mp[tri(j) + i] = df_to_double(phi);
+    }
+    const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
+    for (int i = lane; i < k; i += 32) {
+        dfl xd[3];
+        for (int d = 0; d < 3; d++) xd[d] = {s.XH[i * 3 + d], s.XL[i * 3 + d]};
+        for (int m = 0; m < nmon; m++) {
+            dfl v = {1.0f, 0.0f};
+            for (int d = 0; d < dim; d++)
+                for (int t = 0; t < P.exps[m][d]; t++) v = df_mul(v, xd[d]);
+            s.Mp[tri(k + m) + i] = df_to_double(v);
+        }
+        double D[3];
+        for (int d = 0; d < dim; d++) D[d] = -s.X[i * 3 + d];
+        for (int q = 0; q < nops; q++) s.bv[i * nops + q] = phs_op<double>(P.phs, P.op_code[q], P.op_dim[q], D, dim, AI);
+    }
+    for (int t = lane; t < nmon * nops; t += 32) {
+        const int m = t / nops, q = t - (t / nops) * nops;
+        s.bv[(k + m) * nops + q] = mono_op_at_origin(P, m, P.op_code[q], P.op_dim[q]);
+    }
+    __syncwarp();
+}
+
+// A(i, j) of the packed symmetric system
+__device__ __forceinline__ double pk_at(const double *Mp, int i, int j) {
+    return Mp[i >= j ? tri(i) + j : tri(j) + i];
+}
+
+// Hands stencil e to the general refined kernel (its FP64 fallback included).
+__device__ __forceinline__ void split_defer(const StencilParams &P, int64_t e, int lane) {
+    if (lane == 0) {
+        const unsigned long long t = atomicAdd(&P.counters[7], 1ull);
+        P.defer[t] = (int32_t)e;
+    }
 }
 
 template <int N, int R>
@@ -227,16 +335,11 @@ __device__ void reglu_forward(RegLU<N, R> &L, float (&rhs)[RegLU<N, R>::ROWS][R]
 
 template <int N, int R>
 __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams P, int wpb, size_t warp_bytes) {
-    constexpr int ROWS = RegLU<N, R>::ROWS, W = RegLU<N, R>::W;
+    constexpr int ROWS = RegLU<N, R>::ROWS;
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    char *base = smem + wib * warp_bytes;
-    WarpSmem w = carve(base, P.n, P.k, P.nops);
-    const RegSmem rs = carve_reg(base, P.n, P.k, P.nops);
-    const Warp32 &u = rs.u;
-    const int ld = mat_ld(N, R);
-    float *rowbuf = rs.rowbuf;
-    float *xs = u.v;  // N x R floats
+    const SplitSmem s = carve_split(smem + wib * warp_bytes, N, P.k, R);
+    float *xs = s.xs;  // N x R floats
     // upper-triangle pair table of the RBF block, shared by the block's warps
     uint16_t *pairs = reinterpret_cast<uint16_t *>(smem + wpb * warp_bytes);
     for (int p = threadIdx.x; p < P.k * (P.k + 1) / 2; p += blockDim.x) {
@@ -251,39 +354,38 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
         // behind the load and assembly (lane t holds entry t and t + 32; one operator)
         float seed_reg[ROWS];
 #pragma unroll
-        for (int s = 0; s < ROWS; s++) {
-            const int i = lane + 32 * s;
-            seed_reg[s] = (R == 1 && P.seed && i < P.k) ? __ldg(&P.seed[e * P.k + i]) : 0.0f;
+        for (int r = 0; r < ROWS; r++) {
+            const int i = lane + 32 * r;
+            seed_reg[r] = (R == 1 && P.seed && i < P.k) ? __ldg(&P.seed[e * P.k + i]) : 0.0f;
         }
-        int es = 0, eval_local = -2;
-        int st = load_stencil(P, e, w, lane, &es, &eval_local);
-        if (st != 0) {
+        // boundary stencils (Hermite rows) go to the general refined kernel
+        int es = 0;
+        if (load_interior(P, e, s, lane, &es) != 0) {
+            split_defer(P, e, lane);
             __syncwarp();
             continue;
         }
-        assemble_refined(P, w, u, lane, es, eval_local, pairs);
-        float *rcp = rs.rcp;
+        assemble_packed(P, s, lane, es, pairs);
         RegLU<N, R> L;
 #pragma unroll
-        for (int s = 0; s < ROWS; s++) {
-            const int r = lane + 32 * s;
-            const bool act = r < N;
-            L.step[s] = act ? N + 1 : -1;
+        for (int r = 0; r < ROWS; r++) {
+            const int i = lane + 32 * r;
+            const bool act = i < N;
+            L.step[r] = act ? N + 1 : -1;
 #pragma unroll
-            for (int cc = 0; cc < N; cc++) L.a[s][cc] = act ? narrow(w.M[r * ld + cc]) : 0.0f;
+            for (int cc = 0; cc < N; cc++) L.a[r][cc] = act ? narrow(pk_at(s.Mp, act ? i : 0, cc)) : 0.0f;
         }
-        __syncwarp();
         // start of the refinement: x0 = 0 and rhs = b, or with a learned seed x0 = [w_pred; 0]
         // and rhs = b - A32 x0, formed here from the FP32 rows while they are still unfactored
         float rhs[ROWS][R];
         if (P.seed) {
             if constexpr (R == 1) {
 #pragma unroll
-                for (int s = 0; s < ROWS; s++) {
-                    const int t = lane + 32 * s;
+                for (int r = 0; r < ROWS; r++) {
+                    const int t = lane + 32 * r;
                     if (t < N) {
-                        xs[t] = seed_reg[s];
-                        u.x[t] = widen(seed_reg[s]);
+                        xs[t] = seed_reg[r];
+                        s.x[t] = widen(seed_reg[r]);
                     }
                 }
             } else {
@@ -291,34 +393,34 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
                     const int i = t / R;
                     const float sv = i < P.k ? __ldg(&P.seed[e * P.k + i]) : 0.0f;
                     xs[t] = sv;
-                    u.x[t] = widen(sv);
+                    s.x[t] = widen(sv);
                 }
             }
             __syncwarp();
 #pragma unroll
-            for (int s = 0; s < ROWS; s++) {
-                const int i = lane + 32 * s;
+            for (int r = 0; r < ROWS; r++) {
+                const int i = lane + 32 * r;
 #pragma unroll
                 for (int q = 0; q < R; q++) {
-                    float acc = i < N ? (float)w.M[(i < N ? i : 0) * ld + N + q] : 0.0f;
+                    float acc = i < N ? narrow(s.bv[(i < N ? i : 0) * R + q]) : 0.0f;
                     static_for<0, N, 1>([&](auto jI) {
                         constexpr int j = decltype(jI)::value;
-                        acc = fmaf(-L.a[s][j], xs[j * R + q], acc);
+                        acc = fmaf(-L.a[r][j], xs[j * R + q], acc);
                     });
-                    rhs[s][q] = acc;
+                    rhs[r][q] = acc;
                 }
             }
         } else {
-            for (int t = lane; t < N * R; t += 32) u.x[t] = 0.0;
+            for (int t = lane; t < N * R; t += 32) s.x[t] = 0.0;
 #pragma unroll
-            for (int s = 0; s < ROWS; s++) {
-                const int i = lane + 32 * s;
+            for (int r = 0; r < ROWS; r++) {
+                const int i = lane + 32 * r;
 #pragma unroll
-                for (int q = 0; q < R; q++) rhs[s][q] = i < N ? (float)w.M[(i < N ? i : 0) * ld + N + q] : 0.0f;
+                for (int q = 0; q < R; q++) rhs[r][q] = i < N ? narrow(s.bv[(i < N ? i : 0) * R + q]) : 0.0f;
             }
         }
         __syncwarp();
-        const bool ok = reglu_factor<N, R>(L, rowbuf, u.piv, rcp, lane);
+        const bool ok = reglu_factor<N, R>(L, s.rowbuf, s.piv, s.rcp, lane);
         bool accepted = false;
         double est_final = 0.0;
         int nres = 0;
@@ -341,13 +443,14 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
                     for (int q = 0; q < R; q++) acc[q] = 0.0;
                     if (i < N) {
                         const int j0 = jb * JL;
+                        const int ti = tri(i);
 #pragma unroll 2
                         for (int jj = 0; jj < JL; jj++) {
                             const int j = j0 + jj;
                             if (j < N) {
-                                const double aij = w.M[j * ld + i];
+                                const double aij = s.Mp[j <= i ? ti + j : tri(j) + i];
 #pragma unroll
-                                for (int q = 0; q < R; q++) acc[q] = fma(-aij, u.x[j * R + q], acc[q]);
+                                for (int q = 0; q < R; q++) acc[q] = fma(-aij, s.x[j * R + q], acc[q]);
                             }
                         }
                     }
@@ -357,14 +460,14 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
                         for (int q = 0; q < R; q++) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
                     if (i < N && jb == 0)
 #pragma unroll
-                        for (int q = 0; q < R; q++) rbuf[i * R + q] = __double2float_rn(w.M[i * ld + N + q] + acc[q]);
+                        for (int q = 0; q < R; q++) rbuf[i * R + q] = __double2float_rn(s.bv[i * R + q] + acc[q]);
                 }
                 __syncwarp();
 #pragma unroll
-                for (int s = 0; s < ROWS; s++) {
-                    const int i = lane + 32 * s;
+                for (int r = 0; r < ROWS; r++) {
+                    const int i = lane + 32 * r;
 #pragma unroll
-                    for (int q = 0; q < R; q++) rhs[s][q] = i < N ? rbuf[i * R + q] : 0.0f;
+                    for (int q = 0; q < R; q++) rhs[r][q] = i < N ? rbuf[(i < N ? i : 0) * R + q] : 0.0f;
                 }
                 __syncwarp();
             };
@@ -373,15 +476,15 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
             const float tolf = (float)P.tol;
             float dprev = 0.0f;
             for (int step = 0;; step++) {
-                reglu_forward<N, R>(L, rhs, u.piv, lane);
-                reglu_back<N, R>(L, rhs, u.piv, rcp, xs, lane);
+                reglu_forward<N, R>(L, rhs, s.piv, lane);
+                reglu_back<N, R>(L, rhs, s.piv, s.rcp, xs, lane);
                 float dmaxf = 0.0f, xmaxf = 0.0f;
                 for (int t = lane; t < N * R; t += 32) {
                     const float d = xs[t];
-                    u.x[t] += widen(d);
+                    s.x[t] += widen(d);
                     if (t / R < P.k) {
                         dmaxf = fmaxf(dmaxf, fabsf(d));
-                        xmaxf = fmaxf(xmaxf, fabsf(__double2float_rn(u.x[t])));
+                        xmaxf = fmaxf(xmaxf, fabsf(__double2float_rn(s.x[t])));
                     }
                 }
 #pragma unroll
@@ -420,33 +523,27 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
         }
         if (lane == 0 && ok) atomicAdd(&P.counters[4], (unsigned long long)nres);
         if (accepted) {
-            scatter_row(P, e, w, lane, es, u.x, R, 1);
+            WarpSmem w;
+            w.cols = s.cols;
+            scatter_row(P, e, w, lane, es, s.x, R, 1);
             if (lane == 0) {
                 if (P.status) P.status[e] = 0;
                 atomicMax(reinterpret_cast<unsigned long long *>(P.max_resid),
                           (unsigned long long)__double_as_longlong(est_final));
             }
         } else {
-            if (eval_local == -2) assemble_fp64(P, w, lane, es, eval_local);
-            const bool ok64 = lu_solve_fp64(w.M, N, R, lane);
-            if (ok64) {
-                scatter_row(P, e, w, lane, es, w.M + N, ld, 1);
-                if (lane == 0) {
-                    if (P.status) P.status[e] = 3;
-                    atomicAdd(&P.counters[2], 1ull);
-                }
-            } else if (lane == 0) {
-                if (P.status) P.status[e] = 1;
-                atomicAdd(&P.counters[0], 1ull);
-            }
+            split_defer(P, e, lane);  // the general kernel's refinement, then its FP64 fallback
         }
         __syncwarp();
     }
 }
 
+// Launches the register kernel; the caller finishes the stencils it hands over (boundary
+// stencils, failed refinements: P.defer, counted in P.counters[7]) with the general kernel.
 template <int N, int R>
 int launch_refined_reg(rbf_ctx *ctx, const StencilParams &P) {
-    const size_t wb = reg_smem_bytes(P.n, P.k, P.nops);
+    if (!P.defer) return rbf_fail(ctx, RBF_ERR_INTERNAL, "register kernel without a deferred list");
+    const size_t wb = split_smem_bytes(N, P.k, R);
     const int wpb = 4;
     const size_t smem = wb * wpb + sizeof(uint16_t) * (size_t)(P.k * (P.k + 1) / 2);
     RBF_CUDA(ctx, cudaFuncSetAttribute(build_refined_reg_kernel<N, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,

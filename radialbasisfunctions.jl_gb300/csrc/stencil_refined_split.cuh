@@ -23,9 +23,6 @@
 
 namespace {
 
-// lower triangle by rows: A(i, j), j <= i, at tri(i) + j
-__host__ __device__ constexpr int tri(int i) { return (i * (i + 1)) >> 1; }
-
 template <int N>
 struct SplitLU {
     static constexpr int NX = N - 32;        // extra rows
@@ -34,143 +31,6 @@ struct SplitLU {
     float b[PW];                             // piece (lane & 3) of extra row 32 + (lane >> 2)
     int mstep, xstep;  // step at which the row was the pivot; N + 1: not yet; -1: padding
 };
-
-// Shared memory of one warp: packed FP64 system and right-hand side, local coordinates and
-// column indices, FP64 solution, FP32 increments, split coordinates, pivots, reciprocal
-// pivots and two pivot-row buffers (16-byte aligned, 4 * ceil(n/4) floats each).
-struct SplitSmem {
-    double *Mp, *bv, *X, *x;
-    int *cols, *piv;
-    float *xs, *XH, *XL, *rcp, *rowbuf;
-};
-
-__host__ __device__ inline size_t split_smem_bytes(int n, int k) {
-    size_t b = sizeof(double) * ((size_t)tri(n) + 2 * (size_t)n + 3 * (size_t)k);
-    b += sizeof(int) * ((size_t)k + n) + sizeof(float) * ((size_t)n + 6 * (size_t)k + n);
-    b = (b + 15) & ~(size_t)15;
-    b += sizeof(float) * 8 * (((size_t)n + 3) / 4);  // two buffers, alternating by step
-    return (b + 15) & ~(size_t)15;
-}
-
-__device__ inline SplitSmem carve_split(char *base, int n, int k) {
-    SplitSmem s;
-    double *d = reinterpret_cast<double *>(base);
-    s.Mp = d;
-    s.bv = s.Mp + tri(n);
-    s.X = s.bv + n;
-    s.x = s.X + 3 * k;
-    s.cols = reinterpret_cast<int *>(s.x + n);
-    s.piv = s.cols + k;
-    s.xs = reinterpret_cast<float *>(s.piv + n);
-    s.XH = s.xs + n;
-    s.XL = s.XH + 3 * k;
-    s.rcp = s.XL + 3 * k;
-    size_t o = (size_t)(reinterpret_cast<char *>(s.rcp + n) - base);
-    s.rowbuf = reinterpret_cast<float *>(base + ((o + 15) & ~(size_t)15));
-    return s;
-}
-
-// Column indices and local coordinates (scaled by 2^-es, as load_stencil) of stencil e.
-// Returns 1 without scaling when a boundary point is in the stencil: such stencils are
-// deferred to the general kernel.
-__device__ int load_interior(const StencilParams &P, int64_t e, const SplitSmem &s, int lane, int *es_out) {
-    const int k = P.k, dim = P.dim;
-    double x0[3] = {0, 0, 0};
-    for (int d = 0; d < dim; d++) x0[d] = P.eval[e * dim + d];
-    double r2max = 0.0;
-    bool anyb = false;
-    const int32_t *nbr = P.adj_ptr ? P.adjl + P.adj_ptr[e] : P.adjl + e * k;
-    for (int i = lane; i < k; i += 32) {
-        const int g = nbr[i];
-        s.cols[i] = g;
-        double r2 = 0.0;
-        for (int d = 0; d < 3; d++) {
-            const double dd = d < dim ? P.data[(int64_t)g * dim + d] - x0[d] : 0.0;
-            s.X[i * 3 + d] = dd;
-            r2 += dd * dd;
-        }
-        r2max = fmax(r2max, r2);
-        if (P.isb) anyb |= (P.isb[g] != 0);
-    }
-    if (__any_sync(0xffffffffu, anyb)) return 1;
-    {  // r2max >= 0: an integer max of its bit pattern
-        long long m = __double_as_longlong(r2max);
-        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-        r2max = __longlong_as_double(m);
-    }
-    int es = 0;
-    if (r2max > 0.0) frexp(sqrt(r2max), &es);
-    *es_out = es;
-    __syncwarp();
-    for (int i = lane; i < k; i += 32)
-        for (int d = 0; d < dim; d++) s.X[i * 3 + d] = scale2(s.X[i * 3 + d], -es);
-    __syncwarp();
-    return 0;
-}
-
-// [Phi P; P^T 0] of an interior stencil in double-float (the arithmetic of
-// assemble_refined), stored as the packed lower triangle, and the right-hand side.
-__device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int lane, int es, const uint16_t *pairs) {
-    const int k = P.k, n = P.n, dim = P.dim, nmon = P.nmon;
-    for (int i = lane; i < k; i += 32)
-        for (int d = 0; d < 3; d++) {
-            const double xv = d < dim ? s.X[i * 3 + d] : 0.0;
-            const float hi = __double2float_rn(xv);
-            s.XH[i * 3 + d] = hi;
-            s.XL[i * 3 + d] = __double2float_rn(xv - widen(hi));
-        }
-    for (int t = lane; t < tri(n) - tri(k); t += 32) s.Mp[tri(k) + t] = 0.0;  // rows k..n-1; the
-    __syncwarp();                                                           // P^T part is set below
-    const int npairs = k * (k + 1) / 2;
-    for (int p = lane; p < npairs; p += 32) {
-        const unsigned pk = pairs[p];
-        const int i = (int)(pk & 0xffu), j = (int)(pk >> 8);  // i <= j
-        dfl r2 = {0.0f, 0.0f};
-        for (int d = 0; d < dim; d++) {
-            dfl dd = ts(s.XH[i * 3 + d], -s.XH[j * 3 + d]);
-            dd = qts(dd.hi, dd.lo + (s.XL[i * 3 + d] - s.XL[j * 3 + d]));
-            r2 = df_add(r2, df_sqr(dd));
-        }
-        const dfl r = df_sqrt(r2);
-        dfl phi;
-        switch (P.phs) {
-        case 1: phi = r; break;
-        case 3: phi = df_mul(r2, r); break;
-        case 5: phi = df_mul(df_sqr(r2), r); break;
-        default: phi = df_mul(df_mul(df_sqr(r2), r2), r); break;
-        }
-        s.Mp[tri(j) + i] = df_to_double(phi);
-    }
-    const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
-    for (int i = lane; i < k; i += 32) {
-        dfl xd[3];
-        for (int d = 0; d < 3; d++) xd[d] = {s.XH[i * 3 + d], s.XL[i * 3 + d]};
-        for (int m = 0; m < nmon; m++) {
-            dfl v = {1.0f, 0.0f};
-            for (int d = 0; d < dim; d++)
-                for (int t = 0; t < P.exps[m][d]; t++) v = df_mul(v, xd[d]);
-            s.Mp[tri(k + m) + i] = df_to_double(v);
-        }
-        double D[3];
-        for (int d = 0; d < dim; d++) D[d] = -s.X[i * 3 + d];
-        s.bv[i] = phs_op<double>(P.phs, P.op_code[0], P.op_dim[0], D, dim, AI);
-    }
-    for (int m = lane; m < nmon; m += 32) s.bv[k + m] = mono_op_at_origin(P, m, P.op_code[0], P.op_dim[0]);
-    __syncwarp();
-}
-
-// A(i, j) of the packed symmetric system
-__device__ __forceinline__ double pk_at(const double *Mp, int i, int j) {
-    return Mp[i >= j ? tri(i) + j : tri(j) + i];
-}
-
-template <int N>
-__device__ __forceinline__ void split_defer(const StencilParams &P, int64_t e, int lane) {
-    if (lane == 0) {
-        const unsigned long long t = atomicAdd(&P.counters[7], 1ull);
-        P.defer[t] = (int32_t)e;
-    }
-}
 
 template <int N>
 __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilParams P, int wpb, size_t warp_bytes) {
@@ -200,7 +60,7 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
         const float seed_x = (P.seed && lane < NX && 32 + lane < P.k) ? __ldg(&P.seed[e * P.k + 32 + lane]) : 0.0f;
         int es = 0;
         if (load_interior(P, e, s, lane, &es) != 0) {
-            split_defer<N>(P, e, lane);
+            split_defer(P, e, lane);
             __syncwarp();
             continue;
         }
@@ -434,7 +294,7 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
                           (unsigned long long)__double_as_longlong(est_final));
             }
         } else {
-            split_defer<N>(P, e, lane);
+            split_defer(P, e, lane);
         }
         __syncwarp();
     }

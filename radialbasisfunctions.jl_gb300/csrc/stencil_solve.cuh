@@ -127,7 +127,9 @@ __device__ void finish_fp32r_warp(const StencilParams &P, int64_t e, const WarpS
     __syncwarp();
 }
 
-// One stencil e on one warp, FP32 factorisation + FP64 refinement, FP64 fallback.
+// One stencil e on one warp, FP32 factorisation + FP64 refinement, FP64 fallback (ND: the
+// normal-derivative builds' instantiation).
+template <bool ND = false>
 __device__ void solve_fp32r_warp(const StencilParams &P, int64_t e, const WarpSmem &w, const Warp32 &u, int lane) {
     int es = 0, eval_local = -2;
     int st = load_stencil(P, e, w, lane, &es, &eval_local);
@@ -135,7 +137,7 @@ __device__ void solve_fp32r_warp(const StencilParams &P, int64_t e, const WarpSm
         __syncwarp();
         return;
     }
-    assemble_refined(P, w, u, lane, es, eval_local);
+    assemble_refined<ND>(P, w, u, lane, es, eval_local);
     const bool ok = lu_factor_fp32(u.F, u.piv, P.n, lane);
     double est_final = 0.0;
     const bool accepted = ok && refine_fp32_warp(P, w, u, lane, &est_final);
