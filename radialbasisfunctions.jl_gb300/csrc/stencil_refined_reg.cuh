@@ -45,7 +45,8 @@ __host__ __device__ constexpr int tri(int i) { return (i * (i + 1)) >> 1; }
 // Shared memory of one warp of the register kernels: packed FP64 system (lower triangle by
 // rows) and its nops right-hand sides (n x nops), local coordinates and column indices, FP64
 // solution (n x nops), FP32 increments (n x nops), split coordinates, pivots, reciprocal
-// pivots and two pivot-row buffers (16-byte aligned, 4 * ceil(n/4) floats each).
+// pivots and two pivot-row buffers (16-byte aligned, 4 * ceil(n/4) floats each), which the
+// solves reuse for the right-hand sides in pivot order.
 struct SplitSmem {
     double *Mp, *bv, *X, *x;
     int *cols, *piv;
@@ -56,7 +57,10 @@ __host__ __device__ inline size_t split_smem_bytes(int n, int k, int nops = 1) {
     size_t b = sizeof(double) * ((size_t)tri(n) + 2 * (size_t)n * nops + 3 * (size_t)k);
     b += sizeof(int) * ((size_t)k + n) + sizeof(float) * ((size_t)n * nops + 6 * (size_t)k + n);
     b = (b + 15) & ~(size_t)15;
-    b += sizeof(float) * 8 * (((size_t)n + 3) / 4);  // two buffers, alternating by step
+    // two pivot-row buffers, alternating by step; after the inversion the right-hand sides
+    // in pivot order (n x nops)
+    const size_t rb = 8 * (((size_t)n + 3) / 4), rr = (((size_t)n + 3) & ~(size_t)3) * nops;
+    b += sizeof(float) * (rb > rr ? rb : rr);
     return (b + 15) & ~(size_t)15;
 }
 
@@ -186,7 +190,7 @@ __device__ __forceinline__ void split_defer(const StencilParams &P, int64_t e, i
 template <int N, int R>
 struct RegLU {
     static constexpr int ROWS = (N + 31) / 32;
-    static constexpr int W = N;  // matrix only; right-hand sides go through reglu_forward/back
+    static constexpr int W = N;  // matrix only; right-hand sides go through reg_apply_inverse
     float a[ROWS][W];
     int step[ROWS];  // elimination step at which the row was the pivot; N+1: not yet; -1: padding
 };
@@ -200,137 +204,121 @@ __device__ __forceinline__ void static_for(F &&f) {
     }
 }
 
-// Factor in place; returns false on an exactly zero or non-finite pivot.  rowbuf: W floats,
-// piv: N ints, rcp: N floats (pivot rows and reciprocal pivots, in elimination order).
+// Gauss-Jordan inversion in place with partial pivoting (largest |a|, ties to the lower row;
+// the rows not yet used as pivots evolve exactly as in an LU).  Each row slot is a window of
+// N registers: before step c it holds columns c..N-1 of the row, then the row's entries of
+// the c inverse columns formed so far.  Step c eliminates column c (window position 0) from
+// every row but the pivot row, shifts each window left by one and appends the row's entry of
+// the new inverse column (minus the multiplier; 1 in the pivot row, which stays unscaled and
+// is multiplied by its reciprocal pivot at the end).  Every step runs the same code, so the
+// loop stays rolled.  Afterwards the row pivoted at step c holds row c of the inverse, its
+// window position t the column of the row pivoted at step t.  rowbuf: two buffers of
+// 4 ceil(N/4) floats.  Returns false on a zero, subnormal or non-finite pivot.
 template <int N, int R>
-__device__ bool reglu_factor(RegLU<N, R> &L, float *rowbuf, int *piv, float *rcp, int lane) {
-    constexpr int ROWS = RegLU<N, R>::ROWS, W = RegLU<N, R>::W;
+__device__ bool reg_invert(RegLU<N, R> &L, float *rowbuf2, int lane) {
+    constexpr int ROWS = RegLU<N, R>::ROWS, W4 = (N + 3) / 4;
     bool ok = true;
-    static_for<0, N, 1>([&](auto cI) {
-        constexpr int c = decltype(cI)::value;
-        // pivot: largest |a| among rows not yet used (magnitude bits with the 6 low bits
-        // replaced by 63 - row, so one max-reduction also breaks near-ties to the lower row)
+    float rsc[ROWS];
+#pragma unroll
+    for (int r = 0; r < ROWS; r++) rsc[r] = 1.0f;
+#pragma unroll 1
+    for (int c = 0; c < N; c++) {
+        float *const rowbuf = rowbuf2 + (c & 1) * 4 * W4;  // alternating: one barrier per step
         unsigned key = 0u;
 #pragma unroll
-        for (int s = 0; s < ROWS; s++) {
-            const unsigned kk = (__float_as_uint(fabsf(L.a[s][c])) & ~63u) | (unsigned)(63 - (lane + 32 * s));
-            key = max(key, L.step[s] == N + 1 ? kk : 0u);
+        for (int r = 0; r < ROWS; r++) {
+            const unsigned kk = (__float_as_uint(fabsf(L.a[r][0])) & ~63u) | (unsigned)(63 - (lane + 32 * r));
+            key = max(key, L.step[r] == N + 1 ? kk : 0u);
         }
         key = __reduce_max_sync(0xffffffffu, key);
         const int brow = 63 - (int)(key & 63u);
-        const int pl = brow & 31, ps = brow >> 5;
-        // the slot ps is the same in every lane: one branch per slot publishes the row
-        // straight from its registers
 #pragma unroll
-        for (int s = 0; s < ROWS; s++) {
-            if (s == ps && lane == pl) {
-                L.step[s] = c;
+        for (int r = 0; r < ROWS; r++) {
+            if (brow == lane + 32 * r) {
 #pragma unroll
-                for (int q4 = c / 4; q4 < (W + 3) / 4; q4++) {
+                for (int q4 = 0; q4 < W4; q4++) {
                     float4 v;
-                    v.x = (4 * q4 + 0 < W) ? L.a[s][(4 * q4 + 0 < W) ? 4 * q4 + 0 : 0] : 0.0f;
-                    v.y = (4 * q4 + 1 < W) ? L.a[s][(4 * q4 + 1 < W) ? 4 * q4 + 1 : 0] : 0.0f;
-                    v.z = (4 * q4 + 2 < W) ? L.a[s][(4 * q4 + 2 < W) ? 4 * q4 + 2 : 0] : 0.0f;
-                    v.w = (4 * q4 + 3 < W) ? L.a[s][(4 * q4 + 3 < W) ? 4 * q4 + 3 : 0] : 0.0f;
+                    v.x = L.a[r][4 * q4];
+                    v.y = 4 * q4 + 1 < N ? L.a[r][4 * q4 + 1 < N ? 4 * q4 + 1 : 0] : 0.0f;
+                    v.z = 4 * q4 + 2 < N ? L.a[r][4 * q4 + 2 < N ? 4 * q4 + 2 : 0] : 0.0f;
+                    v.w = 4 * q4 + 3 < N ? L.a[r][4 * q4 + 3 < N ? 4 * q4 + 3 : 0] : 0.0f;
                     reinterpret_cast<float4 *>(rowbuf)[q4] = v;
                 }
             }
         }
         __syncwarp();
-        const float pvt = rowbuf[c];
-        ok &= (pvt != 0.0f) && isfinite(pvt);
-        // correctly rounded reciprocal without the division's slow path (a zero or
-        // non-finite pivot has already failed the factorisation)
-        const float inv = __frcp_rn(pvt);
-        if (lane == 0) {
-            piv[c] = brow;
-            rcp[c] = inv;
-        }
-        // elimination; up to 40 rows it is branch-free: rows already used as pivots (and
-        // padding rows) get a zero multiplier, which leaves them unchanged (larger systems
-        // keep the branch, which needs fewer live registers)
+        const float pvt = rowbuf[0];
+        // approximate reciprocal (the FP32 inverse only preconditions the refinement)
+        float inv;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(pvt));
+        ok &= (pvt != 0.0f) && isfinite(pvt) && isfinite(inv);
 #pragma unroll
-        for (int s = 0; s < ROWS; s++) {
-            const bool act = L.step[s] == N + 1;
-            if constexpr (N > 40)
-                if (!act) continue;
-            const float l = act ? L.a[s][c] * inv : 0.0f;
-            L.a[s][c] = act ? l : L.a[s][c];
+        for (int r = 0; r < ROWS; r++) {
+            const bool pr = brow == lane + 32 * r;
+            if (pr) {
+                L.step[r] = c;
+                rsc[r] = inv;
+            }
+            const float m = pr ? 0.0f : L.a[r][0] * inv;
 #pragma unroll
-            for (int q4 = (c + 1) / 4; q4 < (W + 3) / 4; q4++) {
+            for (int q4 = 0; q4 < W4; q4++) {
                 const float4 v = reinterpret_cast<const float4 *>(rowbuf)[q4];
                 const float vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
                 for (int t = 0; t < 4; t++) {
-                    const int cc = 4 * q4 + t;
-                    if (cc > c && cc < W) L.a[s][cc < W ? cc : 0] = fmaf(-l, vv[t], L.a[s][cc < W ? cc : 0]);
+                    const int j = 4 * q4 + t;
+                    if (j >= 1 && j < N) L.a[r][j - 1 >= 0 ? j - 1 : 0] = fmaf(-m, vv[t], L.a[r][j < N ? j : 0]);
                 }
             }
+            L.a[r][N - 1] = pr ? 1.0f : -m;
         }
-        __syncwarp();
-    });
+    }
+#pragma unroll
+    for (int r = 0; r < ROWS; r++)
+#pragma unroll
+        for (int j = 0; j < N; j++) L.a[r][j] *= rsc[r];
+    __syncwarp();
     return ok;
 }
 
-// Back substitution of right-hand sides held per row (already forward-substituted); x
-// (N x R floats, row-major) is written to xs.
+// x = A32^{-1} rhs for the R right-hand sides held per row: every row puts its right-hand
+// sides at its pivot step in rp (N x R floats, 16-byte aligned), then each row's dot products
+// with the inverse's row are the unknowns at its pivot step, written to xs (N x R).
 template <int N, int R>
-__device__ void reglu_back(RegLU<N, R> &L, float (&rhs)[RegLU<N, R>::ROWS][R], const int *piv, const float *rcp,
-                           float *xs, int lane) {
+__device__ void reg_apply_inverse(const RegLU<N, R> &L, const float (&rhs)[RegLU<N, R>::ROWS][R], float *rp,
+                                  float *xs, int lane) {
     constexpr int ROWS = RegLU<N, R>::ROWS;
-    static_for<N - 1, -1, -1>([&](auto cI) {
-        constexpr int c = decltype(cI)::value;
-        const int p = piv[c];
-        const int pl = p & 31, ps = p >> 5;
-        const float rc = rcp[c];
-        float xq[R];
 #pragma unroll
-        for (int q = 0; q < R; q++) {
-            float v = rhs[0][q];
+    for (int r = 0; r < ROWS; r++)
+        if (L.step[r] >= 0)
 #pragma unroll
-            for (int t = 1; t < ROWS; t++)
-                if (ps == t) v = rhs[t][q];
-            xq[q] = __shfl_sync(0xffffffffu, v, pl) * rc;
-        }
-        if (lane < R) {
-#pragma unroll
-            for (int q = 0; q < R; q++)
-                if (q == lane) xs[c * R + q] = xq[q];
-        }
-#pragma unroll
-        for (int s = 0; s < ROWS; s++)
-            if (L.step[s] >= 0 && L.step[s] < c) {
-#pragma unroll
-                for (int q = 0; q < R; q++) rhs[s][q] = fmaf(-L.a[s][c], xq[q], rhs[s][q]);
-            }
-    });
+            for (int q = 0; q < R; q++) rp[L.step[r] * R + q] = rhs[r][q];
     __syncwarp();
-}
-
-// Forward substitution of right-hand sides (held per row) with the stored multipliers.
-template <int N, int R>
-__device__ void reglu_forward(RegLU<N, R> &L, float (&rhs)[RegLU<N, R>::ROWS][R], const int *piv, int lane) {
-    constexpr int ROWS = RegLU<N, R>::ROWS;
-    static_for<0, N, 1>([&](auto cI) {
-        constexpr int c = decltype(cI)::value;
-        const int p = piv[c];
-        const int pl = p & 31, ps = p >> 5;
-        float yq[R];
 #pragma unroll
-        for (int q = 0; q < R; q++) {
-            float v = rhs[0][q];
+    for (int r = 0; r < ROWS; r++) {
+        float acc[R];
 #pragma unroll
-            for (int t = 1; t < ROWS; t++)
-                if (ps == t) v = rhs[t][q];
-            yq[q] = __shfl_sync(0xffffffffu, v, pl);
-        }
+        for (int q = 0; q < R; q++) acc[q] = 0.0f;
+        if constexpr (R == 4) {
 #pragma unroll
-        for (int s = 0; s < ROWS; s++)
-            if (L.step[s] > c) {
-#pragma unroll
-                for (int q = 0; q < R; q++) rhs[s][q] = fmaf(-L.a[s][c], yq[q], rhs[s][q]);
+            for (int j = 0; j < N; j++) {
+                const float4 v = reinterpret_cast<const float4 *>(rp)[j];
+                acc[0] = fmaf(L.a[r][j], v.x, acc[0]);
+                acc[1] = fmaf(L.a[r][j], v.y, acc[1]);
+                acc[2] = fmaf(L.a[r][j], v.z, acc[2]);
+                acc[3] = fmaf(L.a[r][j], v.w, acc[3]);
             }
-    });
+        } else {
+#pragma unroll
+            for (int j = 0; j < N; j++)
+#pragma unroll
+                for (int q = 0; q < R; q++) acc[q] = fmaf(L.a[r][j], rp[j * R + q], acc[q]);
+        }
+        if (L.step[r] >= 0)
+#pragma unroll
+            for (int q = 0; q < R; q++) xs[L.step[r] * R + q] = acc[q];
+    }
+    __syncwarp();
 }
 
 template <int N, int R>
@@ -420,7 +408,7 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
             }
         }
         __syncwarp();
-        const bool ok = reglu_factor<N, R>(L, s.rowbuf, s.piv, s.rcp, lane);
+        const bool ok = reg_invert<N, R>(L, s.rowbuf, lane);
         bool accepted = false;
         double est_final = 0.0;
         int nres = 0;
@@ -433,7 +421,7 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
                 nres++;
                 constexpr int JB = residual_blocks(N);
                 constexpr int JL = (N + JB - 1) / JB;
-                float *rbuf = xs;  // N x R floats, free until the next back substitution
+                float *rbuf = xs;  // N x R floats, free until the next solve
 #pragma unroll 1
                 for (int pass = 0; pass < (N * JB + 31) / 32; pass++) {
                     const int pr = pass * 32 + lane;
@@ -476,8 +464,7 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
             const float tolf = (float)P.tol;
             float dprev = 0.0f;
             for (int step = 0;; step++) {
-                reglu_forward<N, R>(L, rhs, s.piv, lane);
-                reglu_back<N, R>(L, rhs, s.piv, s.rcp, xs, lane);
+                reg_apply_inverse<N, R>(L, rhs, s.rowbuf, xs, lane);
                 float dmaxf = 0.0f, xmaxf = 0.0f;
                 for (int t = lane; t < N * R; t += 32) {
                     const float d = xs[t];

@@ -14,10 +14,13 @@
 //   * interior stencils only.  Stencils with a boundary point (Hermite rows) and the rare
 //     stencil whose refinement fails go to a list that the general refined kernel
 //     (FP32 factor, FP64 refinement, FP64 fallback) finishes in a second launch.
-// Together: 16 resident warps per SM.  The elimination, the substitutions and the
-// acceptance rule are those of the register kernel (pivot choice by magnitude, ties to
-// the lower row); multipliers of an extra row reach the lanes that need them by shuffle
-// within the row's group of four lanes.
+// Together: 16 resident warps per SM.  The FP32 factorisation is a Gauss-Jordan inversion
+// (pivot choice by magnitude, ties to the lower row, as the register kernel's LU; the rows
+// not yet used as pivots evolve exactly as in the LU), run as one rolled loop over the steps
+// with each row a shifting register window, so the code stays small and every solve of the
+// refinement is one product with the inverse instead of two serial substitutions.
+// Multipliers of an extra row reach the lanes that need them by shuffle within the row's
+// group of four lanes.  The acceptance rule is the register kernel's.
 #pragma once
 #include "stencil_refined_reg.cuh"
 
@@ -38,6 +41,7 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
     constexpr int NX = LU::NX, PW = LU::PW;
     static_assert(NX >= 1 && NX <= 8, "split layout: 33..40 rows");
     static_assert(PW % 2 == 0, "pieces are published as float2");
+    static_assert(N == 4 * PW, "the inversion shifts whole rows of four pieces");
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const SplitSmem s = carve_split(smem + wib * warp_bytes, N, P.k);
@@ -103,115 +107,121 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
         }
         __syncwarp();
 
-        // ---- FP32 LU with partial pivoting, rows in place
+        // ---- FP32 Gauss-Jordan inversion with partial pivoting, rows in place.  Every row is a
+        // window of N registers: before step c it holds columns c..N-1 of the row, then the
+        // row's entries of the c inverse columns formed so far.  Step c eliminates column c
+        // (window position 0) from every row but the pivot row, shifts each window left by one
+        // and appends the row's entry of the new inverse column: minus the multiplier, or 1 in
+        // the pivot row, which is left unscaled (a row may carry any scale factor through the
+        // later steps; the pivot row's row of the inverse is multiplied by its reciprocal
+        // pivot at the end).  Every step runs the same code, so the loop stays rolled and the
+        // solves become products with the inverse: no serial substitution chains.
         bool ok = true;
-        static_for<0, N, 1>([&](auto cI) {
-            constexpr int c = decltype(cI)::value;
-            constexpr int qc = c / PW, tc = c % PW;
+        float rsc = 1.0f, xsc = 1.0f;  // reciprocal pivots of this lane's main and extra rows
+#pragma unroll 1
+        for (int c = 0; c < N; c++) {
             // pivot-row buffers alternate by step: the publish of step c + 1 cannot overwrite
             // the row that step c is still reading, so one warp barrier per step suffices
-            float *const rowbuf = s.rowbuf + (c & 1) * 4 * ((N + 3) / 4);
-            const unsigned km = L.mstep == N + 1
-                                    ? (__float_as_uint(fabsf(L.a[c])) & ~63u) | (unsigned)(63 - lane) : 0u;
-            const unsigned kx = (L.xstep == N + 1 && q == qc)
-                                    ? (__float_as_uint(fabsf(L.b[tc])) & ~63u) | (unsigned)(63 - gx) : 0u;
+            float *const rowbuf = s.rowbuf + (c & 1) * 4 * PW;
+            const unsigned km = L.mstep == N + 1 ? (__float_as_uint(fabsf(L.a[0])) & ~63u) | (unsigned)(63 - lane) : 0u;
+            const unsigned kx =
+                (L.xstep == N + 1 && q == 0) ? (__float_as_uint(fabsf(L.b[0])) & ~63u) | (unsigned)(63 - gx) : 0u;
             const unsigned key = __reduce_max_sync(0xffffffffu, max(km, kx));
             const int brow = 63 - (int)(key & 63u);
-            if (brow < 32) {  // the same in every lane
-                if (lane == brow) {
-                    L.mstep = c;
+            const bool pm = brow == lane;           // this lane's main row is the pivot row
+            const bool px = xvalid && brow == gx;  // this lane's extra row is the pivot row
+            if (pm) {
 #pragma unroll
-                    for (int q4 = c / 4; q4 < (N + 3) / 4; q4++) {
-                        float4 v;
-                        v.x = L.a[4 * q4 + 0 < N ? 4 * q4 + 0 : 0];
-                        v.y = 4 * q4 + 1 < N ? L.a[4 * q4 + 1 < N ? 4 * q4 + 1 : 0] : 0.0f;
-                        v.z = 4 * q4 + 2 < N ? L.a[4 * q4 + 2 < N ? 4 * q4 + 2 : 0] : 0.0f;
-                        v.w = 4 * q4 + 3 < N ? L.a[4 * q4 + 3 < N ? 4 * q4 + 3 : 0] : 0.0f;
-                        reinterpret_cast<float4 *>(rowbuf)[q4] = v;
-                    }
-                }
-            } else if (gx == brow && xvalid) {  // the four lanes of the pivot's group
-                L.xstep = c;
+                for (int q4 = 0; q4 < N / 4; q4++)
+                    reinterpret_cast<float4 *>(rowbuf)[q4] =
+                        make_float4(L.a[4 * q4], L.a[4 * q4 + 1], L.a[4 * q4 + 2], L.a[4 * q4 + 3]);
+            } else if (px) {
 #pragma unroll
                 for (int t = 0; t < PW; t += 2)
-                    reinterpret_cast<float2 *>(rowbuf)[(q * PW + t) >> 1] =
-                        make_float2(L.b[t], t + 1 < PW ? L.b[t + 1 < PW ? t + 1 : 0] : 0.0f);
+                    reinterpret_cast<float2 *>(rowbuf)[(q * PW + t) >> 1] = make_float2(L.b[t], L.b[t + 1]);
             }
             __syncwarp();
-            const float pvt = rowbuf[c];
-            // approximate reciprocal (the FP32 factor only preconditions the refinement); a
+            const float pvt = rowbuf[0];
+            // approximate reciprocal (the FP32 inverse only preconditions the refinement); a
             // zero, subnormal or non-finite pivot fails the factorisation
             float inv;
             asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(pvt));
             ok &= (pvt != 0.0f) && isfinite(pvt) && isfinite(inv);
-            if (lane == 0) {
-                s.piv[c] = brow;
-                s.rcp[c] = inv;
+            if (pm) {
+                L.mstep = c;
+                rsc = inv;
             }
-            // main rows: multiplier into column c, update of columns c+1..N-1 (rows already
-            // used as pivots get a zero multiplier)
+            if (px) {
+                L.xstep = c;
+                xsc = inv;
+            }
+            // main row: window position j - 1 <- j minus the multiplier times the pivot row
             {
-                const bool act = L.mstep == N + 1;
-                const float l = act ? L.a[c] * inv : 0.0f;
-                L.a[c] = act ? l : L.a[c];
+                const float m = pm ? 0.0f : L.a[0] * inv;
 #pragma unroll
-                for (int q4 = (c + 1) / 4; q4 < (N + 3) / 4; q4++) {
+                for (int q4 = 0; q4 < N / 4; q4++) {
                     const float4 v = reinterpret_cast<const float4 *>(rowbuf)[q4];
                     const float vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
                     for (int t = 0; t < 4; t++) {
-                        const int cc = 4 * q4 + t;
-                        if (cc > c && cc < N) L.a[cc < N ? cc : 0] = fmaf(-l, vv[t], L.a[cc < N ? cc : 0]);
+                        const int j = 4 * q4 + t;
+                        if (j >= 1) L.a[j >= 1 ? j - 1 : 0] = fmaf(-m, vv[t], L.a[j]);
                     }
                 }
+                L.a[N - 1] = pm ? 1.0f : -m;
             }
-            // extra rows: the lane holding column c computes the multiplier, its group gets
-            // it by shuffle; columns of the piece right of c are updated
+            // extra row: the multiplier comes from the piece holding window position 0, the
+            // entry shifted into a piece's last slot from the next piece of the same row
             {
-                const bool xact = L.xstep == N + 1;
-                float lx = __shfl_sync(0xffffffffu, L.b[tc] * inv, (lane & ~3) | qc);
-                lx = xact ? lx : 0.0f;
-                const bool right_hi = q >= qc, right_lo = q > qc;  // column q*PW+t > c
+                // every lane takes part in the shuffle (the pivot row's lanes then drop it)
+                const float mxs = __shfl_sync(0xffffffffu, L.b[0] * inv, lane & ~3);
+                const float mx = px ? 0.0f : mxs;
+                const float nxt = __shfl_down_sync(0xffffffffu, L.b[0], 1);
+                const float vn = rowbuf[q < 3 ? (q + 1) * PW : 0];
 #pragma unroll
-                for (int t = 0; t < PW; t += 2) {
-                    const float2 v = reinterpret_cast<const float2 *>(rowbuf)[(q * PW + t) >> 1];
-                    if (t > tc ? right_hi : right_lo) L.b[t] = fmaf(-lx, v.x, L.b[t]);
-                    if (t + 1 < PW && (t + 1 > tc ? right_hi : right_lo))
-                        L.b[t + 1 < PW ? t + 1 : 0] = fmaf(-lx, v.y, L.b[t + 1 < PW ? t + 1 : 0]);
-                }
-                if (q == qc && xact) L.b[tc] = lx;
+                for (int t = 0; t + 1 < PW; t++) L.b[t] = fmaf(-mx, rowbuf[q * PW + t + 1], L.b[t + 1]);
+                L.b[PW - 1] = q < 3 ? fmaf(-mx, vn, nxt) : (px ? 1.0f : -mx);
             }
-        });
-        __syncwarp();  // pivots and reciprocal pivots (lane 0) before the solves
+        }
+        // rows of the inverse: the unscaled pivot rows times their reciprocal pivots
+#pragma unroll
+        for (int j = 0; j < N; j++) L.a[j] *= rsc;
+#pragma unroll
+        for (int t = 0; t < PW; t++) L.b[t] *= xsc;
+        __syncwarp();
 
-        // ---- refinement: solves with the register factors, FP64 residuals
+        // ---- refinement: products with the FP32 inverse, FP64 residuals
         bool accepted = false;
         double est_final = 0.0;
         int nres = 0;
         if (ok) {
-            auto forward = [&]() {
-                static_for<0, N, 1>([&](auto cI) {
-                    constexpr int c = decltype(cI)::value;
-                    constexpr int qc = c / PW, tc = c % PW;
-                    const int p = s.piv[c];
-                    const float y = __shfl_sync(0xffffffffu, p < 32 ? rm : rx, p < 32 ? p : 4 * (p - 32));
-                    const float mx = __shfl_sync(0xffffffffu, L.b[tc], (lane & ~3) | qc);
-                    if (L.mstep > c) rm = fmaf(-L.a[c], y, rm);
-                    if (L.xstep > c) rx = fmaf(-mx, y, rx);
-                });
-            };
-            auto back = [&]() {
-                static_for<N - 1, -1, -1>([&](auto cI) {
-                    constexpr int c = decltype(cI)::value;
-                    constexpr int qc = c / PW, tc = c % PW;
-                    const int p = s.piv[c];
-                    const float xq =
-                        __shfl_sync(0xffffffffu, p < 32 ? rm : rx, p < 32 ? p : 4 * (p - 32)) * s.rcp[c];
-                    const float ux = __shfl_sync(0xffffffffu, L.b[tc], (lane & ~3) | qc);
-                    if (lane == 0) s.xs[c] = xq;
-                    if (L.mstep >= 0 && L.mstep < c) rm = fmaf(-L.a[c], xq, rm);
-                    if (L.xstep >= 0 && L.xstep < c) rx = fmaf(-ux, xq, rx);
-                });
+            // x = A32^{-1} r.  The row pivoted at step c holds row c of the inverse, its window
+            // position s the column of the row pivoted at step s: every row puts its right-hand
+            // side at its own pivot step, and each row's dot product is unknown c.
+            float *const rp = s.rowbuf;  // free once the inversion is done (16-byte aligned)
+            auto solve = [&]() {
+                rp[L.mstep] = rm;
+                if (xvalid && q == 0) rp[L.xstep] = rx;
+                __syncwarp();
+                float dm = 0.0f, dx = 0.0f;
+#pragma unroll
+                for (int q4 = 0; q4 < N / 4; q4++) {
+                    const float4 v = reinterpret_cast<const float4 *>(rp)[q4];
+                    dm = fmaf(L.a[4 * q4], v.x, dm);
+                    dm = fmaf(L.a[4 * q4 + 1], v.y, dm);
+                    dm = fmaf(L.a[4 * q4 + 2], v.z, dm);
+                    dm = fmaf(L.a[4 * q4 + 3], v.w, dm);
+                }
+#pragma unroll
+                for (int t = 0; t < PW; t += 2) {
+                    const float2 v = reinterpret_cast<const float2 *>(rp)[(q * PW + t) >> 1];
+                    dx = fmaf(L.b[t], v.x, dx);
+                    dx = fmaf(L.b[t + 1], v.y, dx);
+                }
+                dx += __shfl_xor_sync(0xffffffffu, dx, 1);
+                dx += __shfl_xor_sync(0xffffffffu, dx, 2);
+                s.xs[L.mstep] = dm;
+                if (xvalid && q == 0) s.xs[L.xstep] = dx;
                 __syncwarp();
             };
             // FP64 residual r = b - A x: rows 0..31 one per lane, rows 32..N-1 as (row, quarter
@@ -243,8 +253,7 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
             const float tolf = (float)P.tol;
             float dprev = 0.0f;
             for (int step = 0;; step++) {
-                forward();
-                back();
+                solve();
                 float dmaxf = 0.0f, xmaxf = 0.0f;
                 for (int t = lane; t < N; t += 32) {
                     const float d = s.xs[t];
