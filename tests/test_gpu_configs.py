@@ -80,7 +80,19 @@ def test_unit_disk_hermite_batched(pkg, orc, precision):
         if alpha[b] == 0.0:
             u[i] = 2 * X[i] @ normals[b]
     r = W.apply(u)
-    assert np.abs(r[~isb] - 4.0).max() < 1e-8
+    if precision == "fp64":
+        assert np.abs(r[~isb] - 4.0).max() < 1e-8
+    else:
+        # refined weights carry the error the refinement accepts: at most the contraction bound
+        # it enforces (1e-3) times its tolerance (1e-9), relative, so the bar grows with
+        # sum |w_j u_j|; asked for 1e-11 the same kernels meet the FP64 bar
+        rows = np.repeat(np.arange(len(X)), np.diff(ref.row_ptr))
+        wu = np.zeros(len(X))
+        np.add.at(wu, rows, np.abs(W.val.cpu().numpy() * u[ref.col]))
+        assert (np.abs(r - 4.0) <= 1e-8 + 1e-12 * wu)[~isb].all()
+        Wt = pkg.build_weights_batched([(3, 0)], Xd, None, ap, ai, pkg.PHS(3, poly_deg=3), hermite=herm,
+                                       precision=precision, tune=1, tol=1e-11)[0]
+        assert np.abs(Wt.apply(u)[~isb] - 4.0).max() < 1e-8
     # the apply bar is on the product itself: the oracle's SpMV over the same weights
     mine = orc.CSR(W.row_ptr.cpu().numpy(), W.col.cpu().numpy(), W.val.cpu().numpy()[None], None, W.shape)
     r_ref = orc.spmm(mine, u)

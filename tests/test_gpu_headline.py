@@ -124,12 +124,21 @@ def bcloud(pkg, orc):
     return X, torch.from_numpy(X).cuda(), torch.from_numpy(adjl).cuda(), ref, herm, hi, isb
 
 
-def check_quadratic(W, X, isb, lo):
-    """Laplacian of u = |x|^2 + 1 (du/dn = 0 on x = 0) is 6 at every interior eval point."""
+def check_quadratic(W, X, isb, lo, refined=False):
+    """Laplacian of u = |x|^2 + 1 (du/dn = 0 on x = 0) is 6 at every interior eval point.  FP64
+    weights meet it to 1e-8; refined weights carry the error the refinement accepts, at most its
+    enforced contraction (1e-3) times its tolerance (1e-9) relative, so their bar adds
+    1e-12 sum |w_j u_j| per row."""
     u = (X ** 2).sum(1) + 1.0
     u[lo] = 0.0  # Neumann data at the x = 0 points
     y = W.apply(torch.from_numpy(u).cuda()).cpu().numpy()
-    assert np.abs(y[~isb] - 6.0).max() < 1e-8
+    bar = np.full(len(X), 1e-8)
+    if refined:
+        rp, col, val = W.row_ptr.cpu().numpy(), W.col.cpu().numpy(), W.val.cpu().numpy()
+        wu = np.zeros(len(X))
+        np.add.at(wu, np.repeat(np.arange(len(X)), np.diff(rp)), np.abs(val * u[col]))
+        bar += 1e-12 * wu
+    assert (np.abs(y - 6.0) <= bar)[~isb].all()
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32_refined"])
@@ -142,7 +151,7 @@ def test_boundary_stencils(pkg, bcloud, precision):
     check(W[0], ref, X)
     s = status.cpu().numpy()
     assert (s == 2).sum() == int(hi.sum())  # Dirichlet eval rows: identity
-    check_quadratic(W[0], X, isb, isb & ~hi)
+    check_quadratic(W[0], X, isb, isb & ~hi, refined=precision != "fp64")
 
 
 @pytest.fixture(scope="module")
@@ -170,7 +179,7 @@ def test_learned_build_boundary(pkg, bcloud, trained):
     Wb = pkg.build_weights([(3, 0)], Xd, None, a, pkg.PHS(3, poly_deg=2), hermite=herm, precision="learned",
                            seed=seed)[0]
     check(Wb, ref, X)
-    check_quadratic(Wb, X, isb, isb & ~hi)
+    check_quadratic(Wb, X, isb, isb & ~hi, refined=True)
 
 
 def test_what_the_trained_surrogate_gains(pkg, cloud, trained):
