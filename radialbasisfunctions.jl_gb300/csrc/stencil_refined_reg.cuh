@@ -459,6 +459,57 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
                 }
                 __syncwarp();
             };
+            // After acceptance: the polynomial-reproduction rows (k..N-1) once more in FP64 and
+            // one correction through the inverse.  A product with a Gauss-Jordan inverse is not
+            // backward stable: it leaves a residual of about cond * 2^-24 of the last step, and in
+            // these rows that residual breaks the exact reproduction of polynomials, which the
+            // apply of a smooth field amplifies by sum |w|.  Only the k columns of P enter (the
+            // rows' other block is zero); the rows share the warp's lanes in one pass.
+            auto polish = [&]() {
+                // lane (t, h): row k + t, column block h of c3 blocks (c3 lanes per row)
+                const int k = P.k, nm = N - k;
+                const int c3 = nm >= 32 ? 1 : 32 / nm, cw = (k + c3 - 1) / c3;
+                const int t0 = lane / c3, h = lane - t0 * c3;
+                float *rbuf = xs;
+                for (int tb = 0; tb < nm; tb += 32 / c3) {
+                    const int t = tb + t0;
+                    double acc[R];
+#pragma unroll
+                    for (int q = 0; q < R; q++) acc[q] = 0.0;
+                    if (t < nm && t0 < 32 / c3) {
+                        const int ti2 = tri(k + t);
+                        for (int jj = 0; jj < cw; jj++) {
+                            const int j = h * cw + jj;
+                            if (j < k) {
+                                const double a = s.Mp[ti2 + j];
+#pragma unroll
+                                for (int q = 0; q < R; q++) acc[q] = fma(-a, s.x[j * R + q], acc[q]);
+                            }
+                        }
+                    }
+                    for (int o = 1; o < c3; o++) {
+#pragma unroll
+                        for (int q = 0; q < R; q++) {
+                            const double v = __shfl_down_sync(0xffffffffu, acc[q], o);
+                            if (h == 0) acc[q] += v;
+                        }
+                    }
+                    if (t < nm && t0 < 32 / c3 && h == 0)
+#pragma unroll
+                        for (int q = 0; q < R; q++) rbuf[(k + t) * R + q] = __double2float_rn(s.bv[(k + t) * R + q] + acc[q]);
+                }
+                __syncwarp();
+#pragma unroll
+                for (int r = 0; r < ROWS; r++) {
+                    const int i = lane + 32 * r;
+#pragma unroll
+                    for (int q = 0; q < R; q++) rhs[r][q] = (i >= k && i < N) ? rbuf[(i < N ? i : 0) * R + q] : 0.0f;
+                }
+                __syncwarp();
+                reg_apply_inverse<N, R>(L, rhs, s.rowbuf, xs, lane);
+                for (int t = lane; t < k * R; t += 32) s.x[t] += widen(xs[t]);  // the weights
+                __syncwarp();
+            };
             // the first solve leaves an error at the FP32 floor (about cond(A) * 2^-24
             // relative) from any start: a seed cannot beat it, so it costs no FP64 residual
             const float tolf = (float)P.tol;
@@ -500,6 +551,7 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
                     if (dmaxf <= tolf * xmaxf && dmaxf <= 0.5f * dprev) {
                         accepted = true;
                         est_final = xmaxf > 0.0f ? (double)(dmaxf / xmaxf) : 0.0;
+                        polish();
                         break;
                     }
                     dprev = dmaxf;

@@ -250,6 +250,43 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
                 rm = narrow(s.bv[lane] + ((c0 + c1) + (c2 + c3)));
                 rx = xvalid ? narrow(s.bv[gx] + ex) : 0.0f;
             };
+            // After acceptance: the polynomial-reproduction rows (k..N-1) once more in FP64 and
+            // one correction through the inverse.  A product with a Gauss-Jordan inverse is not
+            // backward stable (unlike the LU substitutions): it leaves a residual of about
+            // cond * 2^-24 of the last step, and in these rows that residual is a violation of
+            // the exact reproduction of polynomials, which the apply of a smooth field
+            // amplifies by sum |w| (~1/h^2).  The correction shrinks it by the same factor.  The
+            // rows' zero block leaves k products per row; the rows share the warp's lanes in one
+            // pass.
+            auto polish = [&]() {
+                // lane (t, h): row k + t, column block h of c3 blocks (c3 lanes per row)
+                const int k = P.k, nm = N - k;
+                const int c3 = nm >= 32 ? 1 : 32 / nm, cw = (k + c3 - 1) / c3;
+                const int t0 = lane / c3, h = lane - t0 * c3;
+                for (int tb = 0; tb < nm; tb += 32 / c3) {
+                    const int t = tb + t0;
+                    double acc = 0.0;
+                    if (t < nm && t0 < 32 / c3) {
+                        const int ti2 = tri(k + t);
+                        for (int jj = 0; jj < cw; jj++) {
+                            const int j = h * cw + jj;
+                            if (j < k) acc = fma(-s.Mp[ti2 + j], s.x[j], acc);
+                        }
+                    }
+                    for (int o = 1; o < c3; o++) {
+                        const double v = __shfl_down_sync(0xffffffffu, acc, o);
+                        if (h == 0) acc += v;
+                    }
+                    if (t < nm && t0 < 32 / c3 && h == 0) s.xs[k + t] = narrow(s.bv[k + t] + acc);
+                }
+                __syncwarp();
+                rm = lane >= k ? s.xs[lane] : 0.0f;
+                rx = (xvalid && gx >= k) ? s.xs[gx] : 0.0f;
+                __syncwarp();
+                solve();
+                for (int t = lane; t < k; t += 32) s.x[t] += widen(s.xs[t]);  // the weights
+                __syncwarp();
+            };
             const float tolf = (float)P.tol;
             float dprev = 0.0f;
             for (int step = 0;; step++) {
@@ -284,6 +321,7 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
                     if (dmaxf <= tolf * xmaxf && dmaxf <= 0.5f * dprev) {
                         accepted = true;
                         est_final = xmaxf > 0.0f ? (double)(dmaxf / xmaxf) : 0.0;
+                        polish();
                         break;
                     }
                     dprev = dmaxf;
