@@ -58,7 +58,7 @@ PEAKS = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.ex
 # case of this workload (`python bench.py --case build_refined --n 1000000` and `--case
 # build_learned` under ncu), scaled by the stencil count (the kernel's traffic grows in
 # proportion).  None: not captured.
-KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": 479.6, "learned": 610.3}
+KERNEL_TRAFFIC_PER_STENCIL = {"fp32_refined": 477.4, "learned": 610.3}
 
 
 def peaks_bf16():
