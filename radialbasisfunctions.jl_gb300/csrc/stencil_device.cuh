@@ -569,10 +569,9 @@ __device__ __forceinline__ double df_to_double(dfl a) { return widen(a.hi) + wid
 // Interior stencils: Phi and P in double-float.  M gets the FP64 system (hi + lo, for the
 // residual and the fallback), F the FP32 factor matrix (hi).  Right-hand sides in FP64.
 // Hermite stencils (a small minority) take the FP64 assembly and are rounded to F.
-// pairs (optional): the upper-triangle pairs (i <= j) in order, packed as i | j << 8.
 template <bool ND = false>
 __device__ void assemble_refined(const StencilParams &P, const WarpSmem &w, const Warp32 &u, int lane, int es,
-                                 int eval_local, const uint16_t *pairs = nullptr) {
+                                 int eval_local) {
     // u.F == nullptr: only the FP64 system is needed (the register kernels narrow it)
     const int k = P.k, n = P.n, nops = P.nops, ld = mat_ld(n, nops), fld = f32_ld(n), dim = P.dim, nmon = P.nmon;
     if (eval_local != -2) {  // Hermite stencil
@@ -599,17 +598,10 @@ __device__ void assemble_refined(const StencilParams &P, const WarpSmem &w, cons
     __syncwarp();
     const int npairs = k * (k + 1) / 2;
     for (int p = lane; p < npairs; p += 32) {
-        int i, j;
-        if (pairs) {
-            const unsigned pk = pairs[p];
-            i = (int)(pk & 0xffu);
-            j = (int)(pk >> 8);
-        } else {
-            j = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
-            while (j * (j + 1) / 2 > p) j--;
-            while ((j + 1) * (j + 2) / 2 <= p) j++;
-            i = p - j * (j + 1) / 2;
-        }
+        int j = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+        while (j * (j + 1) / 2 > p) j--;
+        while ((j + 1) * (j + 2) / 2 <= p) j++;
+        const int i = p - j * (j + 1) / 2;
         dfl r2 = {0.0f, 0.0f};
         for (int d = 0; d < dim; d++) {
             dfl dd = ts(u.XH[i * 3 + d], -u.XH[j * 3 + d]);

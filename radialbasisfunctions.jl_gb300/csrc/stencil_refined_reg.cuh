@@ -133,10 +133,12 @@ __device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int 
         }
     for (int t = lane; t < tri(n) - tri(k); t += 32) s.Mp[tri(k) + t] = 0.0;  // rows k..n-1; the
     __syncwarp();                                                           // P^T part is set below
-    const int npairs = k * (k + 1) / 2;
+    // phi(0) = 0 on the diagonal; the strict pairs i < j from the block's table
+    for (int i = lane; i < k; i += 32) s.Mp[tri(i) + i] = 0.0;
+    const int npairs = k * (k - 1) / 2;
     for (int p = lane; p < npairs; p += 32) {
         const unsigned pk = pairs[p];
-        const int i = (int)(pk & 0xffu), j = (int)(pk >> 8);  // i <= j
+        const int i = (int)(pk & 0xffu), j = (int)(pk >> 8);  // i < j
         dfl r2 = {0.0f, 0.0f};
         for (int d = 0; d < dim; d++) {
             dfl dd = ts(s.XH[i * 3 + d], -s.XH[j * 3 + d]);
@@ -328,12 +330,12 @@ __global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const SplitSmem s = carve_split(smem + wib * warp_bytes, N, P.k, R);
     float *xs = s.xs;  // N x R floats
-    // upper-triangle pair table of the RBF block, shared by the block's warps
+    // strict upper-triangle pair table of the RBF block (i < j), shared by the block's warps
     uint16_t *pairs = reinterpret_cast<uint16_t *>(smem + wpb * warp_bytes);
-    for (int p = threadIdx.x; p < P.k * (P.k + 1) / 2; p += blockDim.x) {
-        int j = 0;
-        while ((j + 1) * (j + 2) / 2 <= p) j++;
-        pairs[p] = (uint16_t)((p - j * (j + 1) / 2) | (j << 8));
+    for (int p = threadIdx.x; p < P.k * (P.k - 1) / 2; p += blockDim.x) {
+        int j = 1;
+        while ((j + 1) * j / 2 <= p) j++;
+        pairs[p] = (uint16_t)((p - j * (j - 1) / 2) | (j << 8));
     }
     __syncthreads();
     const int64_t nwarps = (int64_t)gridDim.x * wpb;

@@ -46,10 +46,10 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const SplitSmem s = carve_split(smem + wib * warp_bytes, N, P.k);
     uint16_t *pairs = reinterpret_cast<uint16_t *>(smem + wpb * warp_bytes);
-    for (int p = threadIdx.x; p < P.k * (P.k + 1) / 2; p += blockDim.x) {
-        int j = 0;
-        while ((j + 1) * (j + 2) / 2 <= p) j++;
-        pairs[p] = (uint16_t)((p - j * (j + 1) / 2) | (j << 8));
+    for (int p = threadIdx.x; p < P.k * (P.k - 1) / 2; p += blockDim.x) {
+        int j = 1;
+        while ((j + 1) * j / 2 <= p) j++;
+        pairs[p] = (uint16_t)((p - j * (j - 1) / 2) | (j << 8));
     }
     __syncthreads();
     const int g = lane >> 2, q = lane & 3;
@@ -238,12 +238,14 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
                 }
 #pragma unroll
                 for (int j = N & ~3; j < N; j++) c0 = fma(-s.Mp[j > lane ? tri(j) + lane : ti + j], s.x[j], c0);
+                // an extra row that is a polynomial-reproduction row (gx >= k) is zero past column
+                // k: its four pieces cover columns 0..k-1 only
                 double ex = 0.0;
                 const int tg = tri(gx);
-#pragma unroll
-                for (int t = 0; t < PW; t++) {
-                    const int j = q * PW + t;
-                    if (j < N) ex = fma(-s.Mp[j <= gx ? tg + j : tri(j) + gx], s.x[j], ex);
+                const int ncol = gx >= P.k ? P.k : N, pw = (ncol + 3) >> 2;
+                for (int t = 0; t < pw; t++) {
+                    const int j = q * pw + t;
+                    if (j < ncol) ex = fma(-s.Mp[j <= gx ? tg + j : tri(j) + gx], s.x[j], ex);
                 }
                 ex += __shfl_xor_sync(0xffffffffu, ex, 1);
                 ex += __shfl_xor_sync(0xffffffffu, ex, 2);
