@@ -10,6 +10,19 @@
 
 #include "rbffd.h"
 
+// Round-to-nearest-even double -> float on the integer pipe (on GB300 the conversion
+// instruction runs on the FP64 pipe); values outside the FP32 normal range take it anyway.
+__device__ __forceinline__ float d2f_rn_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+    if (e <= 0 || e >= 255) return (float)x;
+    const unsigned long long m = b & 0xfffffffffffffull;
+    const unsigned long long rem = m & 0x1fffffffull, half = 1ull << 28;
+    unsigned r = ((unsigned)e << 23) | (unsigned)(m >> 29);
+    if (rem > half || (rem == half && (r & 1u))) r += 1u;  // a carry into the exponent is the right result
+    return __uint_as_float(((unsigned)(b >> 32) & 0x80000000u) | r);
+}
+
 // Size-class keys of the batched build: (m * 65 + k) * 8 + (polynomial degree + 1), k <= 64
 // the stencil length, m <= 64 the normal-derivative unknowns (RBF_FLAG_NORMAL_DOF).
 constexpr int kRbfBatchKeys = 65 * 65 * 8;

@@ -92,6 +92,23 @@ __device__ __forceinline__ double scale2(double x, int e) {
     return ldexp(x, e);
 }
 
+// The exponent frexp gives for sqrt(x), x > 0, from x's bit pattern on the integer pipe:
+// x = m 2^E with m in [0.5, 1) puts sqrt(x) in [2^((E-1)/2), 2^(E/2)), so the exponent is
+// (E + 1) >> 1 (the correctly rounded root of the largest double below 2^E, E even, stays
+// below 2^(E/2): sqrt(1 - u) < 1 - u/2).  Zero, subnormal and non-finite x take the library
+// path.  (frexp(sqrt(x)) would cost an FP64 square root on GB300's FP64 pipe.)
+__device__ __forceinline__ int sqrt_frexp_exponent(double x) {
+    const long long b = __double_as_longlong(x);
+    const int bexp = (int)((b >> 52) & 0x7ff);
+    if (bexp == 0 || bexp == 0x7ff || b < 0) {
+        int e = 0;
+        if (x > 0.0) frexp(sqrt(x), &e);
+        return e;
+    }
+    const int E = bexp - 1022;
+    return (E + 1) >> 1;
+}
+
 template <class T> __device__ __forceinline__ T rbf_sqrt(T x);
 template <> __device__ __forceinline__ double rbf_sqrt<double>(double x) { return sqrt(x); }
 template <> __device__ __forceinline__ float rbf_sqrt<float>(float x) { return sqrtf(x); }

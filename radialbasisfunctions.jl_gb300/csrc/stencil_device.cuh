@@ -75,7 +75,7 @@ __device__ int load_stencil(const StencilParams &P, int64_t e, const WarpSmem &w
     }
     anyb = __any_sync(0xffffffffu, anyb);
     int es = 0;
-    if (r2max > 0.0) frexp(sqrt(r2max), &es);
+    if (r2max > 0.0) es = sqrt_frexp_exponent(r2max);
     *es_out = es;
     __syncwarp();
     for (int i = lane; i < k; i += 32)
@@ -588,9 +588,9 @@ __device__ void assemble_refined(const StencilParams &P, const WarpSmem &w, cons
     for (int i = lane; i < k; i += 32)
         for (int d = 0; d < 3; d++) {
             double xv = d < dim ? w.X[i * 3 + d] : 0.0;
-            float hi = __double2float_rn(xv);
+            float hi = d2f_rn_bits(xv);
             u.XH[i * 3 + d] = hi;
-            u.XL[i * 3 + d] = __double2float_rn(xv - widen(hi));
+            u.XL[i * 3 + d] = d2f_rn_bits(xv - widen(hi));
         }
     for (int t = lane; t < nmon * ld; t += 32) w.M[(k + t / ld) * ld + t % ld] = 0.0;  // zero block rows
     if (u.F)

@@ -111,7 +111,7 @@ __device__ int load_interior(const StencilParams &P, int64_t e, const SplitSmem 
         r2max = __longlong_as_double(m);
     }
     int es = 0;
-    if (r2max > 0.0) frexp(sqrt(r2max), &es);
+    if (r2max > 0.0) es = sqrt_frexp_exponent(r2max);
     *es_out = es;
     __syncwarp();
     for (int i = lane; i < k; i += 32)
@@ -127,9 +127,9 @@ __device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int 
     for (int i = lane; i < k; i += 32)
         for (int d = 0; d < 3; d++) {
             const double xv = d < dim ? s.X[i * 3 + d] : 0.0;
-            const float hi = __double2float_rn(xv);
+            const float hi = d2f_rn_bits(xv);
             s.XH[i * 3 + d] = hi;
-            s.XL[i * 3 + d] = __double2float_rn(xv - widen(hi));
+            s.XL[i * 3 + d] = d2f_rn_bits(xv - widen(hi));
         }
     for (int t = lane; t < tri(n) - tri(k); t += 32) s.Mp[tri(k) + t] = 0.0;  // rows k..n-1; the
     __syncwarp();                                                           // P^T part is set below
