@@ -392,7 +392,7 @@ __device__ __forceinline__ void warp_sort_keys(float (&key)[SLOTS], int32_t (&ki
 // Error bound of an FP32 distance (u = 2^-24, M the largest coordinate magnitude):
 // |d32 - d| <= 8u (M + d).
 template <int DIM, int SLOTS>
-__global__ void __launch_bounds__(KNN_WARPS * 32, 3)  // 24 warps/SM: the register budget
+__global__ void __launch_bounds__(KNN_WARPS * 32, 4)  // 32 warps/SM: 64 registers
 knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__restrict__ sidx,
                 const int32_t *__restrict__ cstart, const double *__restrict__ data, const double *__restrict__ q,
                 const int32_t *__restrict__ qorder, int64_t nq, int k, int kp, int R0, float mag, int64_t ns,
