@@ -323,8 +323,14 @@ __device__ void reg_apply_inverse(const RegLU<N, R> &L, const float (&rhs)[RegLU
     __syncwarp();
 }
 
+// resident blocks of four warps per SM the register kernels are compiled for: one row slot
+// (N <= 32) fits six blocks without spills (78 registers; n = 26 at 2M: 25.4 ms with three
+// blocks, 23.4 ms with six), two row slots need three
+__host__ __device__ constexpr int reg_kernel_blocks(int n) { return n <= 32 ? 6 : 3; }
+
 template <int N, int R>
-__global__ void __launch_bounds__(128, 3) build_refined_reg_kernel(StencilParams P, int wpb, size_t warp_bytes) {
+__global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_kernel(StencilParams P, int wpb,
+                                                                                        size_t warp_bytes) {
     constexpr int ROWS = RegLU<N, R>::ROWS;
     extern __shared__ __align__(16) char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
