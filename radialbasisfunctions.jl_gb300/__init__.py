@@ -1293,3 +1293,7 @@ def directional(data, v, basis=None, **kw):
 def regrid(data, eval_points, basis=None, **kw):
     """regrid(data, eval_points; basis, k, adjl) (regridding.jl:38-47)."""
     return RadialBasisOperator(Regrid(), data, eval_points=eval_points, basis=basis, **kw)
+
+
+# ------------------------------------------------------------------------------ checkpoint / resume
+from .checkpoint import load_operator, load_weights, save_operator, save_weights  # noqa: E402

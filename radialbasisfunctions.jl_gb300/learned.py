@@ -196,16 +196,81 @@ class StencilMLP:
 
     # ------------------------------------------------------------------ checkpoint
     def state_dict(self):
-        return {"dims": self.dims, "k": self.k, "dim": self.dim, "out_scale": self.out_scale, "t": self.t,
-                "W": [w.cpu() for w in self.W], "b": [b.cpu() for b in self.b]}
+        """Everything training resumes from: the FP32 master weights and biases, their bf16
+        copies, the Adam moments and step count (host tensors)."""
+        return {"dims": list(self.dims), "k": self.k, "dim": self.dim, "out_scale": self.out_scale, "t": self.t,
+                "W": [w.cpu() for w in self.W], "b": [b.cpu() for b in self.b], "Wb": [w.cpu() for w in self.Wb],
+                "m": [t.cpu() for t in self.m], "v": [t.cpu() for t in self.v]}
 
     def load_state_dict(self, sd):
         torch = _torch()
+        if list(sd["dims"]) != list(self.dims) or sd["k"] != self.k or sd["dim"] != self.dim:
+            raise ValueError(f"state of a network with layers {sd['dims']} (k = {sd['k']}, dim = {sd['dim']}) "
+                             f"does not fit this one ({self.dims}, k = {self.k}, dim = {self.dim})")
         self.out_scale = sd["out_scale"]
         self.t = sd["t"]
         self.W = [w.to(self.dev).contiguous() for w in sd["W"]]
         self.b = [b.to(self.dev).contiguous() for b in sd["b"]]
-        self.Wb = [w.to(torch.bfloat16).contiguous() for w in self.W]
+        self.Wb = ([w.to(self.dev).contiguous() for w in sd["Wb"]] if "Wb" in sd else
+                   [w.to(torch.bfloat16).contiguous() for w in self.W])
+        if "m" in sd:
+            self.m = [t.to(self.dev).contiguous() for t in sd["m"]]
+            self.v = [t.to(self.dev).contiguous() for t in sd["v"]]
+
+
+SURROGATE_FORMAT = "rbffd-gb300-surrogate-1"
+
+
+def save_surrogate(path, model, progress=None):
+    """A StencilMLP (weights, Adam state) and optionally the training progress to one .npz:
+    progress = {"epoch": epochs done, "hist": losses, "rng": generator state (uint8 tensor)}."""
+    import json
+
+    import numpy as np
+    sd = model.state_dict()
+    arrays = {"format": SURROGATE_FORMAT}
+    nl = len(sd["W"])
+    for name in ("W", "b", "m", "v"):
+        for i, t in enumerate(sd[name]):
+            arrays[f"{name}{i}"] = t.numpy()
+    for i, t in enumerate(sd["Wb"]):  # bf16 bits
+        arrays[f"Wb{i}"] = t.view(_torch().int16).numpy()
+    meta = {"dims": sd["dims"], "k": sd["k"], "dim": sd["dim"], "out_scale": sd["out_scale"], "t": sd["t"],
+            "layers": nl, "nmoments": len(sd["m"])}
+    if progress is not None:
+        meta["epoch"] = int(progress["epoch"])
+        meta["hist"] = [float(h) for h in progress.get("hist", [])]
+        if progress.get("rng") is not None:
+            arrays["rng"] = progress["rng"].cpu().numpy()
+    arrays["meta"] = json.dumps(meta)
+    np.savez(path, **arrays)
+
+
+def load_surrogate(path, ctx=None, return_progress=False):
+    """The StencilMLP of save_surrogate (and, with return_progress, its training progress)."""
+    import json
+
+    import numpy as np
+    torch = _torch()
+    z = np.load(path, allow_pickle=False)
+    if "format" not in z.files or str(z["format"]) != SURROGATE_FORMAT:
+        raise ValueError(f"{path}: not a surrogate checkpoint of this library")
+    meta = json.loads(str(z["meta"]))
+    dims = meta["dims"]
+    model = StencilMLP(meta["k"], meta["dim"], hidden=tuple(dims[1:-1]), ctx=ctx, out_scale=meta["out_scale"])
+    nl, nm = meta["layers"], meta["nmoments"]
+    sd = {"dims": dims, "k": meta["k"], "dim": meta["dim"], "out_scale": meta["out_scale"], "t": meta["t"],
+          "W": [torch.from_numpy(z[f"W{i}"]) for i in range(nl)], "b": [torch.from_numpy(z[f"b{i}"]) for i in range(nl)],
+          "Wb": [torch.from_numpy(z[f"Wb{i}"]).view(torch.bfloat16) for i in range(nl)],
+          "m": [torch.from_numpy(z[f"m{i}"]) for i in range(nm)], "v": [torch.from_numpy(z[f"v{i}"]) for i in range(nm)]}
+    model.load_state_dict(sd)
+    if not return_progress:
+        return model
+    prog = None
+    if "epoch" in meta:
+        prog = {"epoch": meta["epoch"], "hist": meta["hist"],
+                "rng": torch.from_numpy(z["rng"]) if "rng" in z.files else None}
+    return model, prog
 
 
 # ---------------------------------------------------------------------------- data
@@ -253,20 +318,35 @@ def training_set(n_uniform, n_gradient, k, dim, basis, ops, seed=0, ctx=None, gr
 
 
 def train_surrogate(Xb, T, k, dim, hidden=(256, 256, 256), epochs=20, batch=4096, lr=2e-3, ctx=None, seed=0,
-                    log=None):
-    """Train a StencilMLP on bf16 features Xb and local-unit weights T (Adam, cosine decay)."""
+                    log=None, checkpoint=None, resume=None):
+    """Train a StencilMLP on bf16 features Xb and local-unit weights T (Adam, cosine decay).
+
+    checkpoint: a path written at the end of every epoch (network, Adam state, epochs done,
+    the shuffling generator's state); resume: such a path, from which training continues at the
+    next epoch on the same Xb, T and arguments, reaching the weights an uninterrupted run gives."""
     torch = _torch()
     n = Xb.shape[0]
-    scale = float(T.std())
-    model = StencilMLP(k, dim, hidden=hidden, ctx=ctx, seed=seed, out_scale=scale)
+    g = None
+    hist = []
+    start = 0
+    if resume is not None:
+        model, prog = load_surrogate(resume, ctx=ctx, return_progress=True)
+        if prog is None or list(model.dims[1:-1]) != list(hidden) or model.k != k or model.dim != dim:
+            raise ValueError(f"{resume}: not a training checkpoint of this network")
+        start, hist = prog["epoch"], list(prog["hist"])
+        g = torch.Generator(device=model.dev)
+        g.set_state(prog["rng"])
+        scale = model.out_scale
+    else:
+        scale = float(T.std())
+        model = StencilMLP(k, dim, hidden=hidden, ctx=ctx, seed=seed, out_scale=scale)
+        g = torch.Generator(device=model.dev).manual_seed(seed)
     Tn = torch.zeros((n, model.dims[-1]), dtype=torch.float32, device=model.dev)
     Tn[:, :k] = T / scale
-    g = torch.Generator(device=model.dev).manual_seed(seed)
     steps = max(1, n // batch)
     total = epochs * steps
-    hist = []
-    it = 0
-    for ep in range(epochs):
+    it = start * steps
+    for ep in range(start, epochs):
         perm = torch.randperm(n, device=model.dev, generator=g)
         acc = 0.0
         for s in range(steps):
@@ -277,6 +357,8 @@ def train_surrogate(Xb, T, k, dim, hidden=(256, 256, 256), epochs=20, batch=4096
             if s % 50 == 0:
                 acc = float(loss)
         hist.append(acc)
+        if checkpoint is not None:
+            save_surrogate(checkpoint, model, {"epoch": ep + 1, "hist": hist, "rng": g.get_state()})
         if log:
             log(f"epoch {ep}: loss {acc:.4e}")
     return model, hist
