@@ -7,12 +7,12 @@
 namespace {
 // ---------------------------------------------------------------------------------------
 // Register-resident FP32 factorisation for the system sizes of the standard workloads.
-// Lane l owns rows l and l+32 of the augmented matrix [A | b] (N rows, W = N + R columns,
-// fully in registers; N and R are template parameters so every column index is static).
-// LU with partial pivoting without moving rows: the pivot row of step c is published
-// through a shared buffer, every row not yet used as a pivot keeps its multiplier in
-// column c and is updated in columns c+1..W-1.  The factors stay in registers through all
-// refinement solves (forward substitution in pivot order, back substitution by columns).
+// Lane l owns rows l and l+32 of the system (N rows, fully in registers; N and the number R
+// of right-hand sides are template parameters so every column index is static).  The FP32
+// factorisation is a Gauss-Jordan inversion in place (reg_invert); the inverse stays in
+// registers through all refinement solves, each one product with it (reg_apply_inverse).
+// The residuals of the refinement are double-float dot products on the FP32 pipe, the final
+// pass over the polynomial-reproduction rows is FP64.
 // ---------------------------------------------------------------------------------------
 // Number of column blocks per row for the residual so that N*JB (row, block) pairs fill the
 // 32 lanes with the fewest FMA rounds.
@@ -42,11 +42,70 @@ __device__ __forceinline__ float narrow(double d) {
 // lower triangle by rows: A(i, j), j <= i, at tri(i) + j
 __host__ __device__ constexpr int tri(int i) { return (i * (i + 1)) >> 1; }
 
-// Shared memory of one warp of the register kernels: packed FP64 system (lower triangle by
-// rows) and its nops right-hand sides (n x nops), local coordinates and column indices, FP64
-// solution (n x nops), FP32 increments (n x nops), split coordinates, pivots, reciprocal
-// pivots and two pivot-row buffers (16-byte aligned, 4 * ceil(n/4) floats each), which the
-// solves reuse for the right-hand sides in pivot order.
+// ---- double-float storage and residual arithmetic of the register kernels (FP32 pipe) ----
+// The packed system, its right-hand sides and the refined solution are double-float values
+// hi + lo (about 48 significant bits, the accuracy the double-float assembly gives the
+// entries), each kept in one 64-bit shared-memory slot with hi in the low word.  On GB300 the
+// FP64 pipe retires two lanes per SM and clock against 128 for FP32, so the residuals of the
+// refinement run here in double-float arithmetic instead of FP64.
+__device__ __forceinline__ double df_pack(float hi, float lo) {
+    return __hiloint2double(__float_as_int(lo), __float_as_int(hi));
+}
+__device__ __forceinline__ float df_hi(double d) { return __int_as_float(__double2loint(d)); }
+__device__ __forceinline__ float df_lo(double d) { return __int_as_float(__double2hiint(d)); }
+// an FP64 value as the nearest float and the float nearest to the remainder
+__device__ __forceinline__ double df_pack_double(double v) {
+    const float h = d2f_rn_bits(v);
+    return df_pack(h, d2f_rn_bits(v - widen(h)));
+}
+__device__ __forceinline__ double df_unpack_double(double d) { return widen(df_hi(d)) + widen(df_lo(d)); }
+// x + d for a float d, renormalised
+__device__ __forceinline__ double df_add_f(double x, float d) {
+    const float xh = df_hi(x), xl = df_lo(x);
+    const float s = xh + d, z = s - xh;
+    const float q = ((xh - (s - z)) + (d - z)) + xl;
+    const float h = s + q;
+    return df_pack(h, q - (h - s));
+}
+
+// Dot-product accumulation after Sum2 of Ogita, Rump and Oishi ("Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26 (2005)): s is the running sum of the products' high
+// parts, each addition's rounding error is recovered exactly (Knuth's TwoSum) and added to
+// the compensation c, which also takes each product's rounding error (an FMA gives it
+// exactly) and the cross terms hi*lo; the lo*lo terms (~2^-48 relative) are dropped.  The
+// result is as accurate as if computed in about twice the working precision, whatever the
+// cancellation between the terms.
+struct DfSum {
+    float s, c;
+};
+__device__ __forceinline__ DfSum dfsum_of(double b) { return {df_hi(b), df_lo(b)}; }
+// acc -= a * x (a, x packed double-float)
+__device__ __forceinline__ void dfsum_sub(DfSum &acc, double a, double x) {
+    const float ah = df_hi(a), al = df_lo(a), xh = df_hi(x), xl = df_lo(x);
+    const float p = (-ah) * xh;
+    const float e = fmaf(-ah, xh, -p);  // -ah * xh = p + e exactly
+    const float s = acc.s + p, z = s - acc.s;
+    const float q = (acc.s - (s - z)) + (p - z);  // acc.s + p = s + q exactly
+    acc.s = s;
+    acc.c = fmaf(-al, xh, fmaf(-ah, xl, acc.c + (q + e)));
+}
+__device__ __forceinline__ DfSum dfsum_merge(DfSum a, DfSum b) {
+    const float s = a.s + b.s, z = s - a.s;
+    const float q = (a.s - (s - z)) + (b.s - z);
+    return {s, (a.c + b.c) + q};
+}
+// a merged with lane (lane ^ o)'s accumulator; every lane of the warp must execute it
+__device__ __forceinline__ DfSum dfsum_xor(DfSum a, int o) {
+    return dfsum_merge(a, {__shfl_xor_sync(0xffffffffu, a.s, o), __shfl_xor_sync(0xffffffffu, a.c, o)});
+}
+__device__ __forceinline__ float dfsum_value(DfSum a) { return a.s + a.c; }
+
+// Shared memory of one warp of the register kernels: packed system (lower triangle by rows)
+// and its nops right-hand sides (n x nops), both double-float (df_pack), FP64 local
+// coordinates and column indices, the double-float solution (n x nops; the weights are
+// unpacked to FP64 in place before the scatter), FP32 increments (n x nops), split
+// coordinates, pivots, reciprocal pivots and two pivot-row buffers (16-byte aligned,
+// 4 * ceil(n/4) floats each), which the solves reuse for the right-hand sides in pivot order.
 struct SplitSmem {
     double *Mp, *bv, *X, *x;
     int *cols, *piv;
@@ -121,7 +180,9 @@ __device__ int load_interior(const StencilParams &P, int64_t e, const SplitSmem 
 }
 
 // [Phi P; P^T 0] of an interior stencil in double-float (the arithmetic of
-// assemble_refined), stored as the packed lower triangle, and the right-hand sides.
+// assemble_refined), stored as the packed lower triangle, and the right-hand sides (evaluated
+// in FP64): packed double-float entries (DF, for double-float residuals) or FP64 ones.
+template <bool DF>
 __device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int lane, int es, const uint16_t *pairs) {
     const int k = P.k, n = P.n, dim = P.dim, nmon = P.nmon, nops = P.nops;
     for (int i = lane; i < k; i += 32)
@@ -153,7 +214,7 @@ __device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int 
         case 5: phi = df_mul(df_sqr(r2), r); break;
         default: phi = df_mul(df_mul(df_sqr(r2), r2), r); break;
         }
-        s.Mp[tri(j) + i] = df_to_double(phi);
+        s.Mp[tri(j) + i] = DF ? df_pack(phi.hi, phi.lo) : df_to_double(phi);
     }
     const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
     for (int i = lane; i < k; i += 32) {
@@ -163,20 +224,24 @@ __device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int 
             dfl v = {1.0f, 0.0f};
             for (int d = 0; d < dim; d++)
                 for (int t = 0; t < P.exps[m][d]; t++) v = df_mul(v, xd[d]);
-            s.Mp[tri(k + m) + i] = df_to_double(v);
+            s.Mp[tri(k + m) + i] = DF ? df_pack(v.hi, v.lo) : df_to_double(v);
         }
         double D[3];
         for (int d = 0; d < dim; d++) D[d] = -s.X[i * 3 + d];
-        for (int q = 0; q < nops; q++) s.bv[i * nops + q] = phs_op<double>(P.phs, P.op_code[q], P.op_dim[q], D, dim, AI);
+        for (int q = 0; q < nops; q++) {
+            const double b = phs_op<double>(P.phs, P.op_code[q], P.op_dim[q], D, dim, AI);
+            s.bv[i * nops + q] = DF ? df_pack_double(b) : b;
+        }
     }
     for (int t = lane; t < nmon * nops; t += 32) {
         const int m = t / nops, q = t - (t / nops) * nops;
-        s.bv[(k + m) * nops + q] = mono_op_at_origin(P, m, P.op_code[q], P.op_dim[q]);
+        const double b = mono_op_at_origin(P, m, P.op_code[q], P.op_dim[q]);
+        s.bv[(k + m) * nops + q] = DF ? df_pack_double(b) : b;
     }
     __syncwarp();
 }
 
-// A(i, j) of the packed symmetric system
+// A(i, j) of the packed symmetric system (packed double-float)
 __device__ __forceinline__ double pk_at(const double *Mp, int i, int j) {
     return Mp[i >= j ? tri(i) + j : tri(j) + i];
 }
@@ -361,7 +426,7 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
             __syncwarp();
             continue;
         }
-        assemble_packed(P, s, lane, es, pairs);
+        assemble_packed<true>(P, s, lane, es, pairs);
         RegLU<N, R> L;
 #pragma unroll
         for (int r = 0; r < ROWS; r++) {
@@ -369,7 +434,7 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
             const bool act = i < N;
             L.step[r] = act ? N + 1 : -1;
 #pragma unroll
-            for (int cc = 0; cc < N; cc++) L.a[r][cc] = act ? narrow(pk_at(s.Mp, act ? i : 0, cc)) : 0.0f;
+            for (int cc = 0; cc < N; cc++) L.a[r][cc] = act ? df_hi(pk_at(s.Mp, act ? i : 0, cc)) : 0.0f;
         }
         // start of the refinement: x0 = 0 and rhs = b, or with a learned seed x0 = [w_pred; 0]
         // and rhs = b - A32 x0, formed here from the FP32 rows while they are still unfactored
@@ -381,7 +446,7 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                     const int t = lane + 32 * r;
                     if (t < N) {
                         xs[t] = seed_reg[r];
-                        s.x[t] = widen(seed_reg[r]);
+                        s.x[t] = df_pack(seed_reg[r], 0.0f);
                     }
                 }
             } else {
@@ -389,7 +454,7 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                     const int i = t / R;
                     const float sv = i < P.k ? __ldg(&P.seed[e * P.k + i]) : 0.0f;
                     xs[t] = sv;
-                    s.x[t] = widen(sv);
+                    s.x[t] = df_pack(sv, 0.0f);
                 }
             }
             __syncwarp();
@@ -398,7 +463,7 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                 const int i = lane + 32 * r;
 #pragma unroll
                 for (int q = 0; q < R; q++) {
-                    float acc = i < N ? narrow(s.bv[(i < N ? i : 0) * R + q]) : 0.0f;
+                    float acc = i < N ? df_hi(s.bv[(i < N ? i : 0) * R + q]) : 0.0f;
                     static_for<0, N, 1>([&](auto jI) {
                         constexpr int j = decltype(jI)::value;
                         acc = fmaf(-L.a[r][j], xs[j * R + q], acc);
@@ -412,7 +477,7 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
             for (int r = 0; r < ROWS; r++) {
                 const int i = lane + 32 * r;
 #pragma unroll
-                for (int q = 0; q < R; q++) rhs[r][q] = i < N ? narrow(s.bv[(i < N ? i : 0) * R + q]) : 0.0f;
+                for (int q = 0; q < R; q++) rhs[r][q] = i < N ? df_hi(s.bv[(i < N ? i : 0) * R + q]) : 0.0f;
             }
         }
         __syncwarp();
@@ -421,10 +486,10 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
         double est_final = 0.0;
         int nres = 0;
         if (ok) {
-            // FP64 residual r = b - A x into rhs; rows k..N-1 are the polynomial reproduction
-            // constraints.  The N x N products are spread evenly over the warp as (row, block
-            // of JB columns) pairs; partial sums meet by shuffles and the row owner picks its
-            // entry up from shared memory.
+            // double-float residual r = b - A x into rhs; rows k..N-1 are the polynomial
+            // reproduction constraints.  The N x N products are spread evenly over the warp as
+            // (row, block of JB columns) pairs; partial sums meet by shuffles and the row owner
+            // picks its entry up from shared memory.
             auto residual = [&]() {
                 nres++;
                 constexpr int JB = residual_blocks(N);
@@ -434,9 +499,9 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                 for (int pass = 0; pass < (N * JB + 31) / 32; pass++) {
                     const int pr = pass * 32 + lane;
                     const int i = pr / JB, jb = pr % JB;
-                    double acc[R];
+                    DfSum acc[R];
 #pragma unroll
-                    for (int q = 0; q < R; q++) acc[q] = 0.0;
+                    for (int q = 0; q < R; q++) acc[q] = {0.0f, 0.0f};
                     if (i < N) {
                         const int j0 = jb * JL;
                         const int ti = tri(i);
@@ -446,17 +511,18 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                             if (j < N) {
                                 const double aij = s.Mp[j <= i ? ti + j : tri(j) + i];
 #pragma unroll
-                                for (int q = 0; q < R; q++) acc[q] = fma(-aij, s.x[j * R + q], acc[q]);
+                                for (int q = 0; q < R; q++) dfsum_sub(acc[q], aij, s.x[j * R + q]);
                             }
                         }
                     }
 #pragma unroll
                     for (int o = JB / 2; o > 0; o >>= 1)
 #pragma unroll
-                        for (int q = 0; q < R; q++) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+                        for (int q = 0; q < R; q++) acc[q] = dfsum_xor(acc[q], o);
                     if (i < N && jb == 0)
 #pragma unroll
-                        for (int q = 0; q < R; q++) rbuf[i * R + q] = __double2float_rn(s.bv[i * R + q] + acc[q]);
+                        for (int q = 0; q < R; q++)
+                            rbuf[i * R + q] = dfsum_value(dfsum_merge(dfsum_of(s.bv[i * R + q]), acc[q]));
                 }
                 __syncwarp();
 #pragma unroll
@@ -467,15 +533,20 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                 }
                 __syncwarp();
             };
-            // After acceptance: the polynomial-reproduction rows (k..N-1) once more in FP64 and
-            // one correction through the inverse.  A product with a Gauss-Jordan inverse is not
-            // backward stable: it leaves a residual of about cond * 2^-24 of the last step, and in
-            // these rows that residual breaks the exact reproduction of polynomials, which the
-            // apply of a smooth field amplifies by sum |w|.  Only the k columns of P enter (the
-            // rows' other block is zero); the rows share the warp's lanes in one pass.
+            // After acceptance: the polynomial-reproduction rows (k..N-1) once more, in FP64 on
+            // the weights unpacked to FP64, and one correction through the inverse.  A product
+            // with a Gauss-Jordan inverse is not backward stable: it leaves a residual of about
+            // cond * 2^-24 of the last step, and in these rows that residual breaks the exact
+            // reproduction of polynomials, which the apply of a smooth field amplifies by
+            // sum |w|.  The double-float residuals leave ~2^-45 sum |a x| in these rows, which
+            // the same amplification would make visible, so this pass is FP64 (ten rows of k
+            // products).  Only the k columns of P enter (the rows' other block is zero); the
+            // rows share the warp's lanes in one pass.
             auto polish = [&]() {
-                // lane (t, h): row k + t, column block h of c3 blocks (c3 lanes per row)
                 const int k = P.k, nm = N - k;
+                for (int t = lane; t < k * R; t += 32) s.x[t] = df_unpack_double(s.x[t]);  // the weights
+                __syncwarp();
+                // lane (t, h): row k + t, column block h of c3 blocks (c3 lanes per row)
                 const int c3 = nm >= 32 ? 1 : 32 / nm, cw = (k + c3 - 1) / c3;
                 const int t0 = lane / c3, h = lane - t0 * c3;
                 float *rbuf = xs;
@@ -489,7 +560,7 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                         for (int jj = 0; jj < cw; jj++) {
                             const int j = h * cw + jj;
                             if (j < k) {
-                                const double a = s.Mp[ti2 + j];
+                                const double a = df_unpack_double(s.Mp[ti2 + j]);
 #pragma unroll
                                 for (int q = 0; q < R; q++) acc[q] = fma(-a, s.x[j * R + q], acc[q]);
                             }
@@ -504,7 +575,8 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                     }
                     if (t < nm && t0 < 32 / c3 && h == 0)
 #pragma unroll
-                        for (int q = 0; q < R; q++) rbuf[(k + t) * R + q] = __double2float_rn(s.bv[(k + t) * R + q] + acc[q]);
+                        for (int q = 0; q < R; q++)
+                            rbuf[(k + t) * R + q] = __double2float_rn(df_unpack_double(s.bv[(k + t) * R + q]) + acc[q]);
                 }
                 __syncwarp();
 #pragma unroll
@@ -515,11 +587,11 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                 }
                 __syncwarp();
                 reg_apply_inverse<N, R>(L, rhs, s.rowbuf, xs, lane);
-                for (int t = lane; t < k * R; t += 32) s.x[t] += widen(xs[t]);  // the weights
+                for (int t = lane; t < k * R; t += 32) s.x[t] += widen(xs[t]);  // the weights, FP64
                 __syncwarp();
             };
             // the first solve leaves an error at the FP32 floor (about cond(A) * 2^-24
-            // relative) from any start: a seed cannot beat it, so it costs no FP64 residual
+            // relative) from any start: a seed cannot beat it, so it costs no residual
             const float tolf = (float)P.tol;
             float dprev = 0.0f;
             for (int step = 0;; step++) {
@@ -527,10 +599,10 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                 float dmaxf = 0.0f, xmaxf = 0.0f;
                 for (int t = lane; t < N * R; t += 32) {
                     const float d = xs[t];
-                    s.x[t] += widen(d);
+                    s.x[t] = df_add_f(s.x[t], d);
                     if (t / R < P.k) {
                         dmaxf = fmaxf(dmaxf, fabsf(d));
-                        xmaxf = fmaxf(xmaxf, fabsf(__double2float_rn(s.x[t])));
+                        xmaxf = fmaxf(xmaxf, fabsf(df_hi(s.x[t])));
                     }
                 }
 #pragma unroll
@@ -570,7 +642,7 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
         }
         if (lane == 0 && ok) atomicAdd(&P.counters[4], (unsigned long long)nres);
         if (accepted) {
-            WarpSmem w;
+            WarpSmem w;  // the polish left the weights in FP64
             w.cols = s.cols;
             scatter_row(P, e, w, lane, es, s.x, R, 1);
             if (lane == 0) {

@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
             __syncwarp();
             continue;
         }
-        assemble_packed(P, s, lane, es, pairs);
+        assemble_packed<false>(P, s, lane, es, pairs);  // FP64 entries: the residuals run in FP64
         LU L;
         const int ti = tri(lane);
 #pragma unroll
