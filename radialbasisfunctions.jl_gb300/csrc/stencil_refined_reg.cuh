@@ -542,7 +542,7 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
             // the same amplification would make visible, so this pass is FP64 (ten rows of k
             // products).  Only the k columns of P enter (the rows' other block is zero); the
             // rows share the warp's lanes in one pass.
-            auto polish = [&]() {
+            auto polish_rhs = [&]() {
                 const int k = P.k, nm = N - k;
                 for (int t = lane; t < k * R; t += 32) s.x[t] = df_unpack_double(s.x[t]);  // the weights
                 __syncwarp();
@@ -586,16 +586,21 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                     for (int q = 0; q < R; q++) rhs[r][q] = (i >= k && i < N) ? rbuf[(i < N ? i : 0) * R + q] : 0.0f;
                 }
                 __syncwarp();
-                reg_apply_inverse<N, R>(L, rhs, s.rowbuf, xs, lane);
-                for (int t = lane; t < k * R; t += 32) s.x[t] += widen(xs[t]);  // the weights, FP64
-                __syncwarp();
-            };
+            };  // the loop below applies the inverse to these right-hand sides and corrects the weights
             // the first solve leaves an error at the FP32 floor (about cond(A) * 2^-24
             // relative) from any start: a seed cannot beat it, so it costs no residual
+            // One call site of the product with the inverse serves the refinement steps and the
+            // polish (the kernel's code size sets its instruction-fetch stalls).
             const float tolf = (float)P.tol;
             float dprev = 0.0f;
+            bool polishing = false;
             for (int step = 0;; step++) {
                 reg_apply_inverse<N, R>(L, rhs, s.rowbuf, xs, lane);
+                if (polishing) {
+                    for (int t = lane; t < P.k * R; t += 32) s.x[t] += widen(xs[t]);  // the weights, FP64
+                    __syncwarp();
+                    break;
+                }
                 float dmaxf = 0.0f, xmaxf = 0.0f;
                 for (int t = lane; t < N * R; t += 32) {
                     const float d = xs[t];
@@ -631,8 +636,9 @@ __global__ void __launch_bounds__(128, reg_kernel_blocks(N)) build_refined_reg_k
                     if (dmaxf <= tolf * xmaxf && dmaxf <= 0.5f * dprev) {
                         accepted = true;
                         est_final = xmaxf > 0.0f ? (double)(dmaxf / xmaxf) : 0.0;
-                        polish();
-                        break;
+                        polish_rhs();
+                        polishing = true;
+                        continue;
                     }
                     dprev = dmaxf;
                 }

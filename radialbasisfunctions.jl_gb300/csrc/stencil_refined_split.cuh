@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
             // amplifies by sum |w| (~1/h^2).  The correction shrinks it by the same factor.  The
             // rows' zero block leaves k products per row; the rows share the warp's lanes in one
             // pass.
-            auto polish = [&]() {
+            auto polish_rhs = [&]() {
                 // lane (t, h): row k + t, column block h of c3 blocks (c3 lanes per row)
                 const int k = P.k, nm = N - k;
                 const int c3 = nm >= 32 ? 1 : 32 / nm, cw = (k + c3 - 1) / c3;
@@ -285,14 +285,19 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
                 rm = lane >= k ? s.xs[lane] : 0.0f;
                 rx = (xvalid && gx >= k) ? s.xs[gx] : 0.0f;
                 __syncwarp();
-                solve();
-                for (int t = lane; t < k; t += 32) s.x[t] += widen(s.xs[t]);  // the weights
-                __syncwarp();
-            };
+            };  // the loop below solves with these right-hand sides and corrects the weights
+            // One call site of the solve serves the refinement steps and the polish (the
+            // kernel's code size sets its instruction-fetch stalls).
             const float tolf = (float)P.tol;
             float dprev = 0.0f;
+            bool polishing = false;
             for (int step = 0;; step++) {
                 solve();
+                if (polishing) {
+                    for (int t = lane; t < P.k; t += 32) s.x[t] += widen(s.xs[t]);  // the weights
+                    __syncwarp();
+                    break;
+                }
                 float dmaxf = 0.0f, xmaxf = 0.0f;
                 for (int t = lane; t < N; t += 32) {
                     const float d = s.xs[t];
@@ -323,8 +328,9 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
                     if (dmaxf <= tolf * xmaxf && dmaxf <= 0.5f * dprev) {
                         accepted = true;
                         est_final = xmaxf > 0.0f ? (double)(dmaxf / xmaxf) : 0.0;
-                        polish();
-                        break;
+                        polish_rhs();
+                        polishing = true;
+                        continue;
                     }
                     dprev = dmaxf;
                 }
