@@ -187,6 +187,27 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
               const rbf_hermite *herm, const int64_t *row_ptr, int32_t *col, double *val,
               int8_t *status_out, rbf_build_stats *stats);
 
+/* A built operator whose device arrays the library allocated (rbf_build_csr): cfg->nops CSR
+ * matrices ne x ns sharing one structure, row_ptr[ne + 1], col[nnz] (columns ascending within
+ * each row) and val[op * nnz + p].  Release it with rbf_csr_free. */
+typedef struct rbf_csr {
+    int64_t ne, ns, nnz;
+    int32_t nops;
+    int64_t *row_ptr;
+    int32_t *col;
+    double *val;
+} rbf_csr;
+
+/* rbf_build_count, the allocation of the arrays on the context's device, and rbf_build in one
+ * call: the boundary in the form that returns its own sparse matrix, as _build_weights does
+ * (src/solve/api.jl:26-35, 167-196).  Arguments and status as rbf_build; on an error nothing
+ * stays allocated and *out is zeroed. */
+int rbf_build_csr(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns,
+                  const double *eval, int64_t ne, const int32_t *adjl, int32_t k,
+                  const rbf_hermite *herm, int8_t *status_out, rbf_build_stats *stats, rbf_csr *out);
+/* Frees the arrays of an rbf_build_csr result and zeroes *csr (a zeroed csr is a no-op). */
+int rbf_csr_free(rbf_ctx *ctx, rbf_csr *csr);
+
 /* Reverse-mode sensitivities of a build with respect to the point positions: given the
  * cotangent dW of the built values (val layout: dW[op * nnz + p], the row_ptr / column
  * order of the forward rbf_build with the same cfg->flags), writes ddata (ns x dim) and

@@ -106,6 +106,11 @@ class BuildStats(ctypes.Structure):
                 ("seed_rel_err_mean", ctypes.c_double)]
 
 
+class Csr(ctypes.Structure):
+    _fields_ = [("ne", ctypes.c_int64), ("ns", ctypes.c_int64), ("nnz", ctypes.c_int64), ("nops", ctypes.c_int32),
+                ("row_ptr", ctypes.c_void_p), ("col", ctypes.c_void_p), ("val", ctypes.c_void_p)]
+
+
 # exported entry points and their signatures (checked by the CPU tests against include/rbffd.h)
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -121,6 +126,8 @@ SIGNATURES = {
     "rbf_knn": (_I, [_P, _P, _I64, _P, _I64, _I32, _I32, _P]),
     "rbf_build_count": (_I, [_P, _I64, _I64, _I32, _P, _P, _P]),
     "rbf_build": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _I32, _P, _P, _P, _P, _P, _P]),
+    "rbf_build_csr": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _I32, _P, _P, _P, _P]),
+    "rbf_csr_free": (_I, [_P, _P]),
     "rbf_build_backward": (_I, [_P, _P, _P, _I64, _P, _I64, _P, _I32, _P, _P, _P, _P]),
     "rbf_interp_fit": (_I, [_P, _I32, _I32, _I32, _P, _I64, _P, _P]),
     "rbf_interp_eval": (_I, [_P, _I32, _I32, _I32, _P, _I64, _P, _P, _I64, _P]),

@@ -485,6 +485,60 @@ int rbf_build(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_
     return RBF_OK;
 }
 
+int rbf_csr_free(rbf_ctx *ctx, rbf_csr *csr) {
+    RBF_TRY(check_ctx(ctx));
+    if (!csr) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null csr");
+    RBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaError_t e = cudaSuccess;
+    for (void *p : {(void *)csr->row_ptr, (void *)csr->col, (void *)csr->val})
+        if (p) {
+            const cudaError_t f = cudaFree(p);
+            if (e == cudaSuccess) e = f;
+        }
+    *csr = rbf_csr{};
+    if (e != cudaSuccess) return rbf_fail(ctx, RBF_ERR_CUDA, "cudaFree: %s", cudaGetErrorString(e));
+    return RBF_OK;
+}
+
+int rbf_build_csr(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, int64_t ns, const double *eval,
+                  int64_t ne, const int32_t *adjl, int32_t k, const rbf_hermite *herm, int8_t *status_out,
+                  rbf_build_stats *stats, rbf_csr *out) {
+    RBF_TRY(check_ctx(ctx));
+    if (!cfg || !out) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "null configuration or output");
+    *out = rbf_csr{};
+    if (cfg->nops < 1 || cfg->nops > RBF_MAX_OPS)
+        return rbf_fail(ctx, RBF_ERR_ARGUMENT, "nops must be in 1..%d (got %d)", RBF_MAX_OPS, cfg->nops);
+    if (ne < 0) return rbf_fail(ctx, RBF_ERR_ARGUMENT, "invalid sizes");
+    RBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    rbf_csr c{};
+    c.ne = ne;
+    c.ns = ns;
+    c.nops = cfg->nops;
+    int st = RBF_OK;
+    if (cudaMalloc(&c.row_ptr, sizeof(int64_t) * (size_t)(ne + 1)) != cudaSuccess) {
+        c.row_ptr = nullptr;
+        st = rbf_fail(ctx, RBF_ERR_CUDA, "cudaMalloc of %lld row offsets failed", (long long)(ne + 1));
+    }
+    if (st == RBF_OK) st = rbf_build_count(ctx, ns, ne, k, herm, c.row_ptr, &c.nnz);
+    if (st == RBF_OK) {
+        const size_t nz = c.nnz > 0 ? (size_t)c.nnz : 1;
+        if (cudaMalloc(&c.col, sizeof(int32_t) * nz) != cudaSuccess) c.col = nullptr;
+        if (cudaMalloc(&c.val, sizeof(double) * nz * (size_t)cfg->nops) != cudaSuccess) c.val = nullptr;
+        if (!c.col || !c.val)
+            st = rbf_fail(ctx, RBF_ERR_CUDA, "cudaMalloc of %lld entries x %d operators failed", (long long)c.nnz,
+                          cfg->nops);
+    }
+    if (st == RBF_OK) st = rbf_build(ctx, cfg, data, ns, eval, ne, adjl, k, herm, c.row_ptr, c.col, c.val, status_out, stats);
+    if (st != RBF_OK) {
+        const std::string msg = ctx->last_error;  // the build's error, not the free's
+        rbf_csr_free(ctx, &c);
+        ctx->last_error = msg;
+        return st;
+    }
+    *out = c;
+    return RBF_OK;
+}
+
 int rbf_spmm(rbf_ctx *ctx, int64_t ne, int64_t ns, const int64_t *row_ptr, const int32_t *col, const double *val,
              int32_t nf, int32_t layout, const double *X, int64_t ldx, double alpha, double beta, double *Y,
              int64_t ldy) {

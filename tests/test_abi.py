@@ -48,7 +48,8 @@ def test_struct_layouts_match_header(lib):
     src = r'''
 #include <stdio.h>
 #include "rbffd.h"
-int main(void){printf("%zu %zu %zu\n", sizeof(rbf_build_cfg), sizeof(rbf_hermite), sizeof(rbf_build_stats));return 0;}
+int main(void){printf("%zu %zu %zu %zu\n", sizeof(rbf_build_cfg), sizeof(rbf_hermite), sizeof(rbf_build_stats),
+                      sizeof(rbf_csr));return 0;}
 '''
     with tempfile.TemporaryDirectory() as d:
         c = os.path.join(d, "t.c")
@@ -57,7 +58,8 @@ int main(void){printf("%zu %zu %zu\n", sizeof(rbf_build_cfg), sizeof(rbf_hermite
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
         sizes = list(map(int, subprocess.run([exe], capture_output=True, text=True).stdout.split()))
     n = pkg._native
-    assert sizes == [ctypes.sizeof(n.BuildCfg), ctypes.sizeof(n.Hermite), ctypes.sizeof(n.BuildStats)]
+    assert sizes == [ctypes.sizeof(n.BuildCfg), ctypes.sizeof(n.Hermite), ctypes.sizeof(n.BuildStats),
+                     ctypes.sizeof(n.Csr)]
 
 
 def test_version_without_gpu(lib):
