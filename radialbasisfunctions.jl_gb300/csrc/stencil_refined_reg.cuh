@@ -280,11 +280,11 @@ __device__ __forceinline__ void static_for(F &&f) {
 // is multiplied by its reciprocal pivot at the end).  Every step runs the same code, so the
 // loop stays rolled.  Afterwards the row pivoted at step c holds row c of the inverse, its
 // window position t the column of the row pivoted at step t.  rowbuf: two buffers of
-// 4 ceil(N/4) floats.  Returns false on a zero, subnormal or non-finite pivot.
+// 4 ceil(N/4) floats.  Returns false on a zero, subnormal or non-finite pivot (an entry of the
+// inverse that is not finite).
 template <int N, int R>
 __device__ bool reg_invert(RegLU<N, R> &L, float *rowbuf2, int lane) {
     constexpr int ROWS = RegLU<N, R>::ROWS, W4 = (N + 3) / 4;
-    bool ok = true;
     float rsc[ROWS];
 #pragma unroll
     for (int r = 0; r < ROWS; r++) rsc[r] = 1.0f;
@@ -315,10 +315,11 @@ __device__ bool reg_invert(RegLU<N, R> &L, float *rowbuf2, int lane) {
         }
         __syncwarp();
         const float pvt = rowbuf[0];
-        // approximate reciprocal (the FP32 inverse only preconditions the refinement)
+        // approximate reciprocal (the FP32 inverse only preconditions the refinement); a zero,
+        // subnormal (flushed) or non-finite pivot gives an infinite or NaN reciprocal, which
+        // reaches the inverse's entries: the check after the loop fails it
         float inv;
         asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(pvt));
-        ok &= (pvt != 0.0f) && isfinite(pvt) && isfinite(inv);
 #pragma unroll
         for (int r = 0; r < ROWS; r++) {
             const bool pr = brow == lane + 32 * r;
@@ -340,12 +341,15 @@ __device__ bool reg_invert(RegLU<N, R> &L, float *rowbuf2, int lane) {
             L.a[r][N - 1] = pr ? 1.0f : -m;
         }
     }
+    bool fin = true;
 #pragma unroll
     for (int r = 0; r < ROWS; r++)
 #pragma unroll
-        for (int j = 0; j < N; j++) L.a[r][j] *= rsc[r];
-    __syncwarp();
-    return ok;
+        for (int j = 0; j < N; j++) {
+            L.a[r][j] *= rsc[r];
+            fin &= isfinite(L.a[r][j]);
+        }
+    return __all_sync(0xffffffffu, fin);
 }
 
 // x = A32^{-1} rhs for the R right-hand sides held per row: every row puts its right-hand

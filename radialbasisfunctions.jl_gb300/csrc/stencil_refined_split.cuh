@@ -143,10 +143,10 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
             __syncwarp();
             const float pvt = rowbuf[0];
             // approximate reciprocal (the FP32 inverse only preconditions the refinement); a
-            // zero, subnormal or non-finite pivot fails the factorisation
+            // zero, subnormal (flushed) or non-finite pivot gives an infinite or NaN reciprocal,
+            // which reaches the inverse's entries: the check after the loop fails it
             float inv;
             asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(pvt));
-            ok &= (pvt != 0.0f) && isfinite(pvt) && isfinite(inv);
             if (pm) {
                 L.mstep = c;
                 rsc = inv;
@@ -178,17 +178,34 @@ __global__ void __launch_bounds__(128, 4) build_refined_split_kernel(StencilPara
                 const float mx = px ? 0.0f : mxs;
                 const float nxt = __shfl_down_sync(0xffffffffu, L.b[0], 1);
                 const float vn = rowbuf[q < 3 ? (q + 1) * PW : 0];
+                // the piece's pivot-row entries as aligned pairs (q * PW is even)
+                const float2 *const rb2 = reinterpret_cast<const float2 *>(rowbuf + q * PW);
+                float pr[PW];
 #pragma unroll
-                for (int t = 0; t + 1 < PW; t++) L.b[t] = fmaf(-mx, rowbuf[q * PW + t + 1], L.b[t + 1]);
+                for (int t = 0; t < PW / 2; t++) {
+                    const float2 v = rb2[t];
+                    pr[2 * t] = v.x;
+                    pr[2 * t + 1] = v.y;
+                }
+#pragma unroll
+                for (int t = 0; t + 1 < PW; t++) L.b[t] = fmaf(-mx, pr[t + 1], L.b[t + 1]);
                 L.b[PW - 1] = q < 3 ? fmaf(-mx, vn, nxt) : (px ? 1.0f : -mx);
             }
         }
-        // rows of the inverse: the unscaled pivot rows times their reciprocal pivots
+        // rows of the inverse: the unscaled pivot rows times their reciprocal pivots; the
+        // factorisation fails if any entry of the inverse is not finite
+        bool fin = true;
 #pragma unroll
-        for (int j = 0; j < N; j++) L.a[j] *= rsc;
+        for (int j = 0; j < N; j++) {
+            L.a[j] *= rsc;
+            fin &= isfinite(L.a[j]);
+        }
 #pragma unroll
-        for (int t = 0; t < PW; t++) L.b[t] *= xsc;
-        __syncwarp();
+        for (int t = 0; t < PW; t++) {
+            L.b[t] *= xsc;
+            fin &= isfinite(L.b[t]);
+        }
+        ok = __all_sync(0xffffffffu, fin);
 
         // ---- refinement: products with the FP32 inverse, FP64 residuals
         bool accepted = false;
