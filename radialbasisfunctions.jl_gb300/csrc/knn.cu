@@ -391,7 +391,10 @@ __device__ __forceinline__ void warp_sort_keys(float (&key)[SLOTS], int32_t (&ki
 // appended to the fallback list for the exact FP64 search.
 // Error bound of an FP32 distance (u = 2^-24, M the largest coordinate magnitude):
 // |d32 - d| <= 8u (M + d).
-template <int DIM, int SLOTS>
+// SLOTS: registers per lane of the sorted candidate list (32 SLOTS entries, room for the first
+// block's offered keys, kp .. 1.25 kp); XSLOTS: registers per lane of the exact re-rank of the
+// kp listed candidates (kp <= 32 XSLOTS).
+template <int DIM, int SLOTS, int XSLOTS>
 __global__ void __launch_bounds__(KNN_WARPS * 32, 4)  // 32 warps/SM: 64 registers
 knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__restrict__ sidx,
                 const int32_t *__restrict__ cstart, const double *__restrict__ data, const double *__restrict__ q,
@@ -686,10 +689,10 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
         }
 
         // exact keys of the kp candidates, then a transposition sort (they are nearly sorted)
-        unsigned long long xk[SLOTS];
-        int32_t xi[SLOTS];
+        unsigned long long xk[XSLOTS];
+        int32_t xi[XSLOTS];
 #pragma unroll
-        for (int s = 0; s < SLOTS; s++) {
+        for (int s = 0; s < XSLOTS; s++) {
             const int j = lane + 32 * s;
             xk[s] = ~0ull;
             xi[s] = 0x7fffffff;
@@ -706,20 +709,20 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                 xi[s] = kid[s];
             }
         }
-        for (int iter = 0; iter < 32 * SLOTS; iter++) {
+        for (int iter = 0; iter < 32 * XSLOTS; iter++) {
             bool swapped = false;
 #pragma unroll
             for (int phase = 0; phase < 2; phase++) {
                 // neighbours of every position, read before any position of this phase changes
-                unsigned long long up_k[SLOTS], dn_k[SLOTS];
-                int32_t up_i[SLOTS], dn_i[SLOTS];
+                unsigned long long up_k[XSLOTS], dn_k[XSLOTS];
+                int32_t up_i[XSLOTS], dn_i[XSLOTS];
 #pragma unroll
-                for (int s = 0; s < SLOTS; s++) {
+                for (int s = 0; s < XSLOTS; s++) {
                     up_k[s] = __shfl_down_sync(0xffffffffu, xk[s], 1);
                     up_i[s] = __shfl_down_sync(0xffffffffu, xi[s], 1);
                     dn_k[s] = __shfl_up_sync(0xffffffffu, xk[s], 1);
                     dn_i[s] = __shfl_up_sync(0xffffffffu, xi[s], 1);
-                    const int sn = s + 1 < SLOTS ? s + 1 : s;
+                    const int sn = s + 1 < XSLOTS ? s + 1 : s;
                     const int spv = s > 0 ? s - 1 : 0;
                     unsigned long long nx_k = __shfl_sync(0xffffffffu, xk[sn], 0);
                     int32_t nx_i = __shfl_sync(0xffffffffu, xi[sn], 0);
@@ -735,10 +738,10 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                     }
                 }
 #pragma unroll
-                for (int s = 0; s < SLOTS; s++) {
+                for (int s = 0; s < XSLOTS; s++) {
                     const int j = lane + 32 * s;
                     const bool low = ((j & 1) == phase);  // j pairs with j+1, else with j-1
-                    if (low && j < 32 * SLOTS - 1) {
+                    if (low && j < 32 * XSLOTS - 1) {
                         if (xkey_less(up_k[s], up_i[s], xk[s], xi[s])) {
                             xk[s] = up_k[s];
                             xi[s] = up_i[s];
@@ -760,7 +763,7 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
         if ((int64_t)kp < ns) {
             unsigned long long kk = xk[0];
 #pragma unroll
-            for (int s = 1; s < SLOTS; s++)
+            for (int s = 1; s < XSLOTS; s++)
                 if (s == ((k - 1) >> 5)) kk = xk[s];
             kk = __shfl_sync(0xffffffffu, kk, (k - 1) & 31);
             // exact k-th squared distance rounded up vs the squared lower bound of any unlisted
@@ -773,7 +776,7 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
         }
         if (certified) {
 #pragma unroll
-            for (int s = 0; s < SLOTS; s++) {
+            for (int s = 0; s < XSLOTS; s++) {
                 const int j = lane + 32 * s;
                 if (j < k) out[(int64_t)qi * k + j] = xi[s];
             }
@@ -901,19 +904,26 @@ int knn_dim(rbf_ctx *ctx, const double *d_data, int64_t ns, const double *d_eval
     int64_t cap = (int64_t)ctx->num_sms * 32;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    // FP32 search with an exact FP64 re-sort of k + 8 candidates; queries whose FP32
-    // margins do not certify the exact order go to the FP64 search below
-    const int kp = std::min(k + 8, 64);
+    // FP32 search with an exact FP64 re-sort of kp candidates: k + 8, or 32 for 25 <= k <= 30 so
+    // that the re-rank fits one register per lane (a margin of at least two neighbours, whose
+    // distances differ by far more than the FP32 error bound except at near-ties); queries
+    // whose FP32 margins do not certify the exact order go to the FP64 search below
+    const int kp = (k >= 25 && k <= 30) ? 32 : std::min(k + 8, 64);
     float mag = 0.f;
     for (int d = 0; d < DIM; d++) mag = std::max(mag, (float)std::max(std::fabs(lo[d]), std::fabs(hi[d])));
     RBF_TRY(fb.alloc(ctx, sizeof(int32_t) * (ne + 1)));
     RBF_CUDA(ctx, cudaMemsetAsync(fb.as<int32_t>() + ne, 0, sizeof(int32_t), ctx->stream));
-    if (kp <= 32)
-        knn_fast_kernel<DIM, 1><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
+    // list of 32 SLOTS entries, re-rank of kp in 32 XSLOTS (k + 8 <= 32: one register each)
+    if (k + 8 <= 32)
+        knn_fast_kernel<DIM, 1, 1><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
+            g, sp32.as<float4>(), sidx.as<int32_t>(), start.as<int32_t>(), d_data, d_eval, qorder.as<int32_t>(), ne,
+            k, kp, R0, mag, ns, d_idx, fb.as<int32_t>(), fb.as<int32_t>() + ne);
+    else if (kp <= 32)
+        knn_fast_kernel<DIM, 2, 1><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
             g, sp32.as<float4>(), sidx.as<int32_t>(), start.as<int32_t>(), d_data, d_eval, qorder.as<int32_t>(), ne,
             k, kp, R0, mag, ns, d_idx, fb.as<int32_t>(), fb.as<int32_t>() + ne);
     else
-        knn_fast_kernel<DIM, 2><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
+        knn_fast_kernel<DIM, 2, 2><<<(unsigned)blocks, KNN_WARPS * 32, 0, ctx->stream>>>(
             g, sp32.as<float4>(), sidx.as<int32_t>(), start.as<int32_t>(), d_data, d_eval, qorder.as<int32_t>(), ne,
             k, kp, R0, mag, ns, d_idx, fb.as<int32_t>(), fb.as<int32_t>() + ne);
     RBF_CHECK_LAUNCH(ctx);
