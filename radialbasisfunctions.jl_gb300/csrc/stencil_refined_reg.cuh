@@ -104,7 +104,8 @@ __device__ __forceinline__ float dfsum_value(DfSum a) { return a.s + a.c; }
 // and its nops right-hand sides (n x nops), both double-float (df_pack), FP64 local
 // coordinates and column indices, the double-float solution (n x nops; the weights are
 // unpacked to FP64 in place before the scatter), FP32 increments (n x nops), split
-// coordinates, pivots, reciprocal pivots and two pivot-row buffers (16-byte aligned,
+// coordinates (hi and lo parts, four floats per point, 16-byte aligned: one vector load per
+// point), pivots, reciprocal pivots and two pivot-row buffers (16-byte aligned,
 // 4 * ceil(n/4) floats each), which the solves reuse for the right-hand sides in pivot order.
 struct SplitSmem {
     double *Mp, *bv, *X, *x;
@@ -114,7 +115,9 @@ struct SplitSmem {
 
 __host__ __device__ inline size_t split_smem_bytes(int n, int k, int nops = 1) {
     size_t b = sizeof(double) * ((size_t)tri(n) + 2 * (size_t)n * nops + 3 * (size_t)k);
-    b += sizeof(int) * ((size_t)k + n) + sizeof(float) * ((size_t)n * nops + 6 * (size_t)k + n);
+    b += sizeof(int) * ((size_t)k + n) + sizeof(float) * (size_t)n * nops;
+    b = (b + 15) & ~(size_t)15;
+    b += sizeof(float) * (8 * (size_t)k + n);  // split coordinates (2 x 4 per point), reciprocal pivots
     b = (b + 15) & ~(size_t)15;
     // two pivot-row buffers, alternating by step; after the inversion the right-hand sides
     // in pivot order (n x nops)
@@ -133,10 +136,11 @@ __device__ inline SplitSmem carve_split(char *base, int n, int k, int nops = 1) 
     s.cols = reinterpret_cast<int *>(s.x + (size_t)n * nops);
     s.piv = s.cols + k;
     s.xs = reinterpret_cast<float *>(s.piv + n);
-    s.XH = s.xs + (size_t)n * nops;
-    s.XL = s.XH + 3 * k;
-    s.rcp = s.XL + 3 * k;
-    size_t o = (size_t)(reinterpret_cast<char *>(s.rcp + n) - base);
+    size_t o = (size_t)(reinterpret_cast<char *>(s.xs + (size_t)n * nops) - base);
+    s.XH = reinterpret_cast<float *>(base + ((o + 15) & ~(size_t)15));
+    s.XL = s.XH + 4 * k;
+    s.rcp = s.XL + 4 * k;
+    o = (size_t)(reinterpret_cast<char *>(s.rcp + n) - base);
     s.rowbuf = reinterpret_cast<float *>(base + ((o + 15) & ~(size_t)15));
     return s;
 }
@@ -189,8 +193,8 @@ __device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int 
         for (int d = 0; d < 3; d++) {
             const double xv = d < dim ? s.X[i * 3 + d] : 0.0;
             const float hi = d2f_rn_bits(xv);
-            s.XH[i * 3 + d] = hi;
-            s.XL[i * 3 + d] = d2f_rn_bits(xv - widen(hi));
+            s.XH[i * 4 + d] = hi;
+            s.XL[i * 4 + d] = d2f_rn_bits(xv - widen(hi));
         }
     for (int t = lane; t < tri(n) - tri(k); t += 32) s.Mp[tri(k) + t] = 0.0;  // rows k..n-1; the
     __syncwarp();                                                           // P^T part is set below
@@ -200,12 +204,18 @@ __device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int 
     for (int p = lane; p < npairs; p += 32) {
         const unsigned pk = pairs[p];
         const int i = (int)(pk & 0xffu), j = (int)(pk >> 8);  // i < j
+        const float4 hi4 = reinterpret_cast<const float4 *>(s.XH)[i], hj4 = reinterpret_cast<const float4 *>(s.XH)[j];
+        const float4 li4 = reinterpret_cast<const float4 *>(s.XL)[i], lj4 = reinterpret_cast<const float4 *>(s.XL)[j];
+        const float hi[3] = {hi4.x, hi4.y, hi4.z}, hj[3] = {hj4.x, hj4.y, hj4.z};
+        const float li[3] = {li4.x, li4.y, li4.z}, lj[3] = {lj4.x, lj4.y, lj4.z};
         dfl r2 = {0.0f, 0.0f};
-        for (int d = 0; d < dim; d++) {
-            dfl dd = ts(s.XH[i * 3 + d], -s.XH[j * 3 + d]);
-            dd = qts(dd.hi, dd.lo + (s.XL[i * 3 + d] - s.XL[j * 3 + d]));
-            r2 = df_add(r2, df_sqr(dd));
-        }
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+            if (d < dim) {
+                dfl dd = ts(hi[d], -hj[d]);
+                dd = qts(dd.hi, dd.lo + (li[d] - lj[d]));
+                r2 = df_add(r2, df_sqr(dd));
+            }
         const dfl r = df_sqrt(r2);
         dfl phi;
         switch (P.phs) {
@@ -219,7 +229,7 @@ __device__ void assemble_packed(const StencilParams &P, const SplitSmem &s, int 
     const AvoidInf<double> AI = avoid_inf_scaled<double>(es);
     for (int i = lane; i < k; i += 32) {
         dfl xd[3];
-        for (int d = 0; d < 3; d++) xd[d] = {s.XH[i * 3 + d], s.XL[i * 3 + d]};
+        for (int d = 0; d < 3; d++) xd[d] = {s.XH[i * 4 + d], s.XL[i * 4 + d]};
         for (int m = 0; m < nmon; m++) {
             dfl v = {1.0f, 0.0f};
             for (int d = 0; d < dim; d++)
