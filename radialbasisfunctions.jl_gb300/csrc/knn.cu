@@ -503,14 +503,8 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                 const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
                 __syncwarp();
                 // FP32 key and point index of flattened candidate f < total
-                auto cand = [&](int32_t f, float &dd, int32_t &id) {
-                    int lo = 0, hi = KNN_RANGES - 1;
-                    while (lo < hi) {
-                        int mid = (lo + hi + 1) >> 1;
-                        if (my_off[mid] <= f) lo = mid;
-                        else hi = mid - 1;
-                    }
-                    int32_t p = my_start[lo] + (f - my_off[lo]);
+                // FP32 key and point index of the candidate in point slot p
+                auto cand_at = [&](int32_t p, float &dd, int32_t &id) {
                     float4 c4 = __ldg(&sp32[p]);
                     float dx = c4.x - qf[0];
                     dd = dx * dx;
@@ -523,6 +517,16 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                         dd = fmaf(dz, dz, dd);
                     }
                     id = __ldg(&sidx[p]);
+                };
+                // ... of flattened candidate f < total: its cell run by bisection over the offsets
+                auto cand = [&](int32_t f, float &dd, int32_t &id) {
+                    int lo = 0, hi = KNN_RANGES - 1;
+                    while (lo < hi) {
+                        int mid = (lo + hi + 1) >> 1;
+                        if (my_off[mid] <= f) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    cand_at(my_start[lo] + (f - my_off[lo]), dd, id);
                 };
                 // the passing candidates of the warp, one at a time, into the sorted list
                 auto insert_passing = [&](float dd, int32_t id, bool pass) {
@@ -579,6 +583,12 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                     // threshold t with at least kp keys <= t (found by bisection, aiming at
                     // kp .. 1.25 kp): only keys <= t can be among the kp best, so only they
                     // are offered to the list (about kp insertions instead of ~2.8 kp)
+                    // every lane owns one row's run here (nrows <= 32, r_in < 0: no second run):
+                    // it writes the point slots of its candidates, so that each candidate is
+                    // one shared load away instead of a bisection over the run offsets; the
+                    // table then holds the point indices
+                    for (int32_t t = 0; t < l0; t++) my_cid[excl + t] = a0 + t;
+                    __syncwarp();
                     float bk[8];
                     float kmax = 0.0f;
 #pragma unroll
@@ -587,7 +597,7 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                         bk[r] = INFINITY;
                         if (f < total) {
                             int32_t id;
-                            cand(f, bk[r], id);
+                            cand_at(my_cid[f], bk[r], id);
                             my_cid[f] = id;
                             kmax = fmaxf(kmax, bk[r]);
                         }
