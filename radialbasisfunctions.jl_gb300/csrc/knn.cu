@@ -347,34 +347,31 @@ __device__ __forceinline__ bool xkey_less(unsigned long long d1, int32_t i1, uns
 }
 
 // Bitonic sort of the 32 * SLOTS (FP32 key, index) pairs of a warp, ascending (element
-// j = lane + 32 s): strides below 32 by shuffles, stride 32 between a lane's registers.
+// j = lane + 32 s): strides below 32 by shuffles, stride 32 between a lane's registers.  A
+// pair is packed as (key bits << 32) | index: the keys are squared distances (+0 or positive,
+// never NaN), whose bit patterns order as unsigned integers, so the packed order is the
+// (key, index) order of fkey_less and every compare-exchange is one 64-bit shuffle, one
+// unsigned comparison and one select.
 template <int SLOTS>
-__device__ __forceinline__ void warp_sort_keys(float (&key)[SLOTS], int32_t (&kid)[SLOTS], int lane) {
+__device__ __forceinline__ void warp_sort_packed(unsigned long long (&v)[SLOTS], int lane) {
 #pragma unroll
     for (int size = 2; size <= 32 * SLOTS; size <<= 1) {
 #pragma unroll
         for (int stride = size / 2; stride > 0; stride >>= 1) {
             if (stride >= 32) {
                 if constexpr (SLOTS > 1) {
-                    if (fkey_less(key[SLOTS - 1], kid[SLOTS - 1], key[0], kid[0])) {
-                        const float tk = key[0];
-                        const int32_t ti = kid[0];
-                        key[0] = key[SLOTS - 1];
-                        kid[0] = kid[SLOTS - 1];
-                        key[SLOTS - 1] = tk;
-                        kid[SLOTS - 1] = ti;
-                    }
+                    const bool sw = v[SLOTS - 1] < v[0];
+                    const unsigned long long lo = sw ? v[SLOTS - 1] : v[0], hi = sw ? v[0] : v[SLOTS - 1];
+                    v[0] = lo;
+                    v[SLOTS - 1] = hi;
                 }
             } else {
 #pragma unroll
                 for (int s = 0; s < SLOTS; s++) {
                     const int e = lane + 32 * s;
-                    const float ok = __shfl_xor_sync(0xffffffffu, key[s], stride);
-                    const int32_t oi = __shfl_xor_sync(0xffffffffu, kid[s], stride);
+                    const unsigned long long o = __shfl_xor_sync(0xffffffffu, v[s], stride);
                     const bool keep_min = ((e & size) == 0) == ((e & stride) == 0);
-                    const bool take = keep_min ? fkey_less(ok, oi, key[s], kid[s]) : fkey_less(key[s], kid[s], ok, oi);
-                    key[s] = take ? ok : key[s];
-                    kid[s] = take ? oi : kid[s];
+                    v[s] = (keep_min == (o < v[s])) ? o : v[s];
                 }
             }
         }
@@ -403,8 +400,7 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
     __shared__ int32_t s_start[KNN_WARPS][KNN_RANGES];
     __shared__ int32_t s_off[KNN_WARPS][KNN_RANGES + 1];
     __shared__ int32_t s_cid[KNN_WARPS][256];
-    __shared__ float s_lk[KNN_WARPS][32 * SLOTS];
-    __shared__ int32_t s_li[KNN_WARPS][32 * SLOTS];
+    __shared__ unsigned long long s_lv[KNN_WARPS][32 * SLOTS];  // offered (key, index), packed
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t warp0 = (int64_t)blockIdx.x * KNN_WARPS + wib;
     const int64_t nwarps = (int64_t)gridDim.x * KNN_WARPS;
@@ -628,21 +624,24 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                         const bool offer = f < total && bk[r] <= hi_t;
                         const unsigned m = __ballot_sync(0xffffffffu, offer);
                         const int32_t pos = nof + __popc(m & ((1u << lane) - 1u));
-                        if (offer && pos < 32 * SLOTS) {
-                            s_lk[wib][pos] = bk[r];
-                            s_li[wib][pos] = my_cid[f];
-                        }
+                        if (offer && pos < 32 * SLOTS)
+                            s_lv[wib][pos] = ((unsigned long long)__float_as_uint(bk[r]) << 32) | (unsigned)my_cid[f];
                         nof += __popc(m);
                     }
                     __syncwarp();
                     if (nof <= 32 * SLOTS) {
+                        unsigned long long pv[SLOTS];
 #pragma unroll
                         for (int s = 0; s < SLOTS; s++) {
                             const int j = lane + 32 * s;
-                            key[s] = j < nof ? s_lk[wib][j] : INFINITY;
-                            kid[s] = j < nof ? s_li[wib][j] : 0x7fffffff;
+                            pv[s] = j < nof ? s_lv[wib][j] : 0x7f8000007fffffffull;  // (+inf, 0x7fffffff)
                         }
-                        warp_sort_keys<SLOTS>(key, kid, lane);
+                        warp_sort_packed<SLOTS>(pv, lane);
+#pragma unroll
+                        for (int s = 0; s < SLOTS; s++) {
+                            key[s] = __uint_as_float((unsigned)(pv[s] >> 32));
+                            kid[s] = (int32_t)(unsigned)pv[s];
+                        }
                         float kv = key[0];
                         int32_t ki = kid[0];
 #pragma unroll
