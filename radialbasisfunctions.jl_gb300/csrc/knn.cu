@@ -499,8 +499,8 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                 const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
                 __syncwarp();
                 // FP32 key and point index of flattened candidate f < total
-                // FP32 key and point index of the candidate in point slot p
-                auto cand_at = [&](int32_t p, float &dd, int32_t &id) {
+                // FP32 key of the candidate in point slot p
+                auto key_at = [&](int32_t p, float &dd) {
                     float4 c4 = __ldg(&sp32[p]);
                     float dx = c4.x - qf[0];
                     dd = dx * dx;
@@ -512,6 +512,10 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                         float dz = c4.z - qf[2];
                         dd = fmaf(dz, dz, dd);
                     }
+                };
+                // ... and its point index
+                auto cand_at = [&](int32_t p, float &dd, int32_t &id) {
+                    key_at(p, dd);
                     id = __ldg(&sidx[p]);
                 };
                 // ... of flattened candidate f < total: its cell run by bisection over the offsets
@@ -581,8 +585,8 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                     // are offered to the list (about kp insertions instead of ~2.8 kp)
                     // every lane owns one row's run here (nrows <= 32, r_in < 0: no second run):
                     // it writes the point slots of its candidates, so that each candidate is
-                    // one shared load away instead of a bisection over the run offsets; the
-                    // table then holds the point indices
+                    // one shared load away instead of a bisection over the run offsets; only
+                    // the offered candidates' point indices are read
                     for (int32_t t = 0; t < l0; t++) my_cid[excl + t] = a0 + t;
                     __syncwarp();
                     float bk[8];
@@ -592,9 +596,7 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                         const int32_t f = r * 32 + lane;
                         bk[r] = INFINITY;
                         if (f < total) {
-                            int32_t id;
-                            cand_at(my_cid[f], bk[r], id);
-                            my_cid[f] = id;
+                            key_at(my_cid[f], bk[r]);
                             kmax = fmaxf(kmax, bk[r]);
                         }
                     }
@@ -625,7 +627,8 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                         const unsigned m = __ballot_sync(0xffffffffu, offer);
                         const int32_t pos = nof + __popc(m & ((1u << lane) - 1u));
                         if (offer && pos < 32 * SLOTS)
-                            s_lv[wib][pos] = ((unsigned long long)__float_as_uint(bk[r]) << 32) | (unsigned)my_cid[f];
+                            s_lv[wib][pos] = ((unsigned long long)__float_as_uint(bk[r]) << 32) |
+                                             (unsigned)__ldg(&sidx[my_cid[f]]);
                         nof += __popc(m);
                     }
                     __syncwarp();
@@ -657,7 +660,7 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                         for (int r = 0; r < 8; r++) {
                             const int32_t f = r * 32 + lane;
                             const bool offer = f < total && bk[r] <= hi_t;
-                            const int32_t id = offer ? my_cid[f] : 0x7fffffff;
+                            const int32_t id = offer ? __ldg(&sidx[my_cid[f]]) : 0x7fffffff;
                             insert_passing(bk[r], id, offer && fkey_less(bk[r], id, kth, kth_id));
                         }
                     }
@@ -731,19 +734,21 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                     up_i[s] = __shfl_down_sync(0xffffffffu, xi[s], 1);
                     dn_k[s] = __shfl_up_sync(0xffffffffu, xk[s], 1);
                     dn_i[s] = __shfl_up_sync(0xffffffffu, xi[s], 1);
-                    const int sn = s + 1 < XSLOTS ? s + 1 : s;
-                    const int spv = s > 0 ? s - 1 : 0;
-                    unsigned long long nx_k = __shfl_sync(0xffffffffu, xk[sn], 0);
-                    int32_t nx_i = __shfl_sync(0xffffffffu, xi[sn], 0);
-                    unsigned long long pv_k = __shfl_sync(0xffffffffu, xk[spv], 31);
-                    int32_t pv_i = __shfl_sync(0xffffffffu, xi[spv], 31);
-                    if (lane == 31) {
-                        up_k[s] = nx_k;
-                        up_i[s] = nx_i;
-                    }
-                    if (lane == 0) {
-                        dn_k[s] = pv_k;
-                        dn_i[s] = pv_i;
+                    if constexpr (XSLOTS > 1) {  // neighbours across the slots' boundary
+                        const int sn = s + 1 < XSLOTS ? s + 1 : s;
+                        const int spv = s > 0 ? s - 1 : 0;
+                        unsigned long long nx_k = __shfl_sync(0xffffffffu, xk[sn], 0);
+                        int32_t nx_i = __shfl_sync(0xffffffffu, xi[sn], 0);
+                        unsigned long long pv_k = __shfl_sync(0xffffffffu, xk[spv], 31);
+                        int32_t pv_i = __shfl_sync(0xffffffffu, xi[spv], 31);
+                        if (lane == 31) {
+                            up_k[s] = nx_k;
+                            up_i[s] = nx_i;
+                        }
+                        if (lane == 0) {
+                            dn_k[s] = pv_k;
+                            dn_i[s] = pv_i;
+                        }
                     }
                 }
 #pragma unroll
