@@ -457,8 +457,15 @@ knn_fast_kernel(GridDesc g, const float4 *__restrict__ sp32, const int32_t *__re
                 int32_t a0 = 0, l0 = 0, a1 = 0, l1 = 0;
                 if (row < nrows) {
                     int dy = 0, dz = 0;
-                    if (DIM >= 2) dy = (row % side) - R;
-                    if (DIM == 3) dz = (row / side) - R;
+                    if (DIM == 2) dy = row - R;  // row < nrows = side
+                    if (DIM == 3) {
+                        // row / side without an integer division: (row + 1/2) / side is at least
+                        // 1/(2 side) from an integer, the FP32 quotient (2 ulp) within 2e-4 of it
+                        // for side <= 512
+                        const int zq = side <= 512 ? (int)__fdividef((float)row + 0.5f, (float)side) : row / side;
+                        dy = row - zq * side - R;
+                        dz = zq - R;
+                    }
                     int cy = qc[1] + dy, cz = qc[2] + dz;
                     bool inside = (DIM < 2 || (cy >= 0 && cy < g.nc[1])) && (DIM < 3 || (cz >= 0 && cz < g.nc[2]));
                     if (inside) {
