@@ -981,12 +981,12 @@ def main():
             "frac": ach / fp64_peak.value, "traffic": tps * n if tps else None,
             "flops": f"reference FP64 algorithm count per stencil ({flops_stencil:.0f}: n^3/3 + 2n^2R + assembly)",
             "peak_source": "FP64 FMA loop measured in this run (rbf_diag_fma_peak)",
-            "fp32_pipe": {"peak": fp32_peak.value, "frac": ach / fp32_peak.value},
             "traffic_source": "ncu dram__bytes_read+write of the same kernel on a 1M-point case, scaled by stencils"
                               if tps else "not captured",
             "note": "frac: the reference's FP64 algorithm (its FLOP count) at the measured FP64 peak, i.e. the "
                     "speed of light of a plain FP64 build; above 1 because this kernel factorises on the FP32 pipe "
-                    "and spends its FP64 pipe on the residuals (fp64_residual_work below)",
+                    "and spends its FP64 pipe on the residuals (fp64_residual_work below); the kernel itself is "
+                    "bound by instruction issue and latency, not by one pipe",
             "fp64_residual_work": {"fma_per_s": res_fma / (ms_kernel * 1e-3),
                                    "frac_of_fp64_fma_rate": res_fma / (ms_kernel * 1e-3) / (fp64_peak.value * 0.5e12),
                                    "count": "FP64 residuals counted by the build x n^2 R FMAs"}}
