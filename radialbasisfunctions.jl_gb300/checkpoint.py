@@ -11,10 +11,18 @@ only: they can be applied but not rebuilt after resume."""
 from __future__ import annotations
 
 import json
+import os
 
 import numpy as np
 
 FORMAT = "rbffd-gb300-operator-1"
+
+
+def _npz(path):
+    """The file name numpy writes for path: np.savez appends .npz to a name without it, and
+    np.load does not, so both directions use the completed name."""
+    p = os.fspath(path)
+    return p if p.endswith(".npz") else p + ".npz"
 
 
 def _op_spec(L):
@@ -58,14 +66,14 @@ def _host(t):
 
 def save_weights(path, W):
     """One CSR operator (WeightsCSR) to an .npz file."""
-    np.savez(path, format=FORMAT, row_ptr=_host(W.row_ptr), col=_host(W.col), val=_host(W.val),
+    np.savez(_npz(path), format=FORMAT, row_ptr=_host(W.row_ptr), col=_host(W.col), val=_host(W.val),
              shape=np.asarray(W.shape, dtype=np.int64))
 
 
 def load_weights(path, ctx=None):
     """A WeightsCSR from save_weights, on the context's GPU."""
     from . import Context, WeightsCSR, _torch
-    z = np.load(path, allow_pickle=False)
+    z = np.load(_npz(path), allow_pickle=False)
     if str(z["format"]) != FORMAT:
         raise ValueError(f"{path}: not an operator checkpoint of this library (format {z['format']})")
     ctx = ctx or Context.default()
@@ -94,13 +102,13 @@ def save_operator(path, op):
             "precision": op.precision, "tuple": isinstance(op.weights, tuple), "nweights": len(ws),
             "valid_cache": bool(op.valid_cache)}
     arrays["meta"] = json.dumps(meta)
-    np.savez(path, **arrays)
+    np.savez(_npz(path), **arrays)
 
 
 def load_operator(path, ctx=None):
     """Resume a RadialBasisOperator from save_operator without rebuilding its weights."""
     from . import PHS, BoundaryCondition, Context, RadialBasisOperator, WeightsCSR, _torch
-    z = np.load(path, allow_pickle=False)
+    z = np.load(_npz(path), allow_pickle=False)
     if str(z["format"]) != FORMAT:
         raise ValueError(f"{path}: not an operator checkpoint of this library (format {z['format']})")
     meta = json.loads(str(z["meta"]))

@@ -243,7 +243,7 @@ def save_surrogate(path, model, progress=None):
         if progress.get("rng") is not None:
             arrays["rng"] = progress["rng"].cpu().numpy()
     arrays["meta"] = json.dumps(meta)
-    np.savez(path, **arrays)
+    np.savez(path if str(path).endswith(".npz") else str(path) + ".npz", **arrays)
 
 
 def load_surrogate(path, ctx=None, return_progress=False):
@@ -252,7 +252,7 @@ def load_surrogate(path, ctx=None, return_progress=False):
 
     import numpy as np
     torch = _torch()
-    z = np.load(path, allow_pickle=False)
+    z = np.load(path if str(path).endswith(".npz") else str(path) + ".npz", allow_pickle=False)
     if "format" not in z.files or str(z["format"]) != SURROGATE_FORMAT:
         raise ValueError(f"{path}: not a surrogate checkpoint of this library")
     meta = json.loads(str(z["meta"]))

@@ -64,3 +64,17 @@ def test_load_rejects_foreign_file(pkg, tmp_path):
         pkg.load_operator(p)
     with pytest.raises(ValueError, match="not an operator checkpoint"):
         pkg.load_weights(p)
+
+
+def test_path_without_extension(pkg, tmp_path):
+    """np.savez appends .npz to a bare name; saving and loading under the same bare name meet."""
+    op = fake_operator(pkg, pkg.Laplacian(), 1)
+    bare = tmp_path / "lap"
+    pkg.save_operator(bare, op)
+    assert (tmp_path / "lap.npz").exists()
+    z = np.load(str(bare) + ".npz", allow_pickle=False)
+    assert np.array_equal(z["w0_val"], op.weights.val)
+    np.savez(tmp_path / "foreign", format="something-else", meta="{}")
+    with pytest.raises(ValueError, match="not an operator checkpoint"):
+        pkg.load_operator(tmp_path / "foreign")  # found under its completed name, then rejected
+
