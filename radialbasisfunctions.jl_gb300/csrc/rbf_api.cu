@@ -515,8 +515,11 @@ int rbf_build_csr(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, in
     c.ns = ns;
     c.nops = cfg->nops;
     int st = RBF_OK;
+    // a failed allocation's error is cleared (cudaGetLastError), so that the next launch check
+    // does not report it as its own
     if (cudaMalloc(&c.row_ptr, sizeof(int64_t) * (size_t)(ne + 1)) != cudaSuccess) {
         c.row_ptr = nullptr;
+        cudaGetLastError();
         st = rbf_fail(ctx, RBF_ERR_CUDA, "cudaMalloc of %lld row offsets failed", (long long)(ne + 1));
     }
     if (st == RBF_OK) st = rbf_build_count(ctx, ns, ne, k, herm, c.row_ptr, &c.nnz);
@@ -524,9 +527,11 @@ int rbf_build_csr(rbf_ctx *ctx, const rbf_build_cfg *cfg, const double *data, in
         const size_t nz = c.nnz > 0 ? (size_t)c.nnz : 1;
         if (cudaMalloc(&c.col, sizeof(int32_t) * nz) != cudaSuccess) c.col = nullptr;
         if (cudaMalloc(&c.val, sizeof(double) * nz * (size_t)cfg->nops) != cudaSuccess) c.val = nullptr;
-        if (!c.col || !c.val)
+        if (!c.col || !c.val) {
+            cudaGetLastError();
             st = rbf_fail(ctx, RBF_ERR_CUDA, "cudaMalloc of %lld entries x %d operators failed", (long long)c.nnz,
                           cfg->nops);
+        }
     }
     if (st == RBF_OK) st = rbf_build(ctx, cfg, data, ns, eval, ne, adjl, k, herm, c.row_ptr, c.col, c.val, status_out, stats);
     if (st != RBF_OK) {
