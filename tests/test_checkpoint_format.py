@@ -78,3 +78,22 @@ def test_path_without_extension(pkg, tmp_path):
     with pytest.raises(ValueError, match="not an operator checkpoint"):
         pkg.load_operator(tmp_path / "foreign")  # found under its completed name, then rejected
 
+
+
+def test_operator_kinds_round_trip(pkg):
+    """Every operator kind the front ends build is stored by kind and parameters and restored to
+    the same kind, parameters and right-hand sides (what update_weights rebuilds from)."""
+    from importlib import import_module
+    ck = import_module(pkg.__name__ + ".checkpoint")
+    kinds = [pkg.Laplacian(), pkg.Partial(1, 2), pkg.Partial(2, 3), pkg.Jacobian(3), pkg.Regrid(),
+             pkg.Operators(pkg.Jacobian(), pkg.Laplacian())]
+    for L in kinds:
+        spec = ck._op_spec(L)
+        R = ck._op_from_spec(spec)
+        assert type(R) is type(L) and ck._op_spec(R) == spec
+        assert R.ops(3) == L.ops(3)
+    v = np.array([0.6, 0.8, 0.0])
+    D = ck._op_from_spec(ck._op_spec(pkg.Directional(v)), v)
+    assert isinstance(D, pkg.Directional) and np.array_equal(D.v, v) and D.ops(3) == pkg.Directional(v).ops(3)
+    C = ck._op_from_spec({"kind": "derived", "desc": "2.0 * Laplacian (∇²f)", "rank": 0})
+    assert repr(C) == "2.0 * Laplacian (∇²f)" and C.rank == 0
